@@ -1,0 +1,340 @@
+"""Benchmark of the render path on GB300.
+
+Workload (one step = one frame): the 1M-triangle sphere field at 1920x1080 —
+256 UV spheres of 3,906 triangles (999,936 in all), 4 Blinn-Phong materials,
+one point and one directional light both casting 2048^2 shadow maps, AO on,
+sRGB gamma. Metric: Mtri/s = input triangles per second of frame time.
+
+  value  frames rendered with the scene resident in HBM (pr_render_async into
+         device outputs), CUDA events on the library's stream
+  e2e    the same through the public C ABI with host buffers: every step
+         uploads the triangle soup from pinned host memory (pr_scene_upload)
+         and reads back RGBA8 + triangle IDs + depth (pr_render)
+  --impl reference  the CPU restatement of the reference renderer (oracle/),
+         all host threads, single-worker draw order
+
+Multi-GPU: frames do not shard (one view); N ranks render N independent
+replicas (weak scaling), the value is the total over ranks.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRIS = 999_936
+W, H = 1920, 1080
+SHADOW = (2048, 2048)
+
+
+def workload():
+    from polyred_gb300 import procedural
+    return procedural.sphere_field(width=W, height=H)
+
+
+def frame_opts(scene, cam):
+    return dict(width=W, height=H, camera=cam, scene=scene, perspective=True, shadow_map=True, gamma=True,
+                background=(0, 0, 0, 0), shadow_size=SHADOW, directional_shadows=True)
+
+
+def shadow_cams(opts):
+    from polyred_gb300 import pmath, scene as sc
+    import numpy as np
+    src, _ = opts["scene"].lights()
+    center = opts["scene"].center()
+    cv, cp = opts["camera"].view_matrix(), opts["camera"].proj_matrix()
+    cams = {}
+    for k, l in enumerate(src):
+        if l.cast_shadow:
+            pos = l.position if isinstance(l, sc.Point) else (center - l.direction).astype(np.float32)
+            cams[k] = pmath.shadow_camera(pos, center, cv, cp)
+    return cams
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the shade kernel from the committed ncu
+    summary (profiles/shade_kernel_sphere_field_1080p.txt), or None."""
+    p = os.path.join(ROOT, "profiles", "shade_kernel_sphere_field_1080p.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import numpy as np
+    import oracle
+    from polyred_gb300 import render
+    threads = os.cpu_count() or 1
+    s, cam = workload()
+    opts = frame_opts(s, cam)
+    flat = render.FlatScene(s)
+    fd = render.FrameDesc(opts, shadow_cams(opts))
+    state = np.zeros((3, SHADOW[1], SHADOW[0]), np.float32)
+    out = render.Outputs(W, H, ("rgba", "tri_id", "depth"))
+    for _ in range(args.warmup):
+        oracle.render(flat.desc(), fd.desc, out.desc, shadow_state=state, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.render(flat.desc(), fd.desc, out.desc, shadow_state=state, threads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = N_TRIS / dt / 1e6
+    line = {"impl": "reference", "metric": "1080p Mtri/s", "value": v, "unit": "Mtri/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "sphere_field_1M_1080p", "n_tris": N_TRIS, "width": W, "height": H,
+                       "shadow_maps": "2 x 2048^2", "ao": True},
+            "cpu_baseline": {"value": v, "unit": "Mtri/s", "cores": threads, "kind": "port",
+                             "sample": "full frames of the workload, C++ restatement of the Go CPU renderer "
+                                       "(row-band threads, single-worker draw order)"},
+            "e2e": {"value": v, "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "frames_per_s": 1.0 / dt}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample():
+    """The oracle on one full frame with every host core (bounded: one frame)."""
+    import numpy as np
+    import oracle
+    from polyred_gb300 import render
+    threads = os.cpu_count() or 1
+    s, cam = workload()
+    opts = frame_opts(s, cam)
+    flat = render.FlatScene(s)
+    fd = render.FrameDesc(opts, shadow_cams(opts))
+    state = np.zeros((3, SHADOW[1], SHADOW[0]), np.float32)
+    out = render.Outputs(W, H, ("rgba",))
+    t0 = time.perf_counter()
+    oracle.render(flat.desc(), fd.desc, out.desc, shadow_state=state, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": N_TRIS / dt / 1e6, "unit": "Mtri/s", "cores": threads, "kind": "port",
+            "sample": "1 full frame of the workload (C++ restatement of the Go CPU renderer, row-band threads)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from polyred_gb300 import _abi, build, native, render
+
+    build.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = native.load()
+    dev = render.Device(local)
+    s, cam = workload()
+    opts = frame_opts(s, cam)
+    flat = render.FlatScene(s)
+    # pinned host copies of the soup for the end-to-end leg
+    pinned = {}
+    for name in ("pos", "nor", "uv", "col", "mat_id"):
+        a = getattr(flat, name)
+        t = torch.empty(a.shape, dtype={np.float32: torch.float32, np.uint8: torch.uint8,
+                                        np.int32: torch.int32}[a.dtype.type], pin_memory=True)
+        t.numpy()[...] = a
+        pinned[name] = t
+        setattr(flat, name, t.numpy())
+    desc = flat.desc()
+    native.check(lib.pr_scene_upload(dev.handle, C.byref(desc)))
+    fd = render.FrameDesc(opts, shadow_cams(opts))
+    # device outputs for the resident leg
+    rgba = torch.empty((H, W, 4), dtype=torch.uint8, device="cuda")
+    tri = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    dep = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    od = _abi.pr_outputs()
+    od.size = C.sizeof(_abi.pr_outputs)
+    od.flags = _abi.PR_OUT_DEVICE_PTRS
+    od.rgba, od.tri_id, od.depth = rgba.data_ptr(), tri.data_ptr(), dep.data_ptr()
+    stream = torch.cuda.ExternalStream(dev.stream())
+
+    def stats():
+        st = _abi.pr_stats()
+        st.size = C.sizeof(_abi.pr_stats)
+        native.check(lib.pr_frame_stats(dev.handle, C.byref(st)))
+        return st
+
+    # warm-up (also sizes the internal buffers; the synchronous call retries on overflow)
+    for _ in range(args.warmup):
+        native.check(lib.pr_render(dev.handle, C.byref(fd.desc), C.byref(od)))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- resident leg ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phases = {"ms_shadow": [], "ms_setup": [], "ms_raster": [], "ms_shade": []}
+    launches = 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        native.check(lib.pr_render_async(dev.handle, C.byref(fd.desc), C.byref(od)))
+        native.check(lib.pr_sync(dev.handle))
+        st = stats()
+        launches += st.n_kernel_launches
+        for k in phases:
+            phases[k].append(getattr(st, k))
+    ev1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * N_TRIS / (ms / 1e3) / 1e6
+
+    # per-phase device times (CUDA events inside the library, same stream)
+    ph = {k: statistics.mean(v) for k, v in phases.items() if v}
+
+    # ---- end-to-end leg (public C ABI, host buffers) ----
+    out = render.Outputs(W, H, ("rgba", "tri_id", "depth"))
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        native.check(lib.pr_scene_upload(dev.handle, C.byref(desc)))
+        native.check(lib.pr_render(dev.handle, C.byref(fd.desc), C.byref(out.desc)))
+    e1.record(stream)
+    barrier()
+    ems = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ems], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ems = float(t.item())
+    h2d = sum(getattr(flat, n).nbytes for n in ("pos", "nor", "uv", "col", "mat_id"))
+    d2h = W * H * (4 + 4 + 4)
+
+    # roofline of the dominant kernel: the deferred shade kernel
+    # (per pixel: winner id 4 B + depth 4 B read, RGBA8 4 B + tri-ID 4 B + depth 4 B written)
+    peak, peak_kind = measured_peaks()
+    shade_ms = ph.get("ms_shade", 0.0)
+    alg_bytes = W * H * 20
+    achieved = alg_bytes / (shade_ms / 1e3) / 1e9 if shade_ms > 0 else 0.0
+    traffic = ncu_traffic()
+
+    if rank == 0:
+        line = {"metric": "1080p Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "sphere_field_1M_1080p", "n_tris": N_TRIS, "width": W, "height": H,
+                           "shadow_maps": "2 x 2048^2 (point + directional)", "ao": True, "gamma": True,
+                           "l2": "inputs larger than L2 (136 MB triangle soup per frame)",
+                           "parallelism": f"replicas x{world}"},
+                "frames_per_s": world * 1e3 / ms,
+                "e2e": {"value": world * N_TRIS / (ems / 1e3) / 1e6, "unit": "Mtri/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": ems},
+                "phases_ms": ph,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak if peak else None, "traffic": traffic,
+                             "kernel": "shade_kernel", "peak_source": peak_kind,
+                             "algorithmic_bytes": alg_bytes},
+                "gpu_launches": launches,
+                "clocks": clk}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_sample()
+        print(json.dumps(line), flush=True)
+    dev.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,253 @@
+/*
+ * polyred_cuda.h — C ABI of libpolyred_cuda.so, the GB300 (sm_103a) render path
+ * behind polyred's `render.CUDA(dev)` option.
+ *
+ * The library replaces, as one device frame, the CPU passes that
+ * render.(*Renderer).Render runs (render/raster.go:155-199):
+ *   shadow passes   render/shadow.go:92-228   (passShadows / drawDepth)
+ *   forward raster  render/raster.go:226-273, 380-572 (cpuForwardPass / draw /
+ *                   drawClipped) with render/cull.go and render/clipping.go
+ *   deferred shade  render/raster.go:275-359 (passDeferred / shade) with
+ *                   shader/blinn_cpu.go:24-106, render/shadow.go:230-283,
+ *                   material/ao.go:20-73
+ *   gamma           render/raster.go:361-378, shader/gamma.go:13-18,
+ *                   color/srgb.go:15-33
+ * Results follow the reference's single-worker order (render.Workers(1)):
+ * triangle-ID and depth buffers are bit-exact with it.
+ *
+ * Every entry point takes plain integers and pointers (no struct by value, no
+ * callbacks, no varargs) so that a purego binding (gpu/backend_vk.go:209-232
+ * style SyscallN) can call it. Descriptor structs are passed by pointer and
+ * start with a `size` field (sizeof the struct the caller was compiled with).
+ *
+ * Threading: one pr_ctx owns one CUDA stream and its device buffers. Calls on
+ * one context must be serialised by the caller (the Go renderer holds a
+ * mutex, as render/options.go:125-141 waits for an in-flight frame). Distinct
+ * contexts may be used concurrently.
+ *
+ * Errors: every function returns a status (PR_OK or a negative PR_ERR_*).
+ * pr_last_error() gives a thread-local detail string for the last failure on
+ * the calling thread. There is no silent CPU fallback.
+ */
+#ifndef POLYRED_CUDA_H
+#define POLYRED_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PR_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+#define PR_OK                 0
+#define PR_ERR_INVALID_ARG   -1
+#define PR_ERR_OOM           -2
+#define PR_ERR_CUDA          -3
+#define PR_ERR_OVERFLOW      -4  /* an internal capacity was exceeded after retry */
+#define PR_ERR_TIMEOUT       -5  /* a bounded device wait gave up */
+#define PR_ERR_UNIMPLEMENTED -6
+#define PR_ERR_NO_SCENE      -7
+#define PR_ERR_UNSUPPORTED   -8  /* e.g. MSAA != 1, a non-uniform texture */
+#define PR_ERR_NO_DEVICE     -9
+#define PR_ERR_SINGULAR     -10  /* Mat4.Inv of a zero determinant; the
+                                    reference panics (math/mat4.go:261-263) */
+
+/* ---- flags ------------------------------------------------------------ */
+/* material.Standard flags (material/material.go:23-29) */
+#define PR_MAT_FLAT_SHADING    1u
+#define PR_MAT_AO              2u
+#define PR_MAT_RECEIVE_SHADOW  4u
+#define PR_MAT_MIPMAP          8u  /* buffer.Texture.UseMipmap() (buffer/texture.go:56-59) */
+
+#define PR_LIGHT_POINT         0   /* light/point.go */
+#define PR_LIGHT_DIRECTIONAL   1   /* light/directional.go */
+
+#define PR_FRAME_PERSPECTIVE   1u  /* option.Perspect (render/options.go:49-56) */
+#define PR_FRAME_SHADOWMAP     2u  /* render.ShadowMap(true) */
+#define PR_FRAME_GAMMA         4u  /* render.GammaCorrection(true) */
+
+#define PR_SCENE_DEVICE_PTRS   1u  /* triangle arrays are device pointers */
+#define PR_OUT_DEVICE_PTRS     1u  /* output arrays are device pointers */
+
+#define PR_TRI_NONE 0xFFFFFFFFu    /* tri_id of a pixel no triangle covers */
+
+/* ---- scene ------------------------------------------------------------ */
+
+/* One geometry in scene traversal order (scene/core.go:86-200). Its
+ * triangles are [first_tri, first_tri + n_tris) of the soup. `model` is the
+ * composed model matrix that cpuForwardPass builds as
+ * modelMatrix.MulM(g.ModelMatrix()) (render/raster.go:242), row-major
+ * X00 X01 X02 X03 X10 ... X33. `mat_base` is the offset of this geometry's
+ * materials in the flat material table (render/raster.go:252-262). */
+typedef struct pr_object {
+    uint32_t first_tri;
+    uint32_t n_tris;
+    int32_t  mat_base;
+    uint32_t reserved;
+    float    model[16];
+} pr_object;
+
+/* material.BlinnPhong (material/material.go:43-51) with a uniform (1x1)
+ * texture (buffer/texture.go:16-24). Colours are RGBA8 as stored by the
+ * reference (color.FromValue rounds half away from zero). */
+typedef struct pr_material {
+    uint8_t  diffuse[4];
+    uint8_t  specular[4];
+    uint8_t  texture[4];    /* the texel of the 1x1 texture */
+    float    shininess;
+    uint32_t flags;         /* PR_MAT_* */
+    int32_t  texture_size;  /* Texture.Size(); only 1 is supported */
+} pr_material;
+
+/* The triangle soup: per triangle three vertices (primitive.Vertex,
+ * geometry/primitive/vertex.go:14-20). Arrays are host pointers unless
+ * flags has PR_SCENE_DEVICE_PTRS. */
+typedef struct pr_scene_desc {
+    uint32_t size;
+    uint32_t flags;
+    uint32_t n_tris;
+    uint32_t n_objects;
+    uint32_t n_materials;
+    uint32_t reserved;
+    const float*   pos;      /* [n_tris][3][4]  Vertex.Pos (x,y,z,w) */
+    const float*   nor;      /* [n_tris][3][4]  Vertex.Nor (x,y,z,w) */
+    const float*   uv;       /* [n_tris][3][2]  Vertex.UV */
+    const uint8_t* col;      /* [n_tris][3][4]  Vertex.Col RGBA8 */
+    const int32_t* mat_id;   /* [n_tris] Triangle.MaterialID, geometry-local; <0 = vertex colour */
+    const pr_object*   objects;    /* [n_objects] (host memory) */
+    const pr_material* materials;  /* [n_materials] flat table (host memory) */
+} pr_scene_desc;
+
+/* ---- frame ------------------------------------------------------------ */
+
+/* A light source (light.Source) in scene.Lights() order. For a light with
+ * cast_shadow set and PR_FRAME_SHADOWMAP on, shadow_view/shadow_proj are the
+ * light camera initShadowMaps builds (render/shadow.go:41-85); see
+ * pr_shadow_camera. */
+typedef struct pr_light {
+    int32_t type;            /* PR_LIGHT_* */
+    int32_t cast_shadow;
+    float   pos[3];          /* point: Position() */
+    float   dir[3];          /* directional: Dir() (already normalised) */
+    float   intensity;
+    uint8_t color[4];
+    float   shadow_view[16];
+    float   shadow_proj[16];
+} pr_light;
+
+typedef struct pr_frame_desc {
+    uint32_t size;
+    uint32_t flags;          /* PR_FRAME_* */
+    int32_t  width, height;  /* framebuffer size (MSAA 1) */
+    float    view[16];       /* Camera.ViewMatrix() */
+    float    proj[16];       /* Camera.ProjMatrix() */
+    float    cam_pos[3];     /* Camera.Position() */
+    uint8_t  background[4];  /* render.Background */
+    uint32_t n_lights;
+    uint32_t n_ambient;
+    const pr_light* lights;  /* [n_lights] */
+    const float*    ambient; /* [n_ambient] light.Environment intensities, traversal order */
+    int32_t  shadow_width;   /* 0 = framebuffer size (the reference's only mode) */
+    int32_t  shadow_height;
+} pr_frame_desc;
+
+/* ---- outputs ------------------------------------------------------------
+ * Every array is optional (NULL = not wanted). Rows are top-down: row r holds
+ * raster row y = height-1-r, the order of buffer.FragmentBuffer storage
+ * (buffer/buffer.go:209-213) and of Render()'s *image.RGBA. */
+typedef struct pr_outputs {
+    uint32_t size;
+    uint32_t flags;          /* PR_OUT_DEVICE_PTRS */
+    uint8_t*  rgba;          /* [H][W][4] final image (after gamma when enabled) */
+    uint32_t* tri_id;        /* [H][W] winning input triangle index, PR_TRI_NONE if empty */
+    float*    depth;         /* [H][W] Fragment.Depth (0 where empty) */
+    float*    nor;           /* [H][W][4] Fragment.Nor */
+    float*    face_nor;      /* [H][W][4] Fragment.FaceNor */
+    float*    world_pos;     /* [H][W][4] Fragment.WordPos */
+    float*    uvd;           /* [H][W][4] Fragment.U, V, Du, Dv */
+    uint8_t*  vcol;          /* [H][W][4] Fragment.Col (interpolated vertex colour) */
+    int32_t*  mat_id;        /* [H][W] flat Fragment.MaterialID (-1 where empty) */
+    float*    shadow_maps;   /* [n_lights][SH][SW] shadow depth maps after the frame
+                                (rows bottom-up, index x + y*SW as render/shadow.go:213) */
+} pr_outputs;
+
+/* Per-frame counters (optional, pr_frame_stats). */
+typedef struct pr_stats {
+    uint32_t size;
+    uint32_t n_tris_in;
+    uint32_t n_raster_tris;    /* after cull/clip, main view */
+    uint32_t n_clipped_tris;   /* input triangles that went through clipTriangle */
+    uint32_t n_large_tris;     /* raster triangles on the tiled path */
+    uint32_t n_nan_fragments;  /* fragments with NaN depth (degenerate triangles) */
+    uint32_t n_kernel_launches;
+    uint32_t reserved;
+    float    ms_shadow, ms_setup, ms_raster, ms_shade, ms_total;
+} pr_stats;
+
+/* ---- entry points ------------------------------------------------------ */
+
+int         pr_abi_version(void);
+const char* pr_error_string(int status);
+const char* pr_last_error(void);
+
+/* Create a context on CUDA device `device` (a caller-chosen ordinal). The
+ * context never resets or closes the device (cf. render/raster.go:57-60: a
+ * caller-supplied device is not closed by the renderer). */
+int pr_create(int device, void** out_ctx);
+int pr_destroy(void* ctx);
+
+/* Copy a scene to the device (replacing the previous one). Host arrays may
+ * be freed after the call returns. Also clears the shadow maps, as
+ * initShadowMaps allocates them zeroed (render/shadow.go:87). */
+int pr_scene_upload(void* ctx, const pr_scene_desc* scene);
+
+/* Zero the persistent shadow maps (initShadowMaps on NewRenderer/Options:
+ * render/raster.go:135-140, render/options.go:135-140). Render() itself never
+ * clears them (render/shadow.go:221-228). */
+int pr_shadow_reset(void* ctx);
+
+/* Render one frame: shadows, forward raster, deferred shading, gamma
+ * (render/raster.go:155-199), then copy the requested outputs. Blocks until
+ * the outputs are complete. */
+int pr_render(void* ctx, const pr_frame_desc* frame, pr_outputs* out);
+
+/* Render without synchronising; outputs must be device pointers
+ * (PR_OUT_DEVICE_PTRS). pr_sync waits for the context's stream. */
+int pr_render_async(void* ctx, const pr_frame_desc* frame, pr_outputs* out);
+int pr_sync(void* ctx);
+
+/* Counters of the last frame rendered on this context. */
+int pr_frame_stats(void* ctx, pr_stats* out);
+
+/* The CUDA stream (cudaStream_t) the context launches on, for callers that
+ * time or order work around it. */
+int pr_stream(void* ctx, void** out_stream);
+
+/* ---- host math helpers --------------------------------------------------
+ * f32 arithmetic exactly as the reference's Go (amd64) evaluates it, so a
+ * host that is not Go can build the same matrices. Matrices are row-major. */
+
+/* camera.ViewMatrix(pos, target, up)  (camera/camera.go:42-53) */
+int pr_view_matrix(const float pos[3], const float target[3], const float up[3], float out[16]);
+/* (*camera.Perspective).ProjMatrix (camera/perspective.go:100-111); fov in degrees */
+int pr_perspective_matrix(float fov, float aspect, float near, float far, float out[16]);
+/* (*camera.Orthographic).ProjMatrix (camera/orthographic.go:106-119) */
+int pr_orthographic_matrix(float left, float right, float bottom, float top,
+                           float near, float far, float out[16]);
+/* Mat4.MulM (math/mat4.go:201-220): out = a * b */
+int pr_mat4_mul(const float a[16], const float b[16], float out[16]);
+/* Mat4.Inv (math/mat4.go:259-283); PR_ERR_SINGULAR on a zero determinant */
+int pr_mat4_inv(const float m[16], float out[16]);
+/* The orthographic light camera initShadowMaps fits around the main camera
+ * frustum (render/shadow.go:41-85): writes its view and projection. */
+int pr_shadow_camera(const float light_pos[3], const float scene_center[3],
+                     const float cam_view[16], const float cam_proj[16],
+                     float out_view[16], float out_proj[16]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POLYRED_CUDA_H */

@@ -1,0 +1,120 @@
+"""ctypes mirror of include/polyred_cuda.h (layouts must match the header).
+
+Shared by the product loader (polyred_gb300.native) and by the test-side
+oracle loader, so both read the same scene/frame/output descriptors.
+"""
+import ctypes as C
+
+ABI_VERSION = 1
+
+PR_OK = 0
+PR_ERR_INVALID_ARG = -1
+PR_ERR_OOM = -2
+PR_ERR_CUDA = -3
+PR_ERR_OVERFLOW = -4
+PR_ERR_TIMEOUT = -5
+PR_ERR_UNIMPLEMENTED = -6
+PR_ERR_NO_SCENE = -7
+PR_ERR_UNSUPPORTED = -8
+PR_ERR_NO_DEVICE = -9
+PR_ERR_SINGULAR = -10
+
+PR_MAT_FLAT_SHADING = 1
+PR_MAT_AO = 2
+PR_MAT_RECEIVE_SHADOW = 4
+PR_MAT_MIPMAP = 8
+
+PR_LIGHT_POINT = 0
+PR_LIGHT_DIRECTIONAL = 1
+
+PR_FRAME_PERSPECTIVE = 1
+PR_FRAME_SHADOWMAP = 2
+PR_FRAME_GAMMA = 4
+
+PR_SCENE_DEVICE_PTRS = 1
+PR_OUT_DEVICE_PTRS = 1
+
+PR_TRI_NONE = 0xFFFFFFFF
+
+F16 = C.c_float * 16
+
+
+class pr_object(C.Structure):
+    _fields_ = [("first_tri", C.c_uint32), ("n_tris", C.c_uint32), ("mat_base", C.c_int32),
+                ("reserved", C.c_uint32), ("model", F16)]
+
+
+class pr_material(C.Structure):
+    _fields_ = [("diffuse", C.c_uint8 * 4), ("specular", C.c_uint8 * 4), ("texture", C.c_uint8 * 4),
+                ("shininess", C.c_float), ("flags", C.c_uint32), ("texture_size", C.c_int32)]
+
+
+class pr_scene_desc(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("flags", C.c_uint32), ("n_tris", C.c_uint32),
+                ("n_objects", C.c_uint32), ("n_materials", C.c_uint32), ("reserved", C.c_uint32),
+                ("pos", C.c_void_p), ("nor", C.c_void_p), ("uv", C.c_void_p), ("col", C.c_void_p),
+                ("mat_id", C.c_void_p), ("objects", C.POINTER(pr_object)),
+                ("materials", C.POINTER(pr_material))]
+
+
+class pr_light(C.Structure):
+    _fields_ = [("type", C.c_int32), ("cast_shadow", C.c_int32), ("pos", C.c_float * 3),
+                ("dir", C.c_float * 3), ("intensity", C.c_float), ("color", C.c_uint8 * 4),
+                ("shadow_view", F16), ("shadow_proj", F16)]
+
+
+class pr_frame_desc(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("flags", C.c_uint32), ("width", C.c_int32), ("height", C.c_int32),
+                ("view", F16), ("proj", F16), ("cam_pos", C.c_float * 3), ("background", C.c_uint8 * 4),
+                ("n_lights", C.c_uint32), ("n_ambient", C.c_uint32), ("lights", C.POINTER(pr_light)),
+                ("ambient", C.POINTER(C.c_float)), ("shadow_width", C.c_int32),
+                ("shadow_height", C.c_int32)]
+
+
+class pr_outputs(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("flags", C.c_uint32), ("rgba", C.c_void_p), ("tri_id", C.c_void_p),
+                ("depth", C.c_void_p), ("nor", C.c_void_p), ("face_nor", C.c_void_p),
+                ("world_pos", C.c_void_p), ("uvd", C.c_void_p), ("vcol", C.c_void_p),
+                ("mat_id", C.c_void_p), ("shadow_maps", C.c_void_p)]
+
+
+class pr_stats(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("n_tris_in", C.c_uint32), ("n_raster_tris", C.c_uint32),
+                ("n_clipped_tris", C.c_uint32), ("n_large_tris", C.c_uint32), ("n_nan_fragments", C.c_uint32),
+                ("n_kernel_launches", C.c_uint32), ("reserved", C.c_uint32), ("ms_shadow", C.c_float),
+                ("ms_setup", C.c_float), ("ms_raster", C.c_float), ("ms_shade", C.c_float),
+                ("ms_total", C.c_float)]
+
+
+# Every entry point include/polyred_cuda.h declares: (name, restype, argtypes).
+VP = C.c_void_p
+FP = C.POINTER(C.c_float)
+ENTRY_POINTS = [
+    ("pr_abi_version", C.c_int, []),
+    ("pr_error_string", C.c_char_p, [C.c_int]),
+    ("pr_last_error", C.c_char_p, []),
+    ("pr_create", C.c_int, [C.c_int, C.POINTER(VP)]),
+    ("pr_destroy", C.c_int, [VP]),
+    ("pr_scene_upload", C.c_int, [VP, C.POINTER(pr_scene_desc)]),
+    ("pr_shadow_reset", C.c_int, [VP]),
+    ("pr_render", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_outputs)]),
+    ("pr_render_async", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_outputs)]),
+    ("pr_sync", C.c_int, [VP]),
+    ("pr_frame_stats", C.c_int, [VP, C.POINTER(pr_stats)]),
+    ("pr_stream", C.c_int, [VP, C.POINTER(VP)]),
+    ("pr_view_matrix", C.c_int, [FP, FP, FP, FP]),
+    ("pr_perspective_matrix", C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, FP]),
+    ("pr_orthographic_matrix", C.c_int, [C.c_float] * 6 + [FP]),
+    ("pr_mat4_mul", C.c_int, [FP, FP, FP]),
+    ("pr_mat4_inv", C.c_int, [FP, FP]),
+    ("pr_shadow_camera", C.c_int, [FP, FP, FP, FP, FP, FP]),
+]
+
+
+def bind(lib):
+    """Set restype/argtypes for every declared entry point on a CDLL."""
+    for name, res, args in ENTRY_POINTS:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib

@@ -1,0 +1,284 @@
+// pr_devmath.cuh — device arithmetic with the reference's exact float32
+// semantics. The translation unit is compiled with -fmad=false so that every
+// plain a*b+c below stays two IEEE roundings (Go amd64 never fuses); fused
+// operations are spelled out with __fmaf_rn.
+#pragma once
+
+#include <cstdint>
+
+#define PR_DEV __device__ __forceinline__
+
+namespace prd {
+
+// ---------------------------------------------------------------------------
+// float32(fma(float64(a), float64(b), float64(c))): Go's math.FMA[float32]
+// (math/math.go:265-267), used by Vec4.Dot/Apply/Cross and Barycoord.
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the common case is
+// done in FP32:
+//   r1 = fmaf(a, b, c) is the single rounding RN32(s) of s = a*b + c.
+//   The double rounding RN32(RN64(s)) differs from it only when RN64(s) lands
+//   exactly on a float32 rounding midpoint that s itself is not on, i.e. when
+//   the exact residual s - r1 is within half a float64 ulp of +-half a
+//   float32 ulp of r1 (or of a quarter ulp just below a power of two).
+//   The residual is obtained error-free with the ErrFma algorithm of Boldo and
+//   Muller ("Exact and approximated error of the FMA", IEEE TC 2011):
+//   s = r1 + r2 + r3 exactly with |r3| <= ulp(r2)/2.
+//   Only when r2 sits exactly on such a midpoint with a nonzero r3 (a true
+//   hazard), or a special value shows up (tiny/zero r1, inf, NaN), does the
+//   FP64 unit compute the reference expression directly. On random and
+//   pixel-grid data that is fewer than 1 in 10^7 calls.
+// ---------------------------------------------------------------------------
+PR_DEV float fma64f_slow(float a, float b, float c) {
+    return __double2float_rn(__fma_rn((double)a, (double)b, (double)c));
+}
+
+PR_DEV float fma64f(float a, float b, float c) {
+    float r1 = __fmaf_rn(a, b, c);
+    // With a zero factor or a zero addend, a*b + c is exact in float64, so the
+    // single rounding r1 already equals the reference's double rounding.
+    if (a == 0.0f || b == 0.0f || c == 0.0f) return r1;
+    float u1 = __fmul_rn(a, b);
+    float u2 = __fmaf_rn(a, b, -u1);  // a*b = u1 + u2 exactly
+    // TwoSum(c, u2) -> (a1, z1)
+    float a1 = __fadd_rn(c, u2);
+    float t1 = __fsub_rn(a1, c);
+    float z1 = __fadd_rn(__fsub_rn(c, __fsub_rn(a1, t1)), __fsub_rn(u2, t1));
+    // TwoSum(u1, a1) -> (b1, b2)
+    float b1 = __fadd_rn(u1, a1);
+    float t2 = __fsub_rn(b1, u1);
+    float b2 = __fadd_rn(__fsub_rn(u1, __fsub_rn(b1, t2)), __fsub_rn(a1, t2));
+    float g = __fadd_rn(__fsub_rn(b1, r1), b2);
+    float r2 = __fadd_rn(g, z1);
+    uint32_t ex = (__float_as_uint(r1) >> 23) & 0xffu;
+    // Tiny, zero, infinite or NaN r1: the error-free transform may not hold.
+    bool special = (ex < 25u) | (ex == 255u);
+    if (!special && r2 == 0.0f) return r1;  // s == r1 exactly
+    // half a float32 ulp of r1 (r1 normal with exponent field >= 25)
+    float u = __uint_as_float((ex - 24u) << 23);
+    float ad = fabsf(r2);
+    bool bad = !(ad <= u);  // NaN / out-of-bound residual (overflow inside the EFT)
+    if (special | bad) return fma64f_slow(a, b, c);
+    // A double-rounding hazard puts s within 2^-29 u of a midpoint, which
+    // makes r2 = RN32(s - r1) exactly +-u (or +-u/2 below a power of two).
+    if (ad != u && ad != 0.5f * u) return r1;
+    // r2 on a midpoint: s is exactly the midpoint (harmless) iff r3 == 0.
+    float r3 = __fsub_rn(z1, __fsub_rn(r2, g));
+    if (r3 == 0.0f) return r1;
+    return fma64f_slow(a, b, c);
+}
+
+// ---- Go conversions and polyred scalar helpers --------------------------
+
+// Go int(float32) on amd64 (CVTTSS2SQ): NaN / out of range -> INT64_MIN.
+PR_DEV long long go_f2i(float x) {
+    if (!(x < 9.2233720368547758e18f && x >= -9.2233720368547758e18f)) return (long long)0x8000000000000000ull;
+    return (long long)x;
+}
+// Go uint8(float32) on amd64: via int32 (CVTTSS2SL), low byte.
+PR_DEV uint32_t go_f2u8(float x) {
+    if (!(x < 2147483648.0f && x >= -2147483648.0f)) return 0u;
+    return ((uint32_t)(int)x) & 0xffu;
+}
+// polyred math.Round: half away from zero (roundf is exact).
+PR_DEV float pround(float x) { return roundf(x); }
+PR_DEV float pclamp(float n, float lo, float hi) {
+    if (n < lo) return lo;
+    if (n > hi) return hi;
+    return n;
+}
+// Go math.Max / math.Min special cases on float32 arguments.
+PR_DEV float pmax(float x, float y) {
+    if (__float_as_uint(x) == 0x7f800000u || __float_as_uint(y) == 0x7f800000u) return __uint_as_float(0x7f800000u);
+    if (isnan(x) || isnan(y)) return __uint_as_float(0x7fc00000u);
+    if (x == 0.0f && y == 0.0f) return signbit(x) ? y : x;
+    return x > y ? x : y;
+}
+PR_DEV float pmin(float x, float y) {
+    if (__float_as_uint(x) == 0xff800000u || __float_as_uint(y) == 0xff800000u) return __uint_as_float(0xff800000u);
+    if (isnan(x) || isnan(y)) return __uint_as_float(0x7fc00000u);
+    if (x == 0.0f && y == 0.0f) return signbit(x) ? x : y;
+    return x < y ? x : y;
+}
+
+// ---- vectors (math/vec4.go) ----------------------------------------------
+struct V4 { float x, y, z, w; };
+
+PR_DEV V4 sub4(V4 v, V4 u) { return {__fsub_rn(v.x, u.x), __fsub_rn(v.y, u.y), __fsub_rn(v.z, u.z), __fsub_rn(v.w, u.w)}; }
+PR_DEV V4 add4(V4 v, V4 u) { return {__fadd_rn(v.x, u.x), __fadd_rn(v.y, u.y), __fadd_rn(v.z, u.z), __fadd_rn(v.w, u.w)}; }
+PR_DEV float dot4(V4 v, V4 u) {
+    return fma64f(v.x, u.x, fma64f(v.y, u.y, fma64f(v.z, u.z, __fmul_rn(v.w, u.w))));
+}
+PR_DEV float len4(V4 v) { return __fsqrt_rn(dot4(v, v)); }  // sqrt in f64 then f32 == correctly rounded sqrtf
+PR_DEV V4 unit4(V4 v) {
+    float n = __fdiv_rn(1.0f, len4(v));
+    return {__fmul_rn(v.x, n), __fmul_rn(v.y, n), __fmul_rn(v.z, n), __fmul_rn(v.w, n)};
+}
+PR_DEV V4 cross4(V4 v, V4 u) {
+    return {fma64f(v.y, u.z, -__fmul_rn(v.z, u.y)), fma64f(v.z, u.x, -__fmul_rn(v.x, u.z)),
+            fma64f(v.x, u.y, -__fmul_rn(v.y, u.x)), 0.0f};
+}
+PR_DEV V4 pos4(V4 v) {
+    if (v.w == 1.0f || v.w == 0.0f) return {v.x, v.y, v.z, 1.0f};
+    float iw = __fdiv_rn(1.0f, v.w);
+    return {__fmul_rn(v.x, iw), __fmul_rn(v.y, iw), __fmul_rn(v.z, iw), 1.0f};
+}
+// Vec4.Apply with a row-major matrix m[16]
+PR_DEV V4 apply4(V4 v, const float* m) {
+    return {fma64f(m[0], v.x, fma64f(m[1], v.y, fma64f(m[2], v.z, __fmul_rn(m[3], v.w)))),
+            fma64f(m[4], v.x, fma64f(m[5], v.y, fma64f(m[6], v.z, __fmul_rn(m[7], v.w)))),
+            fma64f(m[8], v.x, fma64f(m[9], v.y, fma64f(m[10], v.z, __fmul_rn(m[11], v.w)))),
+            fma64f(m[12], v.x, fma64f(m[13], v.y, fma64f(m[14], v.z, __fmul_rn(m[15], v.w))))};
+}
+// Mat4.MulV: plain float32 sums left to right
+PR_DEV V4 mulv(const float* m, V4 v) {
+    return {__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], v.x), __fmul_rn(m[1], v.y)), __fmul_rn(m[2], v.z)), __fmul_rn(m[3], v.w)),
+            __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[4], v.x), __fmul_rn(m[5], v.y)), __fmul_rn(m[6], v.z)), __fmul_rn(m[7], v.w)),
+            __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[8], v.x), __fmul_rn(m[9], v.y)), __fmul_rn(m[10], v.z)), __fmul_rn(m[11], v.w)),
+            __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[12], v.x), __fmul_rn(m[13], v.y)), __fmul_rn(m[14], v.z)), __fmul_rn(m[15], v.w))};
+}
+// Cross(...).Z of two 2-D vectors (Barycoord, cullBackFace)
+PR_DEV float cross_z(float vx, float vy, float ux, float uy) { return fma64f(vx, uy, -__fmul_rn(vy, ux)); }
+
+// math.Barycoord (math/interpolate.go:66-78) given the triangle's Sabc.
+PR_DEV void barycoord_s(float px, float py, float x1, float y1, float x2, float y2, float x3, float y3,
+                        float sabc, float bc[3]) {
+    float apx = __fsub_rn(px, x1), apy = __fsub_rn(py, y1);
+    float abx = __fsub_rn(x2, x1), aby = __fsub_rn(y2, y1);
+    float acx = __fsub_rn(x3, x1), acy = __fsub_rn(y3, y1);
+    float bcx = __fsub_rn(x3, x2), bcy = __fsub_rn(y3, y2);
+    float bpx = __fsub_rn(px, x2), bpy = __fsub_rn(py, y2);
+    float sabp = cross_z(abx, aby, apx, apy);
+    float sapc = cross_z(apx, apy, acx, acy);
+    float sbcp = cross_z(bcx, bcy, bpx, bpy);
+    bc[0] = __fdiv_rn(sbcp, sabc);
+    bc[1] = __fdiv_rn(sapc, sabc);
+    bc[2] = __fdiv_rn(sabp, sabc);
+}
+PR_DEV float sabc_of(float x1, float y1, float x2, float y2, float x3, float y3) {
+    return cross_z(__fsub_rn(x2, x1), __fsub_rn(y2, y1), __fsub_rn(x3, x1), __fsub_rn(y3, y1));
+}
+
+// Orderable keys: monotone float -> uint32 for non-NaN values, with -0 and +0
+// mapped to the same key (the reference's comparisons treat them as equal).
+PR_DEV uint32_t fkey(float f) {
+    if (f == 0.0f) f = 0.0f;
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+PR_DEV float fkey_decode(uint32_t k) {
+    uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(b);
+}
+
+// ---- Go math.Pow / math.Atan in float64 (Go 1.26 math/pow.go, atan.go) ----
+PR_DEV bool is_odd_int(double x) {
+    if (fabs(x) >= 9007199254740992.0) return false;
+    double xi;
+    double xf = modf(x, &xi);
+    if (xf != 0) return false;
+    long long i = (long long)xi;
+    return (i & 1) == 1;
+}
+PR_DEV double go_pow(double x, double y) {
+    if (y == 0 || x == 1) return 1;
+    if (y == 1) return x;
+    if (isnan(x) || isnan(y)) return __longlong_as_double(0x7ff8000000000000ll);
+    if (x == 0) {
+        if (y < 0) return (signbit(x) && is_odd_int(y)) ? -__longlong_as_double(0x7ff0000000000000ll)
+                                                          : __longlong_as_double(0x7ff0000000000000ll);
+        if (y > 0) return (signbit(x) && is_odd_int(y)) ? x : 0.0;
+    }
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    if (isinf(y)) {
+        if (x == -1) return 1;
+        if ((fabs(x) < 1) == (y > 0)) return 0;
+        return inf;
+    }
+    if (isinf(x)) {
+        if (x < 0) {
+            // Pow(-Inf, y) = Pow(-0, -y)
+            double y2 = -y;
+            if (y2 < 0) return is_odd_int(y2) ? -inf : inf;
+            if (y2 > 0) return is_odd_int(y2) ? -0.0 : 0.0;
+            return 1;
+        }
+        if (y < 0) return 0;
+        if (y > 0) return inf;
+    }
+    if (y == 0.5) return __dsqrt_rn(x);
+    if (y == -0.5) return __ddiv_rn(1.0, __dsqrt_rn(x));
+    double yi;
+    double yf = modf(fabs(y), &yi);
+    if (yf != 0 && x < 0) return __longlong_as_double(0x7ff8000000000000ll);
+    if (yi >= 9223372036854775808.0) {
+        if (x == -1) return 1;
+        if ((fabs(x) < 1) == (y > 0)) return 0;
+        return inf;
+    }
+    double a1 = 1.0;
+    long long ae = 0;
+    if (yf != 0) {
+        if (yf > 0.5) {
+            yf = __dsub_rn(yf, 1.0);
+            yi = __dadd_rn(yi, 1.0);
+        }
+        a1 = exp(__dmul_rn(yf, log(x)));
+    }
+    int xe_i;
+    double x1 = frexp(x, &xe_i);
+    long long xe = xe_i;
+    for (long long i = (long long)yi; i != 0; i >>= 1) {
+        if (xe < -(1 << 12) || (1 << 12) < xe) {
+            ae += xe;
+            break;
+        }
+        if ((i & 1) == 1) {
+            a1 = __dmul_rn(a1, x1);
+            ae += xe;
+        }
+        x1 = __dmul_rn(x1, x1);
+        xe <<= 1;
+        if (x1 < .5) {
+            x1 = __dadd_rn(x1, x1);
+            xe--;
+        }
+    }
+    if (y < 0) {
+        a1 = __ddiv_rn(1.0, a1);
+        ae = -ae;
+    }
+    if (ae > 4096) ae = 4096;
+    if (ae < -4096) ae = -4096;
+    return ldexp(a1, (int)ae);
+}
+
+PR_DEV double go_xatan(double x) {
+    const double P0 = -8.750608600031904122785e-01, P1 = -1.615753718733365076637e+01,
+                 P2 = -7.500855792314704667340e+01, P3 = -1.228866684490136173410e+02,
+                 P4 = -6.485021904942025371773e+01;
+    const double Q0 = +2.485846490142306297962e+01, Q1 = +1.650270098316988542046e+02,
+                 Q2 = +4.328810604912902668951e+02, Q3 = +4.853903996359136964868e+02,
+                 Q4 = +1.945506571482613964425e+02;
+    double z = __dmul_rn(x, x);
+    double num = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(P0, z), P1), z), P2), z), P3), z), P4);
+    double den = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(__dadd_rn(z, Q0), z), Q1), z), Q2), z), Q3), z), Q4);
+    z = __ddiv_rn(__dmul_rn(z, num), den);
+    return __dadd_rn(__dmul_rn(x, z), x);
+}
+PR_DEV double go_satan(double x) {
+    const double Morebits = 6.123233995736765886130e-17;
+    const double Tan3pio8 = 2.41421356237309504880;
+    const double PiOver2 = 1.57079632679489661923132169163975144;
+    const double PiOver4 = 0.785398163397448309615660845819875721;
+    if (x <= 0.66) return go_xatan(x);
+    if (x > Tan3pio8) return __dadd_rn(__dsub_rn(PiOver2, go_xatan(__ddiv_rn(1.0, x))), Morebits);
+    return __dadd_rn(__dadd_rn(PiOver4, go_xatan(__ddiv_rn(__dsub_rn(x, 1.0), __dadd_rn(x, 1.0)))), 0.5 * Morebits);
+}
+PR_DEV double go_atan(double x) {
+    if (x == 0) return x;
+    if (x > 0) return go_satan(x);
+    return -go_satan(-x);
+}
+
+}  // namespace prd

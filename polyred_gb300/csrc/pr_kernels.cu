@@ -1,0 +1,811 @@
+// pr_kernels.cu — the GB300 (sm_103a) render path kernels.
+//
+// Frame = [shadow setup + raster per casting light] -> main setup -> raster
+//         -> (NaN fix-up) -> resolve -> shade (attributes, Blinn-Phong,
+//         shadow lookups, AO, gamma, RGBA8 pack).
+//
+// Visibility is order independent: each fragment issues a 64-bit atomicMax of
+// (orderable depth << 32 | ~seq), which leaves at every pixel the first
+// fragment (in the reference's single-worker draw order) with the greatest
+// depth — exactly what buffer.FragmentBuffer's sequential DepthTest/Set
+// (buffer/buffer.go:221-280) keeps. A NaN-depth fragment only wins when it is
+// the first fragment of its pixel; a rare fix-up pass settles that.
+//
+// Compiled with -fmad=false -prec-div=true -prec-sqrt=true -ftz=false.
+#include <cuda_runtime.h>
+
+#include "pr_devmath.cuh"
+#include "pr_kernels.cuh"
+
+using namespace prd;
+
+namespace prk {
+namespace {
+
+constexpr float kEps = 1e-7f;  // math.Epsilon as float32 (math/math.go:31)
+
+PR_DEV V4 ld4(const float4 q) { return {q.x, q.y, q.z, q.w}; }
+
+// Mat4.MulM (math/mat4.go:201-220), plain float32 sums left to right.
+PR_DEV void mulm(const float* m, const float* n, float* r) {
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            r[i * 4 + j] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[i * 4 + 0], n[0 * 4 + j]), __fmul_rn(m[i * 4 + 1], n[1 * 4 + j])),
+                                               __fmul_rn(m[i * 4 + 2], n[2 * 4 + j])),
+                                     __fmul_rn(m[i * 4 + 3], n[3 * 4 + j]));
+}
+
+PR_DEV bool approx_eq(float a, float b) { return fabsf(__fsub_rn(a, b)) <= kEps; }
+PR_DEV bool approx_less(float a, float b) { return a < b && fabsf(__fsub_rn(a, b)) > kEps; }
+PR_DEV bool le_approx(float a, float b) { return approx_eq(a, b) || approx_less(a, b); }
+
+// Triangle.IsValid (geometry/primitive/triangle.go:63-80)
+PR_DEV bool tri_is_valid(V4 p1, V4 p2, V4 p3) {
+    V4 a = sub4(p2, p1), b = sub4(p3, p1);
+    if (approx_eq(a.x, 0) && approx_eq(a.y, 0) && approx_eq(a.z, 0)) return false;
+    if (approx_eq(b.x, 0) && approx_eq(b.y, 0) && approx_eq(b.z, 0)) return false;
+    float d = __fdiv_rn(dot4(a, b), __fmul_rn(len4(a), len4(b)));
+    return !approx_eq(d, 1.0f) && !approx_eq(d, -1.0f);
+}
+
+struct Box { float mnx, mny, mnz, mxx, mxy, mxz; };
+// NewAABB over three points (geometry/primitive/box.go:15-27)
+PR_DEV Box box3(V4 a, V4 b, V4 c) {
+    Box r;
+    r.mnx = pmin(pmin(pmin(3.40282347e38f, a.x), b.x), c.x);
+    r.mny = pmin(pmin(pmin(3.40282347e38f, a.y), b.y), c.y);
+    r.mnz = pmin(pmin(pmin(3.40282347e38f, a.z), b.z), c.z);
+    r.mxx = pmax(pmax(pmax(-3.40282347e38f, a.x), b.x), c.x);
+    r.mxy = pmax(pmax(pmax(-3.40282347e38f, a.y), b.y), c.y);
+    r.mxz = pmax(pmax(pmax(-3.40282347e38f, a.z), b.z), c.z);
+    return r;
+}
+// AABB.Intersect with the reference's maxZ := Min(aabb.Max.Y, aabb2.Max.Z)
+// (geometry/primitive/box.go:32-41); `a` is the viewport box.
+PR_DEV bool box_intersect(const Box& a, const Box& b) {
+    float minX = pmax(a.mnx, b.mnx), minY = pmax(a.mny, b.mny), minZ = pmax(a.mnz, b.mnz);
+    float maxX = pmin(a.mxx, b.mxx), maxY = pmin(a.mxy, b.mxy), maxZ = pmin(a.mxy, b.mxz);
+    return minX <= maxX && minY <= maxY && minZ <= maxZ;
+}
+PR_DEV bool box_contains(const Box& a, V4 v) {
+    return le_approx(a.mnx, v.x) && le_approx(a.mny, v.y) && le_approx(a.mnz, v.z) && le_approx(v.x, a.mxx) &&
+           le_approx(v.y, a.mxy) && le_approx(v.z, a.mxz);
+}
+
+// Pixel rectangle of drawClipped / drawDepth (render/raster.go:473-477),
+// clamped to the W x H buffer. Returns false when empty.
+PR_DEV bool pixel_box(V4 a, V4 b, V4 c, int W, int H, uint32_t* bx, uint32_t* by, uint32_t* area) {
+    Box r = box3(a, b, c);
+    long long xmin = go_f2i(__fsub_rn(pround(r.mnx), 1.0f));
+    long long xmax = go_f2i(__fadd_rn(pround(r.mxx), 1.0f));
+    long long ymin = go_f2i(__fsub_rn(pround(r.mny), 1.0f));
+    long long ymax = go_f2i(__fadd_rn(pround(r.mxy), 1.0f));
+    long long x0 = xmin < 0 ? 0 : xmin, x1 = xmax > W - 1 ? W - 1 : xmax;
+    long long y0 = ymin < 0 ? 0 : ymin, y1 = ymax > H - 1 ? H - 1 : ymax;
+    if (x0 > x1 || y0 > y1) return false;
+    *bx = (uint32_t)x0 | ((uint32_t)x1 << 16);
+    *by = (uint32_t)y0 | ((uint32_t)y1 << 16);
+    *area = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+    return true;
+}
+
+PR_DEV uint32_t find_object(const uint32_t* first, uint32_t n_obj, uint32_t t) {
+    uint32_t lo = 0, hi = n_obj - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+PR_DEV uint32_t pack_col(uchar4 c) { return (uint32_t)c.x | ((uint32_t)c.y << 8) | ((uint32_t)c.z << 16) | ((uint32_t)c.w << 24); }
+PR_DEV float col_ch(uint32_t c, int k) { return (float)((c >> (8 * k)) & 0xffu); }
+
+struct SubVtx {
+    V4 pos;
+    V4 nor;
+    float u, v;
+    uint32_t col;
+};
+
+// clipTriangle's re-interpolated vertex (render/clipping.go:75-102)
+PR_DEV SubVtx clip_vertex(V4 cp, const SubVtx* t, float psabc) {
+    float b[3];
+    barycoord_s(cp.x, cp.y, t[0].pos.x, t[0].pos.y, t[1].pos.x, t[1].pos.y, t[2].pos.x, t[2].pos.y, psabc, b);
+    SubVtx r;
+    auto lerp3 = [&](float a0, float a1, float a2) {
+        return __fadd_rn(__fadd_rn(__fmul_rn(b[0], a0), __fmul_rn(b[1], a1)), __fmul_rn(b[2], a2));
+    };
+    r.pos = {lerp3(t[0].pos.x, t[1].pos.x, t[2].pos.x), lerp3(t[0].pos.y, t[1].pos.y, t[2].pos.y),
+             lerp3(t[0].pos.z, t[1].pos.z, t[2].pos.z), 1.0f};
+    r.u = lerp3(t[0].u, t[1].u, t[2].u);
+    r.v = lerp3(t[0].v, t[1].v, t[2].v);
+    r.nor = {lerp3(t[0].nor.x, t[1].nor.x, t[2].nor.x), lerp3(t[0].nor.y, t[1].nor.y, t[2].nor.y),
+             lerp3(t[0].nor.z, t[1].nor.z, t[2].nor.z), 0.0f};
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float s = lerp3(col_ch(t[0].col, k), col_ch(t[1].col, k), col_ch(t[2].col, k));
+        c |= go_f2u8(pclamp(s, 0.0f, 255.0f)) << (8 * k);
+    }
+    r.col = c;
+    return r;
+}
+
+// plane.intersectSegment(v0, v1) (render/clipping.go:23-30)
+PR_DEV V4 intersect_segment(V4 P, V4 N, V4 v0, V4 v1) {
+    V4 u = sub4(v1, v0);
+    V4 w = sub4(v0, P);
+    float d = dot4(N, u);
+    float nn = -dot4(N, w);
+    float sc = __fdiv_rn(nn, d);
+    return add4(v0, V4{__fmul_rn(u.x, sc), __fmul_rn(u.y, sc), __fmul_rn(u.z, sc), __fmul_rn(u.w, sc)});
+}
+
+// Sutherland-Hodgman against the six screen-space planes
+// (render/clipping.go:31-68). Returns the vertex count (<= 9), or -1 when a
+// polygon with NaN coordinates outgrows that bound.
+PR_DEV int sutherland_hodgman(const V4* in3, float w, float h, V4* out) {
+    V4 buf[2][10];
+    int n = 3;
+    for (int i = 0; i < 3; i++) buf[0][i] = in3[i];
+    int cur = 0;
+    const float pp[6][4] = {{w, 0, 0, 1}, {0, 0, 0, 1}, {0, h, 0, 1}, {0, 0, 0, 1}, {0, 0, 1, 1}, {0, 0, -1, 1}};
+    const float pn[6][4] = {{-1, 0, 0, 1}, {1, 0, 0, 1}, {0, -1, 0, 1}, {0, 1, 0, 1}, {0, 0, -1, 1}, {0, 0, 1, 1}};
+    for (int pl = 0; pl < 6; pl++) {
+        if (n == 0) return 0;
+        V4 P = {pp[pl][0], pp[pl][1], pp[pl][2], pp[pl][3]};
+        V4 N = {pn[pl][0], pn[pl][1], pn[pl][2], pn[pl][3]};
+        const V4* inp = buf[cur];
+        V4* o = buf[cur ^ 1];
+        int m = 0;
+        V4 s = inp[n - 1];
+        for (int i = 0; i < n; i++) {
+            V4 e = inp[i];
+            bool fe = dot4(sub4(e, P), N) > 0.0f;  // plane.pointInFront
+            bool fs = dot4(sub4(s, P), N) > 0.0f;
+            // A convex polygon gains at most one vertex per plane (<= 9 in
+            // all); more means NaN coordinates broke convexity.
+            if (m + (fe && !fs ? 2 : 1) > 9) return -1;
+            if (fe) {
+                if (!fs) o[m++] = intersect_segment(P, N, s, e);
+                o[m++] = e;
+            } else if (fs) {
+                o[m++] = intersect_segment(P, N, s, e);
+            }
+            s = e;
+        }
+        n = m;
+        cur ^= 1;
+    }
+    for (int i = 0; i < n; i++) out[i] = buf[cur][i];
+    return n;
+}
+
+// Build and store the records of one sub-triangle; returns its pixel area
+// (0 = nothing to raster) and writes its bbox words.
+PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, const SubVtx* v, const float* recipw,
+                          int matid) {
+    RasterRec R;
+    R.x[0] = v[0].pos.x; R.y[0] = v[0].pos.y; R.z[0] = v[0].pos.z;
+    R.x[1] = v[1].pos.x; R.y[1] = v[1].pos.y; R.z[1] = v[1].pos.z;
+    R.x[2] = v[2].pos.x; R.y[2] = v[2].pos.y; R.z[2] = v[2].pos.z;
+    R.sabc = sabc_of(R.x[0], R.y[0], R.x[1], R.y[1], R.x[2], R.y[2]);
+    R.seq = seq;
+    uint32_t area = 0;
+    if (!pixel_box(v[0].pos, v[1].pos, v[2].pos, P.W, P.H, &R.bx, &R.by, &area)) {
+        R.bx = 1u;  // x0 = 1 > x1 = 0: empty
+        R.by = 0u;
+        area = 0;
+    }
+    R.pad[0] = R.pad[1] = R.pad[2] = 0;
+    const float4* rs = reinterpret_cast<const float4*>(&R);
+    float4* rd = reinterpret_cast<float4*>(P.rrec + ridx);
+#pragma unroll
+    for (int k = 0; k < 4; k++) rd[k] = rs[k];
+    if (P.arec) {
+        AttrRec A;
+        V4 m[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            A.recipw[k] = recipw[k];
+            A.nor[k * 3 + 0] = v[k].nor.x;
+            A.nor[k * 3 + 1] = v[k].nor.y;
+            A.nor[k * 3 + 2] = v[k].nor.z;
+            A.uv[k * 2 + 0] = v[k].u;
+            A.uv[k * 2 + 1] = v[k].v;
+            A.col[k] = v[k].col;
+            // render/raster.go:467-469
+            m[k] = apply4(apply4(apply4(v[k].pos, P.viewport_inv), P.proj_inv), P.view_inv);
+            A.m[k * 3 + 0] = m[k].x;
+            A.m[k * 3 + 1] = m[k].y;
+            A.m[k * 3 + 2] = m[k].z;
+        }
+        V4 fn = unit4(cross4(sub4(m[1], m[0]), sub4(m[2], m[0])));  // render/raster.go:479
+        A.fn[0] = fn.x; A.fn[1] = fn.y; A.fn[2] = fn.z; A.fn[3] = fn.w;
+        A.matid = matid;
+        const float4* as = reinterpret_cast<const float4*>(&A);
+        float4* ad = reinterpret_cast<float4*>(P.arec + ridx);
+#pragma unroll
+        for (int k = 0; k < 9; k++) ad[k] = as[k];
+    }
+    return area;
+}
+
+PR_DEV void emit_tasks(const SetupParams& P, const uint32_t* ridx, const uint32_t* area, int n) {
+    uint32_t total = 0;
+    for (int i = 0; i < n; i++) total += (area[i] + kTaskPx - 1) / kTaskPx;
+    if (total == 0) return;
+    uint32_t base = atomicAdd(&P.cnt->n_tasks, total);
+    if (base + total > P.cap_tasks) {
+        atomicOr(&P.cnt->overflow, 2u);
+        atomicMax(&P.cnt->need_tasks, base + total);
+        return;
+    }
+    uint32_t o = base;
+    for (int i = 0; i < n; i++) {
+        uint32_t nt = (area[i] + kTaskPx - 1) / kTaskPx;
+        for (uint32_t c = 0; c < nt; c++) P.tasks[o++] = make_uint2(ridx[i], c);
+    }
+}
+
+// cpuForwardPass + draw for one input triangle (render/raster.go:257-269, 380-444)
+__global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.n_tris) return;
+    uint32_t o = find_object(P.obj_first, P.n_objects, t);
+    V4 p[3], nn[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        p[k] = ld4(P.pos[t * 3 + k]);
+        nn[k] = ld4(P.nor[t * 3 + k]);
+    }
+    if (!tri_is_valid(p[0], p[1], p[2])) return;
+    int matid = P.mat[t];
+    if (matid >= 0) matid += P.obj_matbase[o];
+    float trans[16];
+    mulm(P.pv, P.obj_model + o * 16, trans);
+    const float* nm = P.obj_normal + o * 16;
+    SubVtx v[3];
+    float recipw[3] = {1.0f, 1.0f, 1.0f};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        V4 cp = mulv(trans, p[k]);
+        if (P.perspective) recipw[k] = __fdiv_rn(-1.0f, cp.w);
+        v[k].pos = pos4(apply4(cp, P.viewport));
+        v[k].nor = apply4(nn[k], nm);
+        float2 uv = P.uv[t * 3 + k];
+        v[k].u = uv.x;
+        v[k].v = uv.y;
+        v[k].col = pack_col(P.col[t * 3 + k]);
+    }
+    // cullBackFace (render/cull.go:26-28)
+    if (cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y), __fsub_rn(v[2].pos.x, v[0].pos.x),
+                __fsub_rn(v[2].pos.y, v[0].pos.y)) < 0.0f)
+        return;
+    Box vp = {0.0f, 0.0f, -1.0f, (float)P.W, (float)P.H, 1.0f};
+    Box tb = box3(v[0].pos, v[1].pos, v[2].pos);
+    if (!box_intersect(vp, tb)) return;
+    uint32_t seq0 = t * 8u;
+    if (box_contains(vp, v[0].pos) && box_contains(vp, v[1].pos) && box_contains(vp, v[2].pos)) {
+        uint32_t ridx = atomicAdd(&P.cnt->n_rec, 1u);
+        if (ridx >= P.cap_rec) {
+            atomicOr(&P.cnt->overflow, 1u);
+            atomicMax(&P.cnt->need_rec, ridx + 1);
+            return;
+        }
+        P.first_rec[t] = ridx;
+        uint32_t area = write_sub(P, ridx, seq0, v, recipw, matid);
+        emit_tasks(P, &ridx, &area, 1);
+        return;
+    }
+    // clipTriangle (render/clipping.go:70-157)
+    atomicAdd(&P.cnt->n_clipped, 1u);
+    V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
+    V4 clips[10];
+    int nc = sutherland_hodgman(in3, (float)P.W, (float)P.H, clips);
+    if (nc < 0) {
+        atomicOr(&P.cnt->overflow, 4u);
+        return;
+    }
+    int nsub = nc - 2;
+    if (nsub <= 0) return;
+    uint32_t base = atomicAdd(&P.cnt->n_rec, (uint32_t)nsub);
+    if (base + nsub > P.cap_rec) {
+        atomicOr(&P.cnt->overflow, 1u);
+        atomicMax(&P.cnt->need_rec, base + nsub);
+        return;
+    }
+    P.first_rec[t] = base;
+    float psabc = sabc_of(v[0].pos.x, v[0].pos.y, v[1].pos.x, v[1].pos.y, v[2].pos.x, v[2].pos.y);
+    uint32_t ridxs[8], areas[8];
+    SubVtx s[3];
+    s[0] = clip_vertex(clips[0], v, psabc);
+    for (int i = 2; i < nc; i++) {
+        s[1] = clip_vertex(clips[i - 1], v, psabc);
+        s[2] = clip_vertex(clips[i], v, psabc);
+        uint32_t ridx = base + (uint32_t)(i - 2);
+        ridxs[i - 2] = ridx;
+        areas[i - 2] = write_sub(P, ridx, seq0 + (uint32_t)(i - 2), s, recipw, matid);
+    }
+    emit_tasks(P, ridxs, areas, nsub);
+}
+
+// passShadows / drawDepth for one input triangle (render/shadow.go:137-192)
+__global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.n_tris) return;
+    uint32_t o = find_object(P.obj_first, P.n_objects, t);
+    V4 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) p[k] = ld4(P.pos[t * 3 + k]);
+    if (!tri_is_valid(p[0], p[1], p[2])) return;
+    float trans[16];
+    mulm(P.pv, P.obj_model + o * 16, trans);
+    SubVtx v[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        v[k].pos = pos4(apply4(mulv(trans, p[k]), P.viewport));
+        v[k].nor = {0, 0, 0, 0};
+        v[k].u = v[k].v = 0;
+        v[k].col = 0;
+    }
+    if (cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y), __fsub_rn(v[2].pos.x, v[0].pos.x),
+                __fsub_rn(v[2].pos.y, v[0].pos.y)) < 0.0f)
+        return;
+    // cullViewFrustum (render/cull.go:15-23): NewAABB((W,H,1),(0,0,0),(0,0,-1))
+    Box vp = box3(V4{(float)P.W, (float)P.H, 1.0f, 1.0f}, V4{0, 0, 0, 1}, V4{0, 0, -1.0f, 1});
+    Box tb = box3(v[0].pos, v[1].pos, v[2].pos);
+    if (!box_intersect(vp, tb)) return;
+    float rw[3] = {1, 1, 1};
+    uint32_t area = write_sub(P, t, t, v, rw, -1);
+    emit_tasks(P, &t, &area, 1);
+}
+
+// ---------------------------------------------------------------- raster
+
+constexpr int kRasterWarps = 8;
+
+struct SmRec {
+    float x[3], y[3], z[3], sabc;
+    uint32_t x0, y0, bw, seq, k0;
+};
+
+// Coverage and depth of one pixel against one record (drawClipped's
+// Barycoord / inside / z lines, render/raster.go:487-496).
+PR_DEV bool pixel_depth(const SmRec& r, int px, int py, float* zout) {
+    float fx = __fadd_rn((float)px, 0.5f), fy = __fadd_rn((float)py, 0.5f);
+    float apx = __fsub_rn(fx, r.x[0]), apy = __fsub_rn(fy, r.y[0]);
+    float abx = __fsub_rn(r.x[1], r.x[0]), aby = __fsub_rn(r.y[1], r.y[0]);
+    float acx = __fsub_rn(r.x[2], r.x[0]), acy = __fsub_rn(r.y[2], r.y[0]);
+    float bcx = __fsub_rn(r.x[2], r.x[1]), bcy = __fsub_rn(r.y[2], r.y[1]);
+    float bpx = __fsub_rn(fx, r.x[1]), bpy = __fsub_rn(fy, r.y[1]);
+    float sabc = r.sabc;
+    float as = fabsf(sabc);
+    if (as >= 1e-30f && as <= 1e30f) {
+        // Conservative early reject: the single-rounding estimate differs from
+        // the reference's double rounding by at most one ulp, so a margin of
+        // 2^-20 relative decides only pixels that are certainly outside.
+        float inv = __frcp_rn(sabc);
+        float w0 = __fmul_rn(__fmaf_rn(bcx, bpy, -__fmul_rn(bcy, bpx)), inv);
+        float w1 = __fmul_rn(__fmaf_rn(apx, acy, -__fmul_rn(apy, acx)), inv);
+        float w2 = __fmul_rn(__fmaf_rn(abx, apy, -__fmul_rn(aby, apx)), inv);
+        const float shrink = 0.99999904632568359375f;  // 1 - 2^-20
+        if (__fmul_rn(w0, shrink) < -kEps || __fmul_rn(w1, shrink) < -kEps || __fmul_rn(w2, shrink) < -kEps)
+            return false;
+    }
+    float sabp = cross_z(abx, aby, apx, apy);
+    float sapc = cross_z(apx, apy, acx, acy);
+    float sbcp = cross_z(bcx, bcy, bpx, bpy);
+    float b0 = __fdiv_rn(sbcp, sabc), b1 = __fdiv_rn(sapc, sabc), b2 = __fdiv_rn(sabp, sabc);
+    if (b0 < -kEps || b1 < -kEps || b2 < -kEps) return false;
+    *zout = __fadd_rn(__fadd_rn(__fmul_rn(b0, r.z[0]), __fmul_rn(b1, r.z[1])), __fmul_rn(b2, r.z[2]));
+    return true;
+}
+
+__global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_constant__ RasterParams P) {
+    __shared__ SmRec s_rec[kRasterWarps][32];
+    __shared__ int s_start[kRasterWarps][32];
+    const Counters* c = P.cnt;
+    if (P.mode == kMainFixup || P.mode == kShadowFixup) {
+        if (c->nan_flag == 0) return;
+    }
+    uint32_t n_tasks = c->n_tasks;
+    if (c->overflow) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t gw = blockIdx.x * kRasterWarps + warp, nw = gridDim.x * kRasterWarps;
+    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) {
+        uint32_t ti = base + lane;
+        int cnt = 0;
+        if (ti < n_tasks) {
+            uint2 tk = P.tasks[ti];
+            const float4* rp = reinterpret_cast<const float4*>(P.rrec + tk.x);
+            float4 q0 = rp[0], q1 = rp[1], q2 = rp[2], q3 = rp[3];
+            SmRec& s = s_rec[warp][lane];
+            s.x[0] = q0.x; s.y[0] = q0.y; s.z[0] = q0.z;
+            s.x[1] = q0.w; s.y[1] = q1.x; s.z[1] = q1.y;
+            s.x[2] = q1.z; s.y[2] = q1.w; s.z[2] = q2.x;
+            s.sabc = q2.y;
+            uint32_t bx = __float_as_uint(q2.z), by = __float_as_uint(q2.w);
+            s.seq = __float_as_uint(q3.x);
+            uint32_t x0 = bx & 0xffffu, x1 = bx >> 16, y0 = by & 0xffffu, y1 = by >> 16;
+            if (x0 <= x1 && y0 <= y1) {
+                uint32_t bw = x1 - x0 + 1, area = bw * (y1 - y0 + 1);
+                uint32_t k0 = tk.y * (uint32_t)kTaskPx;
+                if (k0 < area) cnt = (int)min(area - k0, (uint32_t)kTaskPx);
+                s.x0 = x0;
+                s.y0 = y0;
+                s.bw = bw;
+                s.k0 = k0;
+            }
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += v;
+        }
+        s_start[warp][lane] = incl - cnt;
+        int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        for (int g = lane; g < total; g += 32) {
+            int j = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (s_start[warp][j + step] <= g) j += step;
+            const SmRec& r = s_rec[warp][j];
+            uint32_t k = r.k0 + (uint32_t)(g - s_start[warp][j]);
+            uint32_t qy = k / r.bw;
+            int px = (int)(r.x0 + (k - qy * r.bw));
+            int py = (int)(r.y0 + qy);
+            float z;
+            if (!pixel_depth(r, px, py, &z)) continue;
+            bool zn = isnan(z);
+            if (P.mode == kMain) {
+                size_t i = (size_t)(P.H - 1 - py) * P.W + px;
+                if (zn) {
+                    atomicMin(&P.nanseq[i], r.seq);
+                    atomicExch(&P.cnt_w->nan_flag, 1u);
+                    atomicAdd(&P.cnt_w->n_nan, 1u);
+                } else {
+                    unsigned long long key = ((unsigned long long)fkey(z) << 32) | (unsigned long long)(0xFFFFFFFFu - r.seq);
+                    atomicMax(&P.keys[i], key);
+                }
+            } else if (P.mode == kMainFixup) {
+                size_t i = (size_t)(P.H - 1 - py) * P.W + px;
+                if (!zn) {
+                    uint32_t ns = P.nanseq[i];
+                    if (ns != kNone && r.seq < ns) P.beaten[i] = 1u;
+                }
+            } else if (P.mode == kShadow) {
+                size_t i = (size_t)px + (size_t)py * P.W;
+                if (zn) {
+                    atomicMax(&P.lastnan[i], r.seq + 1u);
+                    atomicExch(&P.cnt_w->nan_flag, 1u);
+                    atomicAdd(&P.cnt_w->n_nan, 1u);
+                } else {
+                    atomicMax(&P.smap[i], fkey(z));
+                }
+            } else {  // kShadowFixup
+                size_t i = (size_t)px + (size_t)py * P.W;
+                uint32_t ln = P.lastnan[i];
+                if (!zn && ln != 0u && r.seq + 1u > ln) atomicMax(&P.smap[i], fkey(z));
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void resolve_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
+                               const uint32_t* beaten, const Counters* cnt, uint32_t* win, float* depth_ao) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)W * H) return;
+    unsigned long long key = keys[i];
+    uint32_t w = kNone;
+    float d = -1.0f;
+    if (cnt->nan_flag && nanseq[i] != kNone && beaten[i] == 0u) {
+        w = nanseq[i];
+        d = __uint_as_float(0x7fc00000u);
+    } else if (key != 0ull) {
+        w = 0xFFFFFFFFu - (uint32_t)(key & 0xFFFFFFFFull);
+        d = fkey_decode((uint32_t)(key >> 32));
+    }
+    win[i] = w;
+    depth_ao[i] = d;
+}
+
+// Shadow NaN fix-up: pixels that saw a NaN-depth fragment restart from NaN
+// (key 0) and take the maximum over the fragments drawn after the last one.
+__global__ void shadow_fixup_reset_kernel(size_t n, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt) {
+    if (cnt->nan_flag == 0) return;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && lastnan[i] != 0u) smap[i] = 0u;
+}
+
+__global__ void decode_shadow_kernel(const uint32_t* smap, float* out, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = fkey_decode(smap[i]);
+}
+
+// ---------------------------------------------------------------- shade
+
+// Go math.Pow(0.5, n) for an integer 0 <= n <= 16 is exactly 2^-n.
+PR_DEV float pow_half(int n) { return __uint_as_float((uint32_t)(127 - n) << 23); }
+
+__global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.W || r >= P.H) return;
+    const int W = P.W, H = P.H;
+    const int y = H - 1 - r;
+    const size_t i = (size_t)r * W + x;
+    const uint32_t seq = P.win[i];
+    uint32_t c0, c1, c2, c3;
+    if (seq == kNone) {
+        c0 = P.background[0]; c1 = P.background[1]; c2 = P.background[2]; c3 = P.background[3];
+        if (P.tri_id) P.tri_id[i] = kNone;
+        if (P.depth) P.depth[i] = 0.0f;
+        if (P.gnor) P.gnor[i] = make_float4(0, 0, 0, 0);
+        if (P.gfnor) P.gfnor[i] = make_float4(0, 0, 0, 0);
+        if (P.gwpos) P.gwpos[i] = make_float4(0, 0, 0, 0);
+        if (P.guvd) P.guvd[i] = make_float4(0, 0, 0, 0);
+        if (P.gvcol) P.gvcol[i] = make_uchar4(0, 0, 0, 0);
+        if (P.gmat) P.gmat[i] = -1;
+    } else {
+        const uint32_t ridx = P.first_rec[seq >> 3] + (seq & 7u);
+        const float4* rp = reinterpret_cast<const float4*>(P.rrec + ridx);
+        float4 q0 = rp[0], q1 = rp[1], q2 = rp[2];
+        const float X0 = q0.x, Y0 = q0.y, Z0 = q0.z, X1 = q0.w, Y1 = q1.x, Z1 = q1.y, X2 = q1.z, Y2 = q1.w, Z2 = q2.x;
+        const float sabc = q2.y;
+        const AttrRec& A = P.arec[ridx];
+        const float fx = __fadd_rn((float)x, 0.5f), fy = __fadd_rn((float)y, 0.5f);
+        float bc[3];
+        barycoord_s(fx, fy, X0, Y0, X1, Y1, X2, Y2, sabc, bc);
+        const float z = __fadd_rn(__fadd_rn(__fmul_rn(bc[0], Z0), __fmul_rn(bc[1], Z1)), __fmul_rn(bc[2], Z2));
+        const float rw0 = A.recipw[0], rw1 = A.recipw[1], rw2 = A.recipw[2];
+        const float wc1 = __fmul_rn(rw0, bc[0]), wc2 = __fmul_rn(rw1, bc[1]), wc3 = __fmul_rn(rw2, bc[2]);
+        const bool persp = (P.flags & PR_FRAME_PERSPECTIVE) != 0;
+        const float norm = persp ? __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(wc1, wc2), wc3)) : 1.0f;
+        auto wsum = [&](float a, float b, float c, float w1, float w2, float w3) {
+            return __fadd_rn(__fadd_rn(__fmul_rn(w1, a), __fmul_rn(w2, b)), __fmul_rn(w3, c));
+        };
+        const float uvX = __fmul_rn(wsum(A.uv[0], A.uv[2], A.uv[4], wc1, wc2, wc3), norm);
+        const float uvY = __fmul_rn(wsum(A.uv[1], A.uv[3], A.uv[5], wc1, wc2, wc3), norm);
+        const int matid = A.matid;
+        float du = 0.0f, dv = 0.0f;
+        if (matid >= 0) {
+            float bx3[3], by3[3];
+            barycoord_s(__fadd_rn(fx, 1.0f), fy, X0, Y0, X1, Y1, X2, Y2, sabc, bx3);
+            float wc1x = __fmul_rn(rw0, bx3[0]), wc2x = __fmul_rn(rw1, bx3[1]), wc3x = __fmul_rn(rw2, bx3[2]);
+            float normx = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(wc1x, wc2x), wc3x));
+            barycoord_s(fx, __fadd_rn(fy, 1.0f), X0, Y0, X1, Y1, X2, Y2, sabc, by3);
+            float wc1y = __fmul_rn(rw0, by3[0]), wc2y = __fmul_rn(rw1, by3[1]), wc3y = __fmul_rn(rw2, by3[2]);
+            float normy = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(wc1y, wc2y), wc3y));
+            float uvdU = __fmul_rn(wsum(A.uv[0], A.uv[2], A.uv[4], wc1x, wc2x, wc3x), normx);
+            float uvdX = __fmul_rn(wsum(A.uv[1], A.uv[3], A.uv[5], wc1x, wc2x, wc3x), normx);
+            float uvdV = __fmul_rn(wsum(A.uv[0], A.uv[2], A.uv[4], wc1y, wc2y, wc3y), normy);
+            float uvdY = __fmul_rn(wsum(A.uv[1], A.uv[3], A.uv[5], wc1y, wc2y, wc3y), normy);
+            float a = __fsub_rn(uvdU, uvX), b = __fsub_rn(uvdX, uvY);
+            du = __fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b));
+            float c = __fsub_rn(uvdV, uvX), d = __fsub_rn(uvdY, uvY);
+            dv = __fadd_rn(__fmul_rn(c, c), __fmul_rn(d, d));
+        }
+        const V4 n = unit4(V4{wsum(A.nor[0], A.nor[3], A.nor[6], bc[0], bc[1], bc[2]),
+                              wsum(A.nor[1], A.nor[4], A.nor[7], bc[0], bc[1], bc[2]),
+                              wsum(A.nor[2], A.nor[5], A.nor[8], bc[0], bc[1], bc[2]), 0.0f});
+        const V4 wp = {wsum(A.m[0], A.m[3], A.m[6], bc[0], bc[1], bc[2]), wsum(A.m[1], A.m[4], A.m[7], bc[0], bc[1], bc[2]),
+                       wsum(A.m[2], A.m[5], A.m[8], bc[0], bc[1], bc[2]), 1.0f};
+        const V4 fn = {A.fn[0], A.fn[1], A.fn[2], A.fn[3]};
+        uint32_t vc[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            float s = __fmul_rn(wsum(col_ch(A.col[0], k), col_ch(A.col[1], k), col_ch(A.col[2], k), wc1, wc2, wc3), norm);
+            vc[k] = go_f2u8(pclamp(s, 0.0f, 255.0f));
+        }
+        if (P.tri_id) P.tri_id[i] = seq >> 3;
+        if (P.depth) P.depth[i] = z;
+        if (P.gnor) P.gnor[i] = make_float4(n.x, n.y, n.z, n.w);
+        if (P.gfnor) P.gfnor[i] = make_float4(fn.x, fn.y, fn.z, fn.w);
+        if (P.gwpos) P.gwpos[i] = make_float4(wp.x, wp.y, wp.z, wp.w);
+        if (P.guvd) P.guvd[i] = make_float4(uvX, uvY, du, dv);
+        if (P.gvcol) P.gvcol[i] = make_uchar4(vc[0], vc[1], vc[2], vc[3]);
+        if (P.gmat) P.gmat[i] = matid;
+
+        c0 = vc[0]; c1 = vc[1]; c2 = vc[2]; c3 = vc[3];
+        const pr_material* mat = (matid >= 0 && (uint32_t)matid < P.n_mats) ? &P.mats[matid] : nullptr;
+        if (mat) {
+            // FragmentShader (shader/blinn_cpu.go:24-106), uniform texture
+            const uint32_t t0 = mat->texture[0], t1 = mat->texture[1], t2 = mat->texture[2], t3 = mat->texture[3];
+            if (P.n_lights == 0) {
+                c0 = t0; c1 = t1; c2 = t2; c3 = t3;
+            } else {
+                const float cr = (float)t0, cg = (float)t1, cb = (float)t2;
+                float LaR = 0, LaG = 0, LaB = 0;
+                for (int e = 0; e < P.n_ambient; e++) {
+                    LaR = __fadd_rn(LaR, __fmul_rn(P.ambient[e], cr));
+                    LaG = __fadd_rn(LaG, __fmul_rn(P.ambient[e], cg));
+                    LaB = __fadd_rn(LaB, __fmul_rn(P.ambient[e], cb));
+                }
+                float LdR = 0, LdG = 0, LdB = 0, LsR = 0, LsG = 0, LsB = 0;
+                const V4 nn = (mat->flags & PR_MAT_FLAT_SHADING) ? fn : n;
+                const V4 cam = {P.cam[0], P.cam[1], P.cam[2], 1.0f};
+                const double shin = (double)mat->shininess;
+                for (int li = 0; li < P.n_lights; li++) {
+                    const LightK& L = P.lights[li];
+                    V4 Lv;
+                    float I;
+                    if (L.type == PR_LIGHT_POINT) {
+                        V4 Ldir = sub4(V4{L.pos[0], L.pos[1], L.pos[2], 1.0f}, wp);
+                        Lv = unit4(Ldir);
+                        I = __fdiv_rn(L.intensity, len4(Ldir));
+                    } else {
+                        Lv = V4{-L.dir[0], -L.dir[1], -L.dir[2], 0.0f};
+                        I = L.intensity;
+                    }
+                    V4 Vv = unit4(sub4(cam, wp));
+                    V4 Hv = unit4(add4(Lv, Vv));
+                    float Ld = pclamp(dot4(nn, Lv), 0.0f, 1.0f);
+                    float Ls = __double2float_rn(go_pow((double)pclamp(dot4(nn, Hv), 0.0f, 1.0f), shin));
+                    LdR = __fadd_rn(LdR, __fmul_rn(__fmul_rn(Ld, cr), I));
+                    LdG = __fadd_rn(LdG, __fmul_rn(__fmul_rn(Ld, cg), I));
+                    LdB = __fadd_rn(LdB, __fmul_rn(__fmul_rn(Ld, cb), I));
+                    LsR = __fadd_rn(LsR, __fmul_rn(__fmul_rn(Ls, L.color[0]), I));
+                    LsG = __fadd_rn(LsG, __fmul_rn(__fmul_rn(Ls, L.color[1]), I));
+                    LsB = __fadd_rn(LsB, __fmul_rn(__fmul_rn(Ls, L.color[2]), I));
+                }
+                auto fin = [&](float La, float Ld, float Ls, uint8_t kd, uint8_t ks) {
+                    float v = __fadd_rn(__fadd_rn(La, __fdiv_rn(__fmul_rn((float)kd, Ld), 255.0f)),
+                                        __fdiv_rn(__fmul_rn((float)ks, Ls), 255.0f));
+                    return go_f2u8(pclamp(pround(v), 0.0f, 255.0f));
+                };
+                c0 = fin(LaR, LdR, LsR, mat->diffuse[0], mat->specular[0]);
+                c1 = fin(LaG, LdG, LsG, mat->diffuse[1], mat->specular[1]);
+                c2 = fin(LaB, LdB, LsB, mat->diffuse[2], mat->specular[2]);
+                c3 = t3;
+            }
+            // Shadows (render/raster.go:339-352, render/shadow.go:230-283)
+            if ((P.flags & PR_FRAME_SHADOWMAP) && (mat->flags & PR_MAT_RECEIVE_SHADOW)) {
+                int occl = 0;
+                const size_t plane = (size_t)P.SW * P.SH;
+                for (int li = 0; li < P.n_lights; li++) {
+                    const LightK& L = P.lights[li];
+                    if (!L.cast) {
+                        occl++;
+                        continue;
+                    }
+                    V4 sc = pos4(apply4(apply4(apply4(apply4(V4{(float)x, (float)y, z, 1.0f}, P.s2w), L.lview), L.lproj),
+                                        P.shadow_vp));
+                    long long lx = go_f2i(sc.x), ly = go_f2i(sc.y);
+                    long long idx = (long long)((unsigned long long)lx + (unsigned long long)ly * (unsigned long long)(long long)P.SW);
+                    if (idx > 0 && idx < (long long)plane) {
+                        float sz = fkey_decode(P.smaps[plane * li + (size_t)idx]);
+                        if (sc.z < __fsub_rn(sz, 0.03f)) occl++;
+                    }
+                }
+                float w = pow_half(occl);
+                c0 = go_f2u8(__fmul_rn((float)c0, w));
+                c1 = go_f2u8(__fmul_rn((float)c1, w));
+                c2 = go_f2u8(__fmul_rn((float)c2, w));
+            }
+            // AmbientOcclusionShade (material/ao.go:20-73). maxangle is
+            // Max over taps of float32(Atan(elev/dist)); Atan and the float32
+            // rounding are monotone, so it equals float32(Atan(max ratio)),
+            // and only positive ratios can exceed the initial 0. A NaN ratio
+            // makes the direction's result NaN (Go's Max propagates NaN).
+            if (mat->flags & PR_MAT_AO) {
+                const float pxf = (float)x, pyf = (float)y;
+                float total = 0.0f;
+                for (int k = 0; k < P.n_ao; k++) {
+                    const float dX = P.ao_cos[k], dY = P.ao_sin[k];
+                    float best = 0.0f;
+                    bool nanr = false;
+                    for (int ti = 0; ti < 100; ti++) {
+                        const float t = (float)ti;
+                        const float cx = __fadd_rn(pxf, __fmul_rn(dX, t));
+                        const float cy = __fadd_rn(pyf, __fmul_rn(dY, t));
+                        const long long ix = go_f2i(cx), iy = go_f2i(cy);
+                        if (ix < 0 || ix >= W || iy < 0 || iy >= H) break;
+                        const float sd = P.depth_ao[(size_t)(H - 1 - iy) * W + (size_t)ix];
+                        const float elev = __fsub_rn(sd, z);
+                        if (!(elev > 0.0f) && !isnan(elev)) continue;
+                        const float ddx = __fsub_rn(pxf, cx), ddy = __fsub_rn(pyf, cy);
+                        const float dist = __fsqrt_rn(fma64f(ddx, ddx, fma64f(ddy, ddy, 0.0f)));
+                        if (dist < 1.0f) continue;
+                        if (isnan(elev)) {
+                            nanr = true;
+                            break;
+                        }
+                        best = fmaxf(best, __fdiv_rn(elev, dist));
+                    }
+                    float ma;
+                    if (nanr)
+                        ma = __uint_as_float(0x7fc00000u);
+                    else
+                        ma = best > 0.0f ? __double2float_rn(go_atan((double)best)) : 0.0f;
+                    total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));
+                }
+                total = __fdiv_rn(total, 12.5663706143591729539f);
+                total = __double2float_rn(go_pow((double)total, 10000.0));
+                c0 = go_f2u8(__fmul_rn(total, (float)c0));
+                c1 = go_f2u8(__fmul_rn(total, (float)c1));
+                c2 = go_f2u8(__fmul_rn(total, (float)c2));
+            }
+        }
+    }
+    if (P.flags & PR_FRAME_GAMMA) {
+        c0 = P.gamma[c0];
+        c1 = P.gamma[c1];
+        c2 = P.gamma[c2];
+    }
+    if (P.rgba) P.rgba[i] = make_uchar4(c0, c1, c2, c3);
+}
+
+__global__ void fma_probe_kernel(const float* a, const float* b, const float* c, float* out, float* out_ref, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = fma64f(a[i], b[i], c[i]);
+    out_ref[i] = fma64f_slow(a[i], b[i], c[i]);
+}
+
+int check(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
+
+}  // namespace
+
+int launch_setup_main(const SetupParams& p, void* stream) {
+    if (p.n_tris == 0) return 0;
+    unsigned nb = (p.n_tris + 127) / 128;
+    setup_main_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_setup_shadow(const SetupParams& p, void* stream) {
+    if (p.n_tris == 0) return 0;
+    unsigned nb = (p.n_tris + 127) / 128;
+    setup_shadow_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_raster(const RasterParams& p, int n_blocks, void* stream) {
+    raster_kernel<<<n_blocks, kRasterWarps * 32, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
+                   const Counters* cnt, uint32_t* win, float* depth_ao, void* stream) {
+    size_t n = (size_t)W * H;
+    resolve_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(W, H, keys, nanseq, beaten, cnt, win,
+                                                                                   depth_ao);
+    return check(cudaGetLastError());
+}
+int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,
+                              void* stream) {
+    size_t n = (size_t)W * H;
+    shadow_fixup_reset_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, lastnan, smap, cnt);
+    return check(cudaGetLastError());
+}
+int launch_shade(const ShadeParams& p, void* stream) {
+    dim3 blk(32, 8);
+    dim3 grd((p.W + 31) / 32, (p.H + 7) / 8);
+    shade_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream) {
+    if (n == 0) return 0;
+    decode_shadow_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(smap, out, n);
+    return check(cudaGetLastError());
+}
+int launch_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n, void* stream) {
+    if (n <= 0) return 0;
+    fma_probe_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a, b, c, out, out_ref, n);
+    return check(cudaGetLastError());
+}
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace prk

@@ -1,0 +1,153 @@
+// pr_kernels.cuh — data layout shared by the CUDA kernels (pr_kernels.cu) and
+// the host orchestration (pr_api.cpp). Plain C++ so the host compiler can
+// include it.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <vector_types.h>
+
+#include "../../include/polyred_cuda.h"
+
+namespace prk {
+
+constexpr int kMaxLights = 16;
+constexpr int kMaxAmbient = 16;
+constexpr int kTaskPx = 1024;        // pixels of one raster task (a bbox chunk)
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+
+// Raster record: what the coverage/depth test of one (sub-)triangle needs.
+// 16 words = 64 bytes, read with four 16-byte loads.
+struct RasterRec {
+    float x[3], y[3], z[3];  // screen-space vertices after Viewport + Pos()
+    float sabc;              // Barycoord's Sabc = ab.Cross(ac).Z (exact reference bits)
+    uint32_t bx;             // x0 | x1 << 16 (pixel bbox clamped to the buffer)
+    uint32_t by;             // y0 | y1 << 16
+    uint32_t seq;            // draw order: tri*8 + clip sub-index (main view), tri (shadow)
+    uint32_t pad[3];
+};
+
+// Attribute record: the rest of drawClipped's inputs for one sub-triangle.
+// 36 words = 144 bytes.
+struct AttrRec {
+    float recipw[3];  // parent triangle's -1/W (render/raster.go:403-406, 440-443)
+    float nor[9];     // vertex normals after Apply(Normal) (xyz per vertex)
+    float uv[6];
+    uint32_t col[3];  // RGBA8 per vertex
+    float m[9];       // world positions m1..m3 (render/raster.go:467-469), xyz
+    float fn[4];      // face normal fN (render/raster.go:479)
+    int32_t matid;    // flat material id (<0 = vertex colour)
+};
+
+struct Counters {
+    uint32_t n_rec;       // records emitted (main view)
+    uint32_t n_tasks;     // raster tasks emitted
+    uint32_t overflow;    // capacity exceeded (records or tasks)
+    uint32_t n_clipped;   // input triangles that were clipped
+    uint32_t nan_flag;    // a NaN-depth fragment was produced
+    uint32_t n_nan;       // number of NaN-depth fragments
+    uint32_t need_rec;    // records needed when overflow
+    uint32_t need_tasks;  // tasks needed when overflow
+};
+
+struct LightK {
+    int32_t type, cast;
+    float pos[3], dir[3], intensity;
+    float color[3];
+    float lview[16], lproj[16];
+};
+
+// Per-view setup parameters (passed by value).
+struct SetupParams {
+    const float4* pos;
+    const float4* nor;
+    const float2* uv;
+    const uchar4* col;
+    const int32_t* mat;
+    const uint32_t* obj_first;   // [n_objects + 1]
+    const float* obj_model;      // [n_objects][16]
+    const float* obj_normal;     // [n_objects][16] Model.Inv().T()
+    const int32_t* obj_matbase;  // [n_objects]
+    uint32_t n_tris, n_objects;
+    int W, H;                    // target size (framebuffer or shadow map)
+    int perspective;
+    float pv[16];                // Proj.MulM(View)
+    float viewport[16];
+    float viewport_inv[16], proj_inv[16], view_inv[16];
+    RasterRec* rrec;
+    AttrRec* arec;
+    uint32_t cap_rec;
+    uint2* tasks;
+    uint32_t cap_tasks;
+    uint32_t* first_rec;
+    Counters* cnt;
+};
+
+enum RasterMode { kMain = 0, kMainFixup = 1, kShadow = 2, kShadowFixup = 3 };
+
+struct RasterParams {
+    const RasterRec* rrec;
+    const uint2* tasks;
+    const Counters* cnt;     // n_tasks read on the device
+    Counters* cnt_w;
+    int W, H;
+    int mode;
+    unsigned long long* keys;  // main: [H][W] (row r = H-1-y)
+    uint32_t* nanseq;          // main: min seq of NaN-depth fragments, kNone if none
+    uint32_t* beaten;          // main fix-up: 1 if a finite fragment precedes nanseq
+    uint32_t* smap;            // shadow: orderable depth keys, index x + y*W
+    uint32_t* lastnan;         // shadow: 1 + max seq of NaN-depth fragments, 0 if none
+};
+
+struct ShadeParams {
+    int W, H;
+    uint32_t flags;             // PR_FRAME_*
+    const uint32_t* win;        // winning seq per pixel
+    const float* depth_ao;      // depth where covered, -1 elsewhere (material/ao.go:57-62)
+    const uint32_t* first_rec;
+    const RasterRec* rrec;
+    const AttrRec* arec;
+    const pr_material* mats;
+    uint32_t n_mats;
+    int n_lights, n_ambient;
+    LightK lights[kMaxLights];
+    float ambient[kMaxAmbient];
+    float cam[3];
+    uint8_t background[4];
+    float s2w[16];              // ViewInv.MulM(ProjInv).MulM(ViewportInv)
+    float shadow_vp[16];        // ViewportMatrix(SW, SH)
+    int SW, SH;
+    const uint32_t* smaps;      // [n_lights][SH*SW] orderable keys
+    float ao_cos[8], ao_sin[8];
+    int n_ao;
+    uint8_t gamma[256];
+    // outputs (device pointers, may be null)
+    uchar4* rgba;
+    uint32_t* tri_id;
+    float* depth;
+    float4* gnor;
+    float4* gfnor;
+    float4* gwpos;
+    float4* guvd;
+    uchar4* gvcol;
+    int32_t* gmat;
+};
+
+}  // namespace prk
+
+// Launch wrappers implemented in pr_kernels.cu (host-callable).
+namespace prk {
+int launch_setup_main(const SetupParams& p, void* stream);
+int launch_setup_shadow(const SetupParams& p, void* stream);
+int launch_raster(const RasterParams& p, int n_blocks, void* stream);
+int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
+                   const Counters* cnt, uint32_t* win, float* depth_ao, void* stream);
+int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,
+                              void* stream);
+int launch_shade(const ShadeParams& p, void* stream);
+int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
+int launch_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n,
+                     void* stream);
+int sm_count();
+}  // namespace prk

@@ -1,0 +1,201 @@
+"""Seeded procedural scenes for the render path's workloads.
+
+  uv_sphere       latitude/longitude sphere, normals = positions
+  ground_plane    two triangles, MaterialID -1 (vertex colour, like model/plane.go)
+  small_scene     one UV sphere (64 lon x 32 lat = 3,968 triangles) on a 10x10
+                  ground, 800x500, one point light + ambient 0.1
+  sphere_field    256 spheres of 63 x 32 segments (999,936 triangles), centres
+                  U[-10,10]^3, radii U[0.2,1.5], 4 materials, point +
+                  directional light, AO and shadow maps
+  triangle_soup   small random triangles with log-normal screen area
+
+Random numbers: splitmix64 seeds a xoshiro128** generator; floats are the top
+24 bits of a draw times 2^-24.
+"""
+import math
+
+import numpy as np
+
+from . import scene as sc
+
+F32 = np.float32
+
+
+class Xoshiro128:
+    """xoshiro128** seeded from splitmix64 (public-domain generators by
+    Blackman and Vigna)."""
+
+    def __init__(self, seed):
+        s = seed & 0xFFFFFFFFFFFFFFFF
+        words = []
+        for _ in range(2):
+            s = (s + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+            z = s
+            z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+            z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+            z ^= z >> 31
+            words += [z & 0xFFFFFFFF, z >> 32]
+        self.s = words
+
+    @staticmethod
+    def _rotl(x, k):
+        return ((x << k) | (x >> (32 - k))) & 0xFFFFFFFF
+
+    def next_u32(self):
+        s = self.s
+        result = (self._rotl((s[1] * 5) & 0xFFFFFFFF, 7) * 9) & 0xFFFFFFFF
+        t = (s[1] << 9) & 0xFFFFFFFF
+        s[2] ^= s[0]
+        s[3] ^= s[1]
+        s[1] ^= s[2]
+        s[0] ^= s[3]
+        s[2] ^= t
+        s[3] = self._rotl(s[3], 11)
+        return result
+
+    def uniform(self, lo=0.0, hi=1.0):
+        return lo + (hi - lo) * ((self.next_u32() >> 8) * (1.0 / 16777216.0))
+
+    def integer(self, n):
+        return self.next_u32() % n
+
+
+def uv_sphere(lon=64, lat=32, radius=1.0, color=(255, 255, 255, 255)):
+    """A UV sphere with 2*lon*(lat-1) triangles, wound counter-clockwise seen
+    from outside; normals equal the unit positions (w = 0), positions w = 1."""
+    th = np.pi * np.arange(lat + 1) / lat
+    ph = 2 * np.pi * np.arange(lon + 1) / lon
+    P = np.zeros((lat + 1, lon + 1, 3))
+    P[..., 0] = np.sin(th)[:, None] * np.cos(ph)[None, :]
+    P[..., 1] = np.cos(th)[:, None] * np.ones_like(ph)[None, :]
+    P[..., 2] = -np.sin(th)[:, None] * np.sin(ph)[None, :]
+    P[0, :] = (0, 1, 0)
+    P[lat, :] = (0, -1, 0)
+    UV = np.stack(np.meshgrid(np.arange(lon + 1) / lon, np.arange(lat + 1) / lat), -1)
+    tris = []
+    for j in range(lat):
+        for i in range(lon):
+            a, b, c, d = (j, i), (j, i + 1), (j + 1, i), (j + 1, i + 1)
+            if j == 0:
+                tris.append((a, c, d))
+            elif j == lat - 1:
+                tris.append((a, c, b))
+            else:
+                tris.append((a, c, d))
+                tris.append((a, d, b))
+    idx = np.array(tris)  # (n, 3, 2)
+    pos = P[idx[..., 0], idx[..., 1]]
+    # orient every triangle outward (counter-clockwise seen from outside)
+    nrm = np.cross(pos[:, 1] - pos[:, 0], pos[:, 2] - pos[:, 0])
+    flip = (nrm * pos.mean(axis=1)).sum(-1) < 0
+    idx[flip] = idx[flip][:, [0, 2, 1]]
+    pos = P[idx[..., 0], idx[..., 1]]
+    uv = UV[idx[..., 0], idx[..., 1]]
+    n = idx.shape[0]
+    p4 = np.ones((n, 3, 4), F32)
+    p4[..., :3] = pos * radius
+    n4 = np.zeros((n, 3, 4), F32)
+    n4[..., :3] = pos
+    col = np.empty((n, 3, 4), np.uint8)
+    col[:] = color
+    return sc.Mesh(p4, n4, uv.astype(F32), col, np.zeros(n, np.int32))
+
+
+def ground_plane(size=10.0, y=-1.0, color=(128, 128, 128, 255), material_id=-1):
+    """Two triangles on y = const facing +y (like model/plane.go, which uses
+    MaterialID -1 so the ground shows its vertex colour)."""
+    h = size / 2
+    q = np.array([[-h, y, h], [h, y, h], [h, y, -h], [-h, y, -h]], np.float64)
+    tri = np.array([[0, 1, 2], [0, 2, 3]])
+    pos = np.ones((2, 3, 4), F32)
+    pos[..., :3] = q[tri]
+    nor = np.zeros((2, 3, 4), F32)
+    nor[..., 1] = 1
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], F32)[tri]
+    col = np.empty((2, 3, 4), np.uint8)
+    col[:] = color
+    return sc.Mesh(pos, nor, uv, col, np.full(2, material_id, np.int32))
+
+
+def small_scene(width=800, height=500):
+    """The small CPU-runnable workload: a 64x32 UV sphere (3,968 triangles)
+    on a 2-triangle ground, one point light, ambient 0.1, no shadows."""
+    kd = sc.color_from_value(0.8, 0.3, 0.2, 1.0)
+    ks = sc.color_from_value(0.5, 0.5, 0.5, 1.0)
+    mat = sc.BlinnPhong(diffuse=kd, specular=ks, shininess=32)
+    sphere = sc.Geometry(uv_sphere(64, 32, 1.0), mat)
+    ground = sc.Geometry(ground_plane(10.0, -1.0))
+    s = sc.Scene(sphere, ground, sc.Point(position=(4, 4, 2), intensity=1.0), sc.Ambient(intensity=0.1))
+    cam = sc.Perspective(position=(0, 1.5, 4), target=(0, 0, 0), up=(0, 1, 0), fov=45, aspect=width / height,
+                         near=0.1, far=100)
+    return s, cam
+
+
+def sphere_field(n_spheres=256, lon=63, lat=32, seed=0x5EED0002, width=1920, height=1080, ao=True,
+                 directional_shadow=True):
+    """The 1M-triangle workload: 256 spheres of 3,906 triangles each."""
+    rng = Xoshiro128(seed)
+    materials = [
+        sc.BlinnPhong(diffuse=sc.color_from_value(0.8, 0.3, 0.2), specular=sc.color_from_value(0.5, 0.5, 0.5),
+                      shininess=32, ambient_occlusion=ao, receive_shadow=True),
+        sc.BlinnPhong(diffuse=sc.color_from_value(0.2, 0.5, 0.8), specular=sc.color_from_value(0.5, 0.5, 0.5),
+                      shininess=16, ambient_occlusion=ao, receive_shadow=True),
+        sc.BlinnPhong(diffuse=sc.color_from_value(0.3, 0.8, 0.3), specular=sc.color_from_value(0.5, 0.5, 0.5),
+                      shininess=64, ambient_occlusion=ao, receive_shadow=True, flat_shading=True),
+        sc.BlinnPhong(diffuse=sc.color_from_value(0.9, 0.9, 0.9), specular=sc.color_from_value(0.5, 0.5, 0.5),
+                      shininess=8, ambient_occlusion=ao, receive_shadow=True),
+    ]
+    mesh = uv_sphere(lon, lat, 1.0)
+    objs = []
+    for _ in range(n_spheres):
+        c = [rng.uniform(-10, 10) for _ in range(3)]
+        r = rng.uniform(0.2, 1.5)
+        m = materials[rng.integer(4)]
+        g = sc.Geometry(mesh, m)
+        g.scale(r, r, r).translate(*c)
+        objs.append(g)
+    s = sc.Scene(*objs)
+    s.add(sc.Point(position=(14, 18, 12), intensity=1.0, cast_shadow=True),
+          sc.Directional(direction=(-1, -1, -0.5), intensity=0.6, cast_shadow=directional_shadow),
+          sc.Ambient(intensity=0.1))
+    cam = sc.Perspective(position=(0, 4, 24), target=(0, 0, 0), up=(0, 1, 0), fov=60, aspect=width / height,
+                         near=0.1, far=100)
+    return s, cam
+
+
+def triangle_soup(n_tris, width, height, seed=0x5EED0003, back_fraction=0.30, fov=60.0):
+    """Small-triangle stress soup: centroids uniform on screen, view depth
+    U[0.1, 100], area ~ LogNormal(ln 1 px^2, 1.0), random shape/orientation,
+    winding flipped with probability back_fraction; unprojected to world
+    space through a camera at the origin looking down -z."""
+    g = np.random.default_rng(seed)
+    cx = g.uniform(0, width, n_tris)
+    cy = g.uniform(0, height, n_tris)
+    depth = g.uniform(0.1, 100.0, n_tris)
+    area = np.exp(g.normal(0.0, 1.0, n_tris))  # px^2, median 1
+    ang = g.uniform(0, 2 * np.pi, n_tris)
+    side = np.sqrt(4 * area / np.sqrt(3))  # equilateral of that area
+    base = np.stack([np.cos(ang[:, None] + np.array([0, 2, 4]) * np.pi / 3),
+                     np.sin(ang[:, None] + np.array([0, 2, 4]) * np.pi / 3)], -1)  # (n,3,2) unit circle
+    jitter = g.uniform(0.6, 1.4, (n_tris, 3, 1))
+    sx = cx[:, None] + base[..., 0] * side[:, None] / np.sqrt(3) * jitter[..., 0]
+    sy = cy[:, None] + base[..., 1] * side[:, None] / np.sqrt(3) * jitter[..., 0]
+    flip = g.uniform(0, 1, n_tris) < back_fraction
+    sx[flip] = sx[flip][:, ::-1]
+    sy[flip] = sy[flip][:, ::-1]
+    t = math.tan(math.radians(fov) / 2)
+    aspect = width / height
+    ndc_x = sx / width * 2 - 1
+    ndc_y = sy / height * 2 - 1
+    z = -depth[:, None] * np.ones((1, 3))
+    X = ndc_x * t * aspect * depth[:, None]
+    Y = ndc_y * t * depth[:, None]
+    pos = np.ones((n_tris, 3, 4), F32)
+    pos[..., 0], pos[..., 1], pos[..., 2] = X, Y, z
+    nrm = np.cross(pos[:, 1, :3] - pos[:, 0, :3], pos[:, 2, :3] - pos[:, 0, :3])
+    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True) + 1e-30
+    nor = np.zeros((n_tris, 3, 4), F32)
+    nor[..., :3] = nrm[:, None, :]
+    col = g.integers(0, 256, (n_tris, 3, 4), dtype=np.uint8)
+    col[..., 3] = 255
+    return sc.Mesh(pos, nor, None, col, np.zeros(n_tris, np.int32))
