@@ -180,7 +180,7 @@ typedef struct pr_stats {
     uint32_t n_tris_in;
     uint32_t n_raster_tris;    /* after cull/clip, main view */
     uint32_t n_clipped_tris;   /* input triangles that went through clipTriangle */
-    uint32_t n_large_tris;     /* raster triangles on the tiled path */
+    uint32_t n_raster_tasks;   /* raster work items (pixel-box chunks of <= 1024 px), all passes */
     uint32_t n_nan_fragments;  /* fragments with NaN depth (degenerate triangles) */
     uint32_t n_kernel_launches;
     uint32_t reserved;

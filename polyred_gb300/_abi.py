@@ -80,7 +80,7 @@ class pr_outputs(C.Structure):
 
 class pr_stats(C.Structure):
     _fields_ = [("size", C.c_uint32), ("n_tris_in", C.c_uint32), ("n_raster_tris", C.c_uint32),
-                ("n_clipped_tris", C.c_uint32), ("n_large_tris", C.c_uint32), ("n_nan_fragments", C.c_uint32),
+                ("n_clipped_tris", C.c_uint32), ("n_raster_tasks", C.c_uint32), ("n_nan_fragments", C.c_uint32),
                 ("n_kernel_launches", C.c_uint32), ("reserved", C.c_uint32), ("ms_shadow", C.c_float),
                 ("ms_setup", C.c_float), ("ms_raster", C.c_float), ("ms_shade", C.c_float),
                 ("ms_total", C.c_float)]

@@ -221,6 +221,23 @@ int validate_frame(const Ctx* c, const pr_frame_desc* f) {
     return PR_OK;
 }
 
+// Counters and per-phase device times of the last frame; the stream must
+// have passed the frame's last event.
+void collect_stats(Ctx* c) {
+    c->stats.n_raster_tris = c->h_cnt[0].n_rec;
+    c->stats.n_clipped_tris = c->h_cnt[0].n_clipped;
+    c->stats.n_nan_fragments = c->h_cnt[0].n_nan;
+    uint32_t n_tasks = 0;
+    for (int k = 0; k <= prk::kMaxLights; k++) n_tasks += c->h_cnt[k].n_tasks;
+    c->stats.n_raster_tasks = n_tasks;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->stats.ms_shadow = ms;
+    cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->stats.ms_setup = ms;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->stats.ms_raster = ms;
+    cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); c->stats.ms_shade = ms;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); c->stats.ms_total = ms;
+}
+
 int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
     int rc = validate_frame(c, f);
     if (rc) return rc;
@@ -449,17 +466,8 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         // frame, so re-rendering with larger buffers needs no roll-back.
         if (ov) return fail(PR_ERR_OVERFLOW, "internal capacity exceeded (records %u, tasks %u)", need_rec, need_tasks);
     }
-    // stats
-    c->stats.n_raster_tris = c->h_cnt[0].n_rec;
-    c->stats.n_clipped_tris = c->h_cnt[0].n_clipped;
-    c->stats.n_nan_fragments = c->h_cnt[0].n_nan;
     c->stats.n_kernel_launches = launches;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->stats.ms_shadow = ms;
-    cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->stats.ms_setup = ms;
-    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->stats.ms_raster = ms;
-    cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); c->stats.ms_shade = ms;
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); c->stats.ms_total = ms;
+    collect_stats(c);
 
     // ---- host outputs ----
     if (out && !out_dev) {
@@ -650,6 +658,7 @@ int pr_sync(void* ctx) {
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     for (int k = 0; k <= prk::kMaxLights; k++)
         if (c->h_cnt[k].overflow) return fail(PR_ERR_OVERFLOW, "internal capacity exceeded in an asynchronous frame");
+    collect_stats(c);
     return PR_OK;
 }
 

@@ -192,10 +192,13 @@ PR_DEV int sutherland_hodgman(const V4* in3, float w, float h, V4* out) {
 PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, const SubVtx* v, const float* recipw,
                           int matid) {
     RasterRec R;
-    R.x[0] = v[0].pos.x; R.y[0] = v[0].pos.y; R.z[0] = v[0].pos.z;
-    R.x[1] = v[1].pos.x; R.y[1] = v[1].pos.y; R.z[1] = v[1].pos.z;
-    R.x[2] = v[2].pos.x; R.y[2] = v[2].pos.y; R.z[2] = v[2].pos.z;
-    R.sabc = sabc_of(R.x[0], R.y[0], R.x[1], R.y[1], R.x[2], R.y[2]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        R.v[3 * k + 0] = v[k].pos.x;
+        R.v[3 * k + 1] = v[k].pos.y;
+        R.v[3 * k + 2] = v[k].pos.z;
+    }
+    R.sabc = sabc_of(R.v[0], R.v[1], R.v[3], R.v[4], R.v[6], R.v[7]);
     R.seq = seq;
     uint32_t area = 0;
     if (!pixel_box(v[0].pos, v[1].pos, v[2].pos, P.W, P.H, &R.bx, &R.by, &area)) {

@@ -18,19 +18,21 @@ constexpr int kTaskPx = 1024;        // pixels of one raster task (a bbox chunk)
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
 // Raster record: what the coverage/depth test of one (sub-)triangle needs.
-// 16 words = 64 bytes, read with four 16-byte loads.
-struct RasterRec {
-    float x[3], y[3], z[3];  // screen-space vertices after Viewport + Pos()
-    float sabc;              // Barycoord's Sabc = ab.Cross(ac).Z (exact reference bits)
-    uint32_t bx;             // x0 | x1 << 16 (pixel bbox clamped to the buffer)
-    uint32_t by;             // y0 | y1 << 16
-    uint32_t seq;            // draw order: tri*8 + clip sub-index (main view), tri (shadow)
+// 16 words = 64 bytes, read with four 16-byte loads (16-byte aligned so a
+// local copy can be stored with vector stores too).
+struct alignas(16) RasterRec {
+    float v[9];     // screen-space vertices after Viewport + Pos(): x0 y0 z0 x1 y1 z1 x2 y2 z2
+    float sabc;     // Barycoord's Sabc = ab.Cross(ac).Z (exact reference bits)
+    uint32_t bx;    // x0 | x1 << 16 (pixel bbox clamped to the buffer)
+    uint32_t by;    // y0 | y1 << 16
+    uint32_t seq;   // draw order: tri*8 + clip sub-index (main view), tri (shadow)
     uint32_t pad[3];
 };
+static_assert(sizeof(RasterRec) == 64, "RasterRec is four float4");
 
 // Attribute record: the rest of drawClipped's inputs for one sub-triangle.
 // 36 words = 144 bytes.
-struct AttrRec {
+struct alignas(16) AttrRec {
     float recipw[3];  // parent triangle's -1/W (render/raster.go:403-406, 440-443)
     float nor[9];     // vertex normals after Apply(Normal) (xyz per vertex)
     float uv[6];
@@ -39,6 +41,7 @@ struct AttrRec {
     float fn[4];      // face normal fN (render/raster.go:479)
     int32_t matid;    // flat material id (<0 = vertex colour)
 };
+static_assert(sizeof(AttrRec) == 144, "AttrRec is nine float4");
 
 struct Counters {
     uint32_t n_rec;       // records emitted (main view)

@@ -37,13 +37,13 @@ class Pair:
     """One scene rendered by both sides, frame after frame (shadow maps
     persist on both sides, as in the reference)."""
 
-    def __init__(self, device, opts, outputs=ALL_OUTPUTS, threads=THREADS):
+    def __init__(self, device, opts, outputs=ALL_OUTPUTS, threads=THREADS, cams=None):
         self.device = device
         self.opts = opts
         self.outputs = tuple(outputs)
         self.threads = threads
         self.flat = render.FlatScene(opts["scene"])
-        self.cams = shadow_cams(opts)
+        self.cams = shadow_cams(opts) if cams is None else cams
         lib = native.load()
         d = self.flat.desc()
         native.check(lib.pr_scene_upload(device.handle, C.byref(d)))

@@ -113,31 +113,74 @@ def test_depth_ties_first_drawn_wins(device):
     assert ids.size > 100 and (ids == 0).all()
 
 
-def test_degenerate_triangles_nan_depth(device):
-    """Triangles that collapse on screen give NaN barycentrics and NaN-depth
-    fragments; the reference keeps such a fragment when it is the first at a
-    pixel, and AO then spreads NaN to its neighbours."""
-    rng = np.random.default_rng(7)
+def _degenerate_scene(seed, rows=128):
+    """Regular triangles mixed with collapsed ones. A collapsed triangle has
+    two vertices sharing (x, y) and its third on the same row y, which under
+    the orthographic camera below maps exactly onto a pixel-centre row: there
+    all three Barycoord cross products are 0 and 0/0 gives NaN coordinates,
+    which pass the inside test with a NaN depth."""
+    rng = np.random.default_rng(seed)
     tris = []
-    for _ in range(300):
-        c = rng.uniform(-2, 2, 3)
-        c[2] = rng.uniform(-1, 1)
-        tris.append([c, c + rng.normal(0, 0.3, 3), c + rng.normal(0, 0.3, 3)])
-    for _ in range(200):  # sub-pixel, collapsing to one screen point
-        c = rng.uniform(-2, 2, 3)
-        d = rng.normal(0, 1e-5, (3, 3))
-        d[0] = 0
-        tris.append([c + d[0], c + d[1], c + d[2]])
-    tris = np.array(tris)
+    for i in range(600):
+        if i % 2 == 0:
+            c = rng.uniform(-2, 2, 3)
+            tris.append([c, c + rng.normal(0, 0.3, 3), c + rng.normal(0, 0.3, 3)])
+        else:
+            k = int(rng.integers(4, rows - 4))
+            y = (2 * k - (rows - 1)) / 64.0  # screen y = 32*y + 64 = k + 0.5
+            x1, x3 = rng.uniform(-2, 2, 2)
+            z1, z2, z3 = rng.uniform(-1, 1, 3)
+            tris.append([[x1, y, z1], [x1, y, z2], [x3, y, z3]])
+    return np.array(tris)
+
+
+def _ortho_cam():
+    # 2/(top-bottom) = 0.5 and a 128-row viewport: y_screen = 32*y + 64 exactly
+    return sc.Orthographic(position=(0, 0, 5), target=(0, 0, 0), up=(0, 1, 0), left=-2.5, right=2.5, bottom=-2,
+                           top=2, near=1, far=-20)
+
+
+def test_degenerate_triangles_nan_depth(device):
+    """The reference keeps a NaN-depth fragment when it is the first at its
+    pixel (DepthTest passes on !Ok, later `z > NaN` never does), shadow maps
+    take NaN and recover on the next finite store, and AO spreads NaN to the
+    neighbours that march across such a pixel."""
     m = _basic_material(ambient_occlusion=True, receive_shadow=True)
-    g = sc.Geometry(_mesh(tris), m)
+    g = sc.Geometry(_mesh(_degenerate_scene(7)), m)
     s = sc.Scene(g, sc.Point(position=(3, 4, 5), cast_shadow=True), sc.Ambient(0.1))
-    p = _pair(device, s, _cam(200, 150), 200, 150, shadow_map=True)
+    p = _pair(device, s, _ortho_cam(), 160, 128, shadow_map=True)
+    nan_frags = 0
     for _ in range(2):
         gpu, cpu = p.frame(with_shadow_maps=True)
         assert_bitexact(gpu, cpu, ["rgba", "tri_id", "depth", "nor", "uvd", "vcol", "mat_id", "world_pos"])
         assert_same_maps(gpu["shadow_maps"], cpu["shadow_maps"])
-    assert p.stats["n_nan_fragments"] > 0
+        nan_frags += p.stats["n_nan_fragments"]
+    assert nan_frags > 0
+    assert np.isnan(gpu["depth"]).any()
+
+
+def test_degenerate_triangles_nan_shadow_map(device):
+    """NaN depths in the shadow pass: the light camera is given the main
+    camera's exact orthographic matrices, so the collapsed triangles land on
+    pixel-centre rows of the shadow map too."""
+    m = _basic_material(receive_shadow=True)
+    g = sc.Geometry(_mesh(_degenerate_scene(9)), m)
+    s = sc.Scene(g, sc.Point(position=(0, 0, 5), cast_shadow=True), sc.Ambient(0.1))
+    cam = _ortho_cam()
+    p = Pair(device, options(s, cam, 160, 128, shadow_map=True), cams={0: (cam.view_matrix(), cam.proj_matrix())})
+    for _ in range(3):
+        gpu, cpu = p.frame(with_shadow_maps=True)
+        assert_bitexact(gpu, cpu, ["rgba", "tri_id", "depth", "nor", "uvd", "vcol", "mat_id", "world_pos"])
+        assert_same_maps(gpu["shadow_maps"], cpu["shadow_maps"])
+    assert np.isnan(cpu["shadow_maps"]).any()
+
+
+def test_degenerate_triangles_perspective(device):
+    m = _basic_material(ambient_occlusion=True)
+    g = sc.Geometry(_mesh(_degenerate_scene(11)), m)
+    s = sc.Scene(g, sc.Point(position=(3, 4, 5)), sc.Ambient(0.1))
+    gpu, cpu = _pair(device, s, _cam(200, 150), 200, 150).frame()
+    assert_bitexact(gpu, cpu)
 
 
 def test_orthographic_camera(device):
