@@ -103,6 +103,8 @@ struct Ctx {
     DevBuf<unsigned long long> keys;
     DevBuf<uint32_t> nanseq, beaten, win;
     DevBuf<float> depth_ao;
+    DevBuf<uint32_t> ao_list;
+    int n_ao_dirs = 0;
     // shadow maps (persistent across frames)
     int SW = 0, SH = 0, n_slights = 0;
     DevBuf<uint32_t> smap, lastnan;
@@ -169,6 +171,7 @@ int ensure_frame(Ctx* c, int W, int H) {
     if ((rc = c->beaten.ensure(n))) return rc;
     if ((rc = c->win.ensure(n))) return rc;
     if ((rc = c->depth_ao.ensure(n))) return rc;
+    if ((rc = c->ao_list.ensure(n))) return rc;
     c->W = W;
     c->H = H;
     return PR_OK;
@@ -420,8 +423,9 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         sp.SW = SW;
         sp.SH = SH;
         sp.smaps = shadows ? c->smap.p : nullptr;
-        prh::ao_directions(sp.ao_cos, sp.ao_sin, &sp.n_ao);
         prh::gamma_table(sp.gamma);
+        sp.ao_list = c->ao_list.p;
+        sp.cnt_w = dcnt;
         // outputs: device pointers directly, or ctx staging buffers
         if (out_dev) {
             sp.rgba = (uchar4*)out->rgba;
@@ -446,6 +450,21 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         }
         KTRY(prk::launch_shade(sp, st));
         launches += 1;
+        if (sp.rgba) {
+            // AmbientOcclusionShade + gamma for the pixels the shade kernel listed
+            prk::AoParams ap{};
+            ap.W = W;
+            ap.H = H;
+            ap.gamma_on = (f->flags & PR_FRAME_GAMMA) ? 1 : 0;
+            ap.n_dirs = c->n_ao_dirs;
+            ap.depth = c->depth_ao.p;
+            ap.list = c->ao_list.p;
+            ap.cnt = dcnt;
+            ap.rgba = sp.rgba;
+            std::memcpy(ap.gamma, sp.gamma, 256);
+            KTRY(prk::launch_ao(ap, c->n_sms * 8, st));
+            launches += 1;
+        }
         CUDA_TRY(cudaEventRecord(c->ev[4], st));
         CUDA_TRY(cudaMemcpyAsync(c->h_cnt, dcnt, sizeof(prk::Counters) * (prk::kMaxLights + 1), cudaMemcpyDeviceToHost, st));
         if (!sync) {
@@ -548,6 +567,15 @@ int pr_create(int device, void** out_ctx) {
         return fail(PR_ERR_OOM, "pinned counter allocation failed");
     }
     c->n_sms = prk::sm_count();
+    {
+        float cs[8], sn[8];
+        prh::ao_directions(cs, sn, &c->n_ao_dirs);
+        int e = prk::set_ao_tables(cs, sn, c->n_ao_dirs, c->stream);
+        if (e) {
+            pr_destroy(c);
+            return fail(PR_ERR_CUDA, "AO table upload: %s", cudaGetErrorString((cudaError_t)e));
+        }
+    }
     *out_ctx = c;
     return PR_OK;
 }
@@ -561,6 +589,7 @@ int pr_destroy(void* ctx) {
     c->obj_first.release(); c->obj_model.release(); c->obj_normal.release(); c->obj_matbase.release();
     c->dmats.release(); c->rrec.release(); c->arec.release(); c->tasks.release(); c->first_rec.release();
     c->keys.release(); c->nanseq.release(); c->beaten.release(); c->win.release(); c->depth_ao.release();
+    c->ao_list.release();
     c->smap.release(); c->lastnan.release(); c->cnt.release();
     c->o_rgba.release(); c->o_vcol.release(); c->o_tri.release(); c->o_depth.release(); c->o_shadow.release();
     c->o_nor.release(); c->o_fnor.release(); c->o_wpos.release(); c->o_uvd.release(); c->o_mat.release();

@@ -549,6 +549,7 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
     const size_t i = (size_t)r * W + x;
     const uint32_t seq = P.win[i];
     uint32_t c0, c1, c2, c3;
+    bool ao_pending = false;
     if (seq == kNone) {
         c0 = P.background[0]; c1 = P.background[1]; c2 = P.background[2]; c3 = P.background[3];
         if (P.tri_id) P.tri_id[i] = kNone;
@@ -695,57 +696,143 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
                 c1 = go_f2u8(__fmul_rn((float)c1, w));
                 c2 = go_f2u8(__fmul_rn((float)c2, w));
             }
-            // AmbientOcclusionShade (material/ao.go:20-73). maxangle is
-            // Max over taps of float32(Atan(elev/dist)); Atan and the float32
-            // rounding are monotone, so it equals float32(Atan(max ratio)),
-            // and only positive ratios can exceed the initial 0. A NaN ratio
-            // makes the direction's result NaN (Go's Max propagates NaN).
-            if (mat->flags & PR_MAT_AO) {
-                const float pxf = (float)x, pyf = (float)y;
-                float total = 0.0f;
-                for (int k = 0; k < P.n_ao; k++) {
-                    const float dX = P.ao_cos[k], dY = P.ao_sin[k];
-                    float best = 0.0f;
-                    bool nanr = false;
-                    for (int ti = 0; ti < 100; ti++) {
-                        const float t = (float)ti;
-                        const float cx = __fadd_rn(pxf, __fmul_rn(dX, t));
-                        const float cy = __fadd_rn(pyf, __fmul_rn(dY, t));
-                        const long long ix = go_f2i(cx), iy = go_f2i(cy);
-                        if (ix < 0 || ix >= W || iy < 0 || iy >= H) break;
-                        const float sd = P.depth_ao[(size_t)(H - 1 - iy) * W + (size_t)ix];
-                        const float elev = __fsub_rn(sd, z);
-                        if (!(elev > 0.0f) && !isnan(elev)) continue;
-                        const float ddx = __fsub_rn(pxf, cx), ddy = __fsub_rn(pyf, cy);
-                        const float dist = __fsqrt_rn(fma64f(ddx, ddx, fma64f(ddy, ddy, 0.0f)));
-                        if (dist < 1.0f) continue;
-                        if (isnan(elev)) {
-                            nanr = true;
-                            break;
-                        }
-                        best = fmaxf(best, __fdiv_rn(elev, dist));
-                    }
-                    float ma;
-                    if (nanr)
-                        ma = __uint_as_float(0x7fc00000u);
-                    else
-                        ma = best > 0.0f ? __double2float_rn(go_atan((double)best)) : 0.0f;
-                    total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));
-                }
-                total = __fdiv_rn(total, 12.5663706143591729539f);
-                total = __double2float_rn(go_pow((double)total, 10000.0));
-                c0 = go_f2u8(__fmul_rn(total, (float)c0));
-                c1 = go_f2u8(__fmul_rn(total, (float)c1));
-                c2 = go_f2u8(__fmul_rn(total, (float)c2));
-            }
+            // AmbientOcclusionShade (material/ao.go:20-73) runs in ao_kernel
+            // on a compacted list of these pixels.
+            ao_pending = (mat->flags & PR_MAT_AO) && P.rgba && P.ao_list;
         }
     }
+    if (ao_pending) {
+        P.rgba[i] = make_uchar4(c0, c1, c2, c3);  // pre-AO, pre-gamma colour
+    }
+    {
+        // warp-aggregated append to the AO list
+        const unsigned act = __activemask();
+        const unsigned want = __ballot_sync(act, ao_pending);
+        if (want) {
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(want) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&P.cnt_w->n_ao, (uint32_t)__popc(want));
+            base = __shfl_sync(act, base, leader);
+            if (ao_pending) P.ao_list[base + __popc(want & ((1u << lane) - 1u))] = (uint32_t)i;
+        }
+    }
+    if (ao_pending) return;
     if (P.flags & PR_FRAME_GAMMA) {
         c0 = P.gamma[c0];
         c1 = P.gamma[c1];
         c2 = P.gamma[c2];
     }
     if (P.rgba) P.rgba[i] = make_uchar4(c0, c1, c2, c3);
+}
+
+// ---------------------------------------------------------------- AO
+
+// Tap offsets float32(dir*t) for the 8 march directions (material/ao.go:28,
+// :51 dir.Scale(t, t, 1, 1)) and, per t, a multiplier m[t] >= 1/(t - 0.01)
+// that bounds the ratio elev/dist from above (see ao_kernel).
+__constant__ float2 c_ao_q[8][100];
+__constant__ float c_ao_rbound[100];
+
+// int(v) of Go for |v| < 2^23: truncation toward zero on the FP32 pipe.
+PR_DEV int trunc_small(float v) {
+    const float a = fabsf(v);
+    const int k = (int)(__float_as_uint(__fadd_rz(a, 8388608.0f)) - 0x4B000000u);
+    return v < 0.0f ? -k : k;
+}
+
+// distance of material/ao.go:52, p.Sub(cur).Len() with z = w = 0
+PR_DEV float ao_distance(float pxf, float pyf, float cx, float cy) {
+    const float ddx = __fsub_rn(pxf, cx), ddy = __fsub_rn(pyf, cy);
+    return __fsqrt_rn(fma64f(ddx, ddx, __fmul_rn(ddy, ddy)));
+}
+
+// AmbientOcclusionShade (material/ao.go:20-73) for the pixels the shade
+// kernel listed. Per direction, maxangle is the Max over taps of
+// float32(Atan(elev/dist)); Atan and the rounding to float32 are monotone, so
+// it is float32(Atan(best)) with best the largest ratio, and only positive
+// ratios can exceed the initial 0. A NaN ratio (at a tap not skipped for
+// dist < 1) makes the direction NaN, as Go's math.Max propagates NaN.
+//
+// Exactness of the fast paths:
+//  * cur = p + float32(dir*t) stays within (-101, W+100) x (-101, H+100), so
+//    Go's int() is a 32-bit truncation here (trunc_small).
+//  * cur moves monotonically in t, so once a tap leaves the buffer every
+//    later tap does too (the reference returns there).
+//  * |cur - (p + dir*t)| < 2^-9 for buffers up to 16384 wide and |dir| = 1
+//    within 1e-7, so dist >= t - 0.002 for t >= 1; a tap with
+//    elev * m[t] <= best cannot raise best, and is skipped without computing
+//    its distance. t = 0 always has dist = 0 and is skipped by the reference.
+__global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParams P) {
+    const uint32_t n = P.cnt->n_ao;
+    const int W = P.W, H = P.H;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t i = P.list[j];
+        const int r = (int)(i / (uint32_t)W);
+        const int x = (int)i - r * W;
+        const int y = H - 1 - r;
+        const float z = P.depth[i];
+        const float pxf = (float)x, pyf = (float)y;
+        float total = 0.0f;
+        for (int k = 0; k < P.n_dirs; k++) {
+            float best = 0.0f;
+            bool nanr = false, done = false;
+            for (int t0 = 1; t0 < 100 && !done; t0 += 4) {
+                float sd[4], cxs[4], cys[4];
+                bool inb[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int t = t0 + u;
+                    const float2 q = c_ao_q[k][t < 100 ? t : 99];
+                    cxs[u] = __fadd_rn(pxf, q.x);
+                    cys[u] = __fadd_rn(pyf, q.y);
+                    const int ix = trunc_small(cxs[u]), iy = trunc_small(cys[u]);
+                    inb[u] = t < 100 && (unsigned)ix < (unsigned)W && (unsigned)iy < (unsigned)H;
+                    const size_t idx = inb[u] ? (size_t)(H - 1 - iy) * W + ix : (size_t)i;
+                    sd[u] = __ldg(P.depth + idx);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (!inb[u]) {
+                        done = true;
+                        break;
+                    }
+                    const int t = t0 + u;
+                    const float elev = __fsub_rn(sd[u], z);
+                    if (elev > 0.0f) {
+                        if (__fmul_rn(elev, c_ao_rbound[t]) > best) {
+                            const float d = ao_distance(pxf, pyf, cxs[u], cys[u]);
+                            if (d >= 1.0f) best = fmaxf(best, __fdiv_rn(elev, d));
+                        }
+                    } else if (isnan(elev)) {
+                        if (t >= 2 || ao_distance(pxf, pyf, cxs[u], cys[u]) >= 1.0f) {
+                            nanr = true;
+                            done = true;
+                            break;
+                        }
+                    }
+                }
+            }
+            float ma;
+            if (nanr)
+                ma = __uint_as_float(0x7fc00000u);
+            else
+                ma = best > 0.0f ? __double2float_rn(go_atan((double)best)) : 0.0f;
+            total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));  // HalfPi - angle
+        }
+        total = __fdiv_rn(total, 12.5663706143591729539f);  // (Pi/2)*8 as float32
+        total = __double2float_rn(go_pow((double)total, 10000.0));
+        const uchar4 c = P.rgba[i];
+        uint32_t c0 = go_f2u8(__fmul_rn(total, (float)c.x));
+        uint32_t c1 = go_f2u8(__fmul_rn(total, (float)c.y));
+        uint32_t c2 = go_f2u8(__fmul_rn(total, (float)c.z));
+        if (P.gamma_on) {
+            c0 = P.gamma[c0];
+            c1 = P.gamma[c1];
+            c2 = P.gamma[c2];
+        }
+        P.rgba[i] = make_uchar4(c0, c1, c2, c.w);
+    }
 }
 
 __global__ void fma_probe_kernel(const float* a, const float* b, const float* c, float* out, float* out_ref, int n) {
@@ -793,6 +880,26 @@ int launch_shade(const ShadeParams& p, void* stream) {
     dim3 grd((p.W + 31) / 32, (p.H + 7) / 8);
     shade_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
     return check(cudaGetLastError());
+}
+int launch_ao(const AoParams& p, int n_blocks, void* stream) {
+    ao_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream) {
+    float2 q[8][100];
+    float rb[100];
+    for (int k = 0; k < 8; k++)
+        for (int t = 0; t < 100; t++) {
+            float ft = (float)t;
+            q[k][t] = k < n ? make_float2(cosv[k] * ft, sinv[k] * ft) : make_float2(0.0f, 0.0f);
+        }
+    rb[0] = 0.0f;
+    for (int t = 1; t < 100; t++) rb[t] = (float)((1.0 / ((double)t - 0.01)) * (1.0 + 0x1p-20));
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_ao_q, q, sizeof(q), 0, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbolAsync(c_ao_rbound, rb, sizeof(rb), 0, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    return check(e);
 }
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream) {
     if (n == 0) return 0;

@@ -52,6 +52,8 @@ struct Counters {
     uint32_t n_nan;       // number of NaN-depth fragments
     uint32_t need_rec;    // records needed when overflow
     uint32_t need_tasks;  // tasks needed when overflow
+    uint32_t n_ao;        // pixels listed for ambient occlusion
+    uint32_t pad[7];
 };
 
 struct LightK {
@@ -122,8 +124,6 @@ struct ShadeParams {
     float shadow_vp[16];        // ViewportMatrix(SW, SH)
     int SW, SH;
     const uint32_t* smaps;      // [n_lights][SH*SW] orderable keys
-    float ao_cos[8], ao_sin[8];
-    int n_ao;
     uint8_t gamma[256];
     // outputs (device pointers, may be null)
     uchar4* rgba;
@@ -135,6 +135,19 @@ struct ShadeParams {
     float4* guvd;
     uchar4* gvcol;
     int32_t* gmat;
+    uint32_t* ao_list;          // pixels whose material has AO (null: AO off)
+    Counters* cnt_w;
+};
+
+struct AoParams {
+    int W, H;
+    int gamma_on;
+    int n_dirs;
+    const float* depth;         // depth_ao
+    const uint32_t* list;
+    const Counters* cnt;
+    uchar4* rgba;
+    uint8_t gamma[256];
 };
 
 }  // namespace prk
@@ -149,6 +162,8 @@ int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t*
 int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,
                               void* stream);
 int launch_shade(const ShadeParams& p, void* stream);
+int launch_ao(const AoParams& p, int n_blocks, void* stream);
+int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
 int launch_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n,
                      void* stream);
