@@ -96,7 +96,7 @@ struct Ctx {
     DevBuf<prk::RasterRec> rrec;
     DevBuf<prk::AttrRec> arec;
     DevBuf<uint2> tasks;
-    DevBuf<uint32_t> first_rec;
+    DevBuf<uint32_t> first_rec, clip_list;
     uint32_t cap_rec = 0, cap_tasks = 0;
     // framebuffer
     int W = 0, H = 0;
@@ -270,6 +270,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
     uint32_t need_rec0 = c->n_tris + c->n_tris / 8 + 1024;
     if ((rc = ensure_work(c, need_rec0, need_rec0))) return rc;
     if ((rc = c->first_rec.ensure(std::max<uint32_t>(c->n_tris, 1)))) return rc;
+    if ((rc = c->clip_list.ensure(std::max<uint32_t>(c->n_tris, 1)))) return rc;
 
     // Shadow maps: allocated zeroed, reset when their geometry changes
     // (initShadowMaps, render/shadow.go:87), never cleared by a frame.
@@ -364,7 +365,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         CUDA_TRY(cudaMemsetAsync(c->keys.p, 0, npx * 8, st));
         CUDA_TRY(cudaMemsetAsync(c->nanseq.p, 0xff, npx * 4, st));
         CUDA_TRY(cudaMemsetAsync(c->beaten.p, 0, npx * 4, st));
-        KTRY(prk::launch_setup_main(mp, st));
+        KTRY(prk::launch_setup_main(mp, c->clip_list.p, st));
         CUDA_TRY(cudaEventRecord(c->ev[2], st));
         prk::RasterParams rp{};
         rp.rrec = c->rrec.p;
@@ -382,7 +383,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
         KTRY(prk::launch_resolve(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p, st));
         CUDA_TRY(cudaEventRecord(c->ev[3], st));
-        launches += 4;
+        launches += 5;
 
         // ---- deferred shading + gamma (render/raster.go:275-378) ----
         std::unique_ptr<prk::ShadeParams> sp_owner(new (std::nothrow) prk::ShadeParams());
@@ -588,6 +589,7 @@ int pr_destroy(void* ctx) {
     c->pos.release(); c->nor.release(); c->uv.release(); c->col.release(); c->mat.release();
     c->obj_first.release(); c->obj_model.release(); c->obj_normal.release(); c->obj_matbase.release();
     c->dmats.release(); c->rrec.release(); c->arec.release(); c->tasks.release(); c->first_rec.release();
+    c->clip_list.release();
     c->keys.release(); c->nanseq.release(); c->beaten.release(); c->win.release(); c->depth_ao.release();
     c->ao_list.release();
     c->smap.release(); c->lastnan.release(); c->cnt.release();

@@ -104,7 +104,7 @@ PR_DEV uint32_t find_object(const uint32_t* first, uint32_t n_obj, uint32_t t) {
 }
 
 PR_DEV uint32_t pack_col(uchar4 c) { return (uint32_t)c.x | ((uint32_t)c.y << 8) | ((uint32_t)c.z << 16) | ((uint32_t)c.w << 24); }
-PR_DEV float col_ch(uint32_t c, int k) { return (float)((c >> (8 * k)) & 0xffu); }
+PR_DEV float col_ch(uint32_t c, int k) { return small_u2f((c >> (8 * k)) & 0xffu); }
 
 struct SubVtx {
     V4 pos;
@@ -240,134 +240,204 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
     return area;
 }
 
-PR_DEV void emit_tasks(const SetupParams& P, const uint32_t* ridx, const uint32_t* area, int n) {
-    uint32_t total = 0;
-    for (int i = 0; i < n; i++) total += (area[i] + kTaskPx - 1) / kTaskPx;
-    if (total == 0) return;
-    uint32_t base = atomicAdd(&P.cnt->n_tasks, total);
-    if (base + total > P.cap_tasks) {
+// ---- warp-aggregated reservations (all 32 lanes must call them) ----------
+
+PR_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Reserve n slots per lane from *counter with one atomic per warp; returns
+// this lane's first slot. Sets *total to the warp's total.
+PR_DEV uint32_t warp_reserve(uint32_t* counter, uint32_t n, uint32_t* total) {
+    const uint32_t lane = lane_id();
+    uint32_t incl = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= (uint32_t)d) incl += v;
+    }
+    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+    *total = tot;
+    uint32_t base = 0;
+    if (tot != 0 && lane == 31) base = atomicAdd(counter, tot);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + incl - n;
+}
+
+PR_DEV uint32_t n_tasks_of(uint32_t area) { return (area + kTaskPx - 1) / kTaskPx; }
+
+// Write the raster tasks of up to 8 records (areas given); all lanes call.
+PR_DEV void emit_tasks_warp(const SetupParams& P, const uint32_t* ridx, const uint32_t* area, int n) {
+    uint32_t mine = 0;
+    for (int i = 0; i < n; i++) mine += n_tasks_of(area[i]);
+    uint32_t tot;
+    uint32_t o = warp_reserve(&P.cnt->n_tasks, mine, &tot);
+    if (mine == 0) return;
+    if (o + mine > P.cap_tasks) {
         atomicOr(&P.cnt->overflow, 2u);
-        atomicMax(&P.cnt->need_tasks, base + total);
+        atomicMax(&P.cnt->need_tasks, o + mine);
         return;
     }
-    uint32_t o = base;
     for (int i = 0; i < n; i++) {
-        uint32_t nt = (area[i] + kTaskPx - 1) / kTaskPx;
+        uint32_t nt = n_tasks_of(area[i]);
         for (uint32_t c = 0; c < nt; c++) P.tasks[o++] = make_uint2(ridx[i], c);
     }
 }
 
-// cpuForwardPass + draw for one input triangle (render/raster.go:257-269, 380-444)
-__global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n_tris) return;
-    uint32_t o = find_object(P.obj_first, P.n_objects, t);
-    V4 p[3], nn[3];
+// draw's transform and culls for triangle t (render/raster.go:380-436):
+// Proj.MulM(View).MulM(Model).MulV, -1/W, Viewport Apply + Pos, back-face,
+// viewport AABB; then the per-vertex attributes of surviving triangles
+// (the normal matrix Apply does not influence the culls).
+PR_DEV bool transform_main(const SetupParams& P, uint32_t t, SubVtx* v, float* recipw, int* matid, bool* contained) {
+    const uint32_t o = find_object(P.obj_first, P.n_objects, t);
+    V4 p[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        p[k] = ld4(P.pos[t * 3 + k]);
-        nn[k] = ld4(P.nor[t * 3 + k]);
-    }
-    if (!tri_is_valid(p[0], p[1], p[2])) return;
-    int matid = P.mat[t];
-    if (matid >= 0) matid += P.obj_matbase[o];
+    for (int k = 0; k < 3; k++) p[k] = ld4(P.pos[t * 3 + k]);
+    if (!tri_is_valid(p[0], p[1], p[2])) return false;
     float trans[16];
     mulm(P.pv, P.obj_model + o * 16, trans);
-    const float* nm = P.obj_normal + o * 16;
-    SubVtx v[3];
-    float recipw[3] = {1.0f, 1.0f, 1.0f};
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        V4 cp = mulv(trans, p[k]);
-        if (P.perspective) recipw[k] = __fdiv_rn(-1.0f, cp.w);
+        const V4 cp = mulv(trans, p[k]);
+        recipw[k] = P.perspective ? __fdiv_rn(-1.0f, cp.w) : 1.0f;
         v[k].pos = pos4(apply4(cp, P.viewport));
-        v[k].nor = apply4(nn[k], nm);
-        float2 uv = P.uv[t * 3 + k];
-        v[k].u = uv.x;
-        v[k].v = uv.y;
-        v[k].col = pack_col(P.col[t * 3 + k]);
     }
     // cullBackFace (render/cull.go:26-28)
     if (cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y), __fsub_rn(v[2].pos.x, v[0].pos.x),
                 __fsub_rn(v[2].pos.y, v[0].pos.y)) < 0.0f)
-        return;
-    Box vp = {0.0f, 0.0f, -1.0f, (float)P.W, (float)P.H, 1.0f};
-    Box tb = box3(v[0].pos, v[1].pos, v[2].pos);
-    if (!box_intersect(vp, tb)) return;
-    uint32_t seq0 = t * 8u;
-    if (box_contains(vp, v[0].pos) && box_contains(vp, v[1].pos) && box_contains(vp, v[2].pos)) {
-        uint32_t ridx = atomicAdd(&P.cnt->n_rec, 1u);
+        return false;
+    const Box vp = {0.0f, 0.0f, -1.0f, (float)P.W, (float)P.H, 1.0f};
+    if (!box_intersect(vp, box3(v[0].pos, v[1].pos, v[2].pos))) return false;
+    *contained = box_contains(vp, v[0].pos) && box_contains(vp, v[1].pos) && box_contains(vp, v[2].pos);
+    const float* nm = P.obj_normal + o * 16;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        v[k].nor = apply4(ld4(P.nor[t * 3 + k]), nm);
+        const float2 uv = P.uv[t * 3 + k];
+        v[k].u = uv.x;
+        v[k].v = uv.y;
+        v[k].col = pack_col(P.col[t * 3 + k]);
+    }
+    int m = P.mat[t];
+    if (m >= 0) m += P.obj_matbase[o];
+    *matid = m;
+    return true;
+}
+
+// cpuForwardPass + draw for triangles fully inside the viewport
+// (render/raster.go:257-269, 380-436); clipped ones go to clip_kernel.
+__global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P, uint32_t* clip_list) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    SubVtx v[3];
+    float recipw[3];
+    int matid = -1;
+    bool contained = false;
+    const bool ok = t < P.n_tris && transform_main(P, t, v, recipw, &matid, &contained);
+    __syncwarp();
+    const bool emit = ok && contained, clip = ok && !contained;
+    uint32_t tot;
+    const uint32_t ci = warp_reserve(&P.cnt->n_clipped, clip ? 1u : 0u, &tot);
+    if (clip) clip_list[ci] = t;
+    uint32_t ridx = warp_reserve(&P.cnt->n_rec, emit ? 1u : 0u, &tot);
+    uint32_t area = 0;
+    if (emit) {
         if (ridx >= P.cap_rec) {
             atomicOr(&P.cnt->overflow, 1u);
             atomicMax(&P.cnt->need_rec, ridx + 1);
-            return;
+        } else {
+            P.first_rec[t] = ridx;
+            area = write_sub(P, ridx, t * 8u, v, recipw, matid);
         }
-        P.first_rec[t] = ridx;
-        uint32_t area = write_sub(P, ridx, seq0, v, recipw, matid);
-        emit_tasks(P, &ridx, &area, 1);
-        return;
     }
-    // clipTriangle (render/clipping.go:70-157)
-    atomicAdd(&P.cnt->n_clipped, 1u);
-    V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
+    emit_tasks_warp(P, &ridx, &area, 1);
+}
+
+// clipTriangle (render/clipping.go:70-157) for the listed triangles: fan
+// sub-triangles with seq = tri*8 + i, drawn with the parent's recipw.
+__global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ SetupParams P, const uint32_t* clip_list) {
+    const uint32_t n = P.cnt->n_clipped;
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * blockDim.x >= n) return;  // whole block idle (uniform per warp too)
+    SubVtx v[3];
+    float recipw[3];
+    int matid = -1;
+    bool contained = false;
+    uint32_t t = 0;
+    int nc = 0;
     V4 clips[10];
-    int nc = sutherland_hodgman(in3, (float)P.W, (float)P.H, clips);
-    if (nc < 0) {
-        atomicOr(&P.cnt->overflow, 4u);
-        return;
+    if (j < n) {
+        t = clip_list[j];
+        transform_main(P, t, v, recipw, &matid, &contained);
+        V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
+        nc = sutherland_hodgman(in3, (float)P.W, (float)P.H, clips);
+        if (nc < 0) {
+            atomicOr(&P.cnt->overflow, 4u);
+            nc = 0;
+        }
     }
-    int nsub = nc - 2;
-    if (nsub <= 0) return;
-    uint32_t base = atomicAdd(&P.cnt->n_rec, (uint32_t)nsub);
-    if (base + nsub > P.cap_rec) {
-        atomicOr(&P.cnt->overflow, 1u);
-        atomicMax(&P.cnt->need_rec, base + nsub);
-        return;
-    }
-    P.first_rec[t] = base;
-    float psabc = sabc_of(v[0].pos.x, v[0].pos.y, v[1].pos.x, v[1].pos.y, v[2].pos.x, v[2].pos.y);
+    __syncwarp();
+    const uint32_t nsub = nc > 2 ? (uint32_t)(nc - 2) : 0u;
+    uint32_t tot;
+    const uint32_t base = warp_reserve(&P.cnt->n_rec, nsub, &tot);
     uint32_t ridxs[8], areas[8];
-    SubVtx s[3];
-    s[0] = clip_vertex(clips[0], v, psabc);
-    for (int i = 2; i < nc; i++) {
-        s[1] = clip_vertex(clips[i - 1], v, psabc);
-        s[2] = clip_vertex(clips[i], v, psabc);
-        uint32_t ridx = base + (uint32_t)(i - 2);
-        ridxs[i - 2] = ridx;
-        areas[i - 2] = write_sub(P, ridx, seq0 + (uint32_t)(i - 2), s, recipw, matid);
+    int nw = 0;
+    if (nsub > 0) {
+        if (base + nsub > P.cap_rec) {
+            atomicOr(&P.cnt->overflow, 1u);
+            atomicMax(&P.cnt->need_rec, base + nsub);
+        } else {
+            P.first_rec[t] = base;
+            const float psabc = sabc_of(v[0].pos.x, v[0].pos.y, v[1].pos.x, v[1].pos.y, v[2].pos.x, v[2].pos.y);
+            SubVtx s[3];
+            s[0] = clip_vertex(clips[0], v, psabc);
+            for (int i = 2; i < nc; i++) {
+                s[1] = clip_vertex(clips[i - 1], v, psabc);
+                s[2] = clip_vertex(clips[i], v, psabc);
+                ridxs[nw] = base + (uint32_t)(i - 2);
+                areas[nw] = write_sub(P, ridxs[nw], t * 8u + (uint32_t)(i - 2), s, recipw, matid);
+                nw++;
+            }
+        }
     }
-    emit_tasks(P, ridxs, areas, nsub);
+    emit_tasks_warp(P, ridxs, areas, nw);
 }
 
 // passShadows / drawDepth for one input triangle (render/shadow.go:137-192)
 __global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n_tris) return;
-    uint32_t o = find_object(P.obj_first, P.n_objects, t);
-    V4 p[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) p[k] = ld4(P.pos[t * 3 + k]);
-    if (!tri_is_valid(p[0], p[1], p[2])) return;
-    float trans[16];
-    mulm(P.pv, P.obj_model + o * 16, trans);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = false;
     SubVtx v[3];
+    if (t < P.n_tris) {
+        const uint32_t o = find_object(P.obj_first, P.n_objects, t);
+        V4 p[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        v[k].pos = pos4(apply4(mulv(trans, p[k]), P.viewport));
-        v[k].nor = {0, 0, 0, 0};
-        v[k].u = v[k].v = 0;
-        v[k].col = 0;
+        for (int k = 0; k < 3; k++) p[k] = ld4(P.pos[t * 3 + k]);
+        if (tri_is_valid(p[0], p[1], p[2])) {
+            float trans[16];
+            mulm(P.pv, P.obj_model + o * 16, trans);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                v[k].pos = pos4(apply4(mulv(trans, p[k]), P.viewport));
+                v[k].nor = {0, 0, 0, 0};
+                v[k].u = v[k].v = 0;
+                v[k].col = 0;
+            }
+            // cullBackFace (render/cull.go:26-28): culled iff cross.Z < 0
+            ok = !(cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y),
+                           __fsub_rn(v[2].pos.x, v[0].pos.x), __fsub_rn(v[2].pos.y, v[0].pos.y)) < 0.0f);
+            // cullViewFrustum (render/cull.go:15-23): NewAABB((W,H,1),(0,0,0),(0,0,-1))
+            if (ok) {
+                const Box vp = box3(V4{(float)P.W, (float)P.H, 1.0f, 1.0f}, V4{0, 0, 0, 1}, V4{0, 0, -1.0f, 1});
+                ok = box_intersect(vp, box3(v[0].pos, v[1].pos, v[2].pos));
+            }
+        }
     }
-    if (cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y), __fsub_rn(v[2].pos.x, v[0].pos.x),
-                __fsub_rn(v[2].pos.y, v[0].pos.y)) < 0.0f)
-        return;
-    // cullViewFrustum (render/cull.go:15-23): NewAABB((W,H,1),(0,0,0),(0,0,-1))
-    Box vp = box3(V4{(float)P.W, (float)P.H, 1.0f, 1.0f}, V4{0, 0, 0, 1}, V4{0, 0, -1.0f, 1});
-    Box tb = box3(v[0].pos, v[1].pos, v[2].pos);
-    if (!box_intersect(vp, tb)) return;
-    float rw[3] = {1, 1, 1};
-    uint32_t area = write_sub(P, t, t, v, rw, -1);
-    emit_tasks(P, &t, &area, 1);
+    __syncwarp();
+    uint32_t area = 0;
+    if (ok) {
+        float rw[3] = {1, 1, 1};
+        area = write_sub(P, t, t, v, rw, -1);
+    }
+    uint32_t ridx = t;
+    emit_tasks_warp(P, &ridx, &area, ok ? 1 : 0);
 }
 
 // ---------------------------------------------------------------- raster
@@ -376,13 +446,15 @@ constexpr int kRasterWarps = 8;
 
 struct SmRec {
     float x[3], y[3], z[3], sabc;
-    uint32_t x0, y0, bw, seq, k0;
+    uint32_t x0, y0, bw, seq;
+    uint32_t qx0, qy0;  // bbox coordinates of the task's first pixel
+    uint32_t magic;     // ceil(2^32 / bw): floor(t / bw) = umulhi(t, magic) for t < 2^16
 };
 
 // Coverage and depth of one pixel against one record (drawClipped's
 // Barycoord / inside / z lines, render/raster.go:487-496).
 PR_DEV bool pixel_depth(const SmRec& r, int px, int py, float* zout) {
-    float fx = __fadd_rn((float)px, 0.5f), fy = __fadd_rn((float)py, 0.5f);
+    float fx = __fadd_rn(small_u2f((uint32_t)px), 0.5f), fy = __fadd_rn(small_u2f((uint32_t)py), 0.5f);
     float apx = __fsub_rn(fx, r.x[0]), apy = __fsub_rn(fy, r.y[0]);
     float abx = __fsub_rn(r.x[1], r.x[0]), aby = __fsub_rn(r.y[1], r.y[0]);
     float acx = __fsub_rn(r.x[2], r.x[0]), acy = __fsub_rn(r.y[2], r.y[0]);
@@ -444,7 +516,9 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
                 s.x0 = x0;
                 s.y0 = y0;
                 s.bw = bw;
-                s.k0 = k0;
+                s.qy0 = k0 / bw;  // one division per task
+                s.qx0 = k0 - s.qy0 * bw;
+                s.magic = 0xFFFFFFFFu / bw + 1u;
             }
         }
         int incl = cnt;
@@ -462,10 +536,12 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
             for (int step = 16; step > 0; step >>= 1)
                 if (s_start[warp][j + step] <= g) j += step;
             const SmRec& r = s_rec[warp][j];
-            uint32_t k = r.k0 + (uint32_t)(g - s_start[warp][j]);
-            uint32_t qy = k / r.bw;
-            int px = (int)(r.x0 + (k - qy * r.bw));
-            int py = (int)(r.y0 + qy);
+            // pixel qx0 + l of the task's first row, l < kTaskPx: t < 2^15,
+            // where the multiply-high quotient is exact for bw < 2^15
+            const uint32_t t = r.qx0 + (uint32_t)(g - s_start[warp][j]);
+            const uint32_t q = __umulhi(t, r.magic);
+            int px = (int)(r.x0 + (t - q * r.bw));
+            int py = (int)(r.y0 + r.qy0 + q);
             float z;
             if (!pixel_depth(r, px, py, &z)) continue;
             bool zn = isnan(z);
@@ -567,7 +643,7 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
         const float X0 = q0.x, Y0 = q0.y, Z0 = q0.z, X1 = q0.w, Y1 = q1.x, Z1 = q1.y, X2 = q1.z, Y2 = q1.w, Z2 = q2.x;
         const float sabc = q2.y;
         const AttrRec& A = P.arec[ridx];
-        const float fx = __fadd_rn((float)x, 0.5f), fy = __fadd_rn((float)y, 0.5f);
+        const float fx = __fadd_rn(small_u2f((uint32_t)x), 0.5f), fy = __fadd_rn(small_u2f((uint32_t)y), 0.5f);
         float bc[3];
         barycoord_s(fx, fy, X0, Y0, X1, Y1, X2, Y2, sabc, bc);
         const float z = __fadd_rn(__fadd_rn(__fmul_rn(bc[0], Z0), __fmul_rn(bc[1], Z1)), __fmul_rn(bc[2], Z2));
@@ -628,7 +704,7 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
             if (P.n_lights == 0) {
                 c0 = t0; c1 = t1; c2 = t2; c3 = t3;
             } else {
-                const float cr = (float)t0, cg = (float)t1, cb = (float)t2;
+                const float cr = small_u2f(t0), cg = small_u2f(t1), cb = small_u2f(t2);
                 float LaR = 0, LaG = 0, LaB = 0;
                 for (int e = 0; e < P.n_ambient; e++) {
                     LaR = __fadd_rn(LaR, __fmul_rn(P.ambient[e], cr));
@@ -663,8 +739,8 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
                     LsB = __fadd_rn(LsB, __fmul_rn(__fmul_rn(Ls, L.color[2]), I));
                 }
                 auto fin = [&](float La, float Ld, float Ls, uint8_t kd, uint8_t ks) {
-                    float v = __fadd_rn(__fadd_rn(La, __fdiv_rn(__fmul_rn((float)kd, Ld), 255.0f)),
-                                        __fdiv_rn(__fmul_rn((float)ks, Ls), 255.0f));
+                    float v = __fadd_rn(__fadd_rn(La, __fdiv_rn(__fmul_rn(small_u2f(kd), Ld), 255.0f)),
+                                        __fdiv_rn(__fmul_rn(small_u2f(ks), Ls), 255.0f));
                     return go_f2u8(pclamp(pround(v), 0.0f, 255.0f));
                 };
                 c0 = fin(LaR, LdR, LsR, mat->diffuse[0], mat->specular[0]);
@@ -682,7 +758,7 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
                         occl++;
                         continue;
                     }
-                    V4 sc = pos4(apply4(apply4(apply4(apply4(V4{(float)x, (float)y, z, 1.0f}, P.s2w), L.lview), L.lproj),
+                    V4 sc = pos4(apply4(apply4(apply4(apply4(V4{small_u2f((uint32_t)x), small_u2f((uint32_t)y), z, 1.0f}, P.s2w), L.lview), L.lproj),
                                         P.shadow_vp));
                     long long lx = go_f2i(sc.x), ly = go_f2i(sc.y);
                     long long idx = (long long)((unsigned long long)lx + (unsigned long long)ly * (unsigned long long)(long long)P.SW);
@@ -692,9 +768,9 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
                     }
                 }
                 float w = pow_half(occl);
-                c0 = go_f2u8(__fmul_rn((float)c0, w));
-                c1 = go_f2u8(__fmul_rn((float)c1, w));
-                c2 = go_f2u8(__fmul_rn((float)c2, w));
+                c0 = go_f2u8(__fmul_rn(small_u2f(c0), w));
+                c1 = go_f2u8(__fmul_rn(small_u2f(c1), w));
+                c2 = go_f2u8(__fmul_rn(small_u2f(c2), w));
             }
             // AmbientOcclusionShade (material/ao.go:20-73) runs in ao_kernel
             // on a compacted list of these pixels.
@@ -734,13 +810,6 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
 __constant__ float2 c_ao_q[8][100];
 __constant__ float c_ao_rbound[100];
 
-// int(v) of Go for |v| < 2^23: truncation toward zero on the FP32 pipe.
-PR_DEV int trunc_small(float v) {
-    const float a = fabsf(v);
-    const int k = (int)(__float_as_uint(__fadd_rz(a, 8388608.0f)) - 0x4B000000u);
-    return v < 0.0f ? -k : k;
-}
-
 // distance of material/ao.go:52, p.Sub(cur).Len() with z = w = 0
 PR_DEV float ao_distance(float pxf, float pyf, float cx, float cy) {
     const float ddx = __fsub_rn(pxf, cx), ddy = __fsub_rn(pyf, cy);
@@ -772,7 +841,7 @@ __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParam
         const int x = (int)i - r * W;
         const int y = H - 1 - r;
         const float z = P.depth[i];
-        const float pxf = (float)x, pyf = (float)y;
+        const float pxf = small_u2f((uint32_t)x), pyf = small_u2f((uint32_t)y);
         float total = 0.0f;
         for (int k = 0; k < P.n_dirs; k++) {
             float best = 0.0f;
@@ -823,9 +892,9 @@ __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParam
         total = __fdiv_rn(total, 12.5663706143591729539f);  // (Pi/2)*8 as float32
         total = __double2float_rn(go_pow((double)total, 10000.0));
         const uchar4 c = P.rgba[i];
-        uint32_t c0 = go_f2u8(__fmul_rn(total, (float)c.x));
-        uint32_t c1 = go_f2u8(__fmul_rn(total, (float)c.y));
-        uint32_t c2 = go_f2u8(__fmul_rn(total, (float)c.z));
+        uint32_t c0 = go_f2u8(__fmul_rn(total, small_u2f(c.x)));
+        uint32_t c1 = go_f2u8(__fmul_rn(total, small_u2f(c.y)));
+        uint32_t c2 = go_f2u8(__fmul_rn(total, small_u2f(c.z)));
         if (P.gamma_on) {
             c0 = P.gamma[c0];
             c1 = P.gamma[c1];
@@ -846,10 +915,15 @@ int check(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
 
 }  // namespace
 
-int launch_setup_main(const SetupParams& p, void* stream) {
+int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream) {
     if (p.n_tris == 0) return 0;
     unsigned nb = (p.n_tris + 127) / 128;
-    setup_main_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p);
+    setup_main_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return check(e);
+    // The clip list length is known only on the device: size the grid for
+    // the worst case; idle blocks exit at once.
+    clip_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
     return check(cudaGetLastError());
 }
 int launch_setup_shadow(const SetupParams& p, void* stream) {

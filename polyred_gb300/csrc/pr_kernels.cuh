@@ -154,7 +154,7 @@ struct AoParams {
 
 // Launch wrappers implemented in pr_kernels.cu (host-callable).
 namespace prk {
-int launch_setup_main(const SetupParams& p, void* stream);
+int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream);
 int launch_setup_shadow(const SetupParams& p, void* stream);
 int launch_raster(const RasterParams& p, int n_blocks, void* stream);
 int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
