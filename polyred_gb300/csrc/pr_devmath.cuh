@@ -29,7 +29,9 @@ namespace prd {
 //   FP64 unit compute the reference expression directly. On random and
 //   pixel-grid data that is fewer than 1 in 10^7 calls.
 // ---------------------------------------------------------------------------
-PR_DEV float fma64f_slow(float a, float b, float c) {
+// Kept out of line: if the compiler predicated this into the fast path, the
+// FP64 pipe (2 lanes/clk/SM on GB300) would be occupied on every call.
+__device__ __noinline__ float fma64f_slow(float a, float b, float c) {
     return __double2float_rn(__fma_rn((double)a, (double)b, (double)c));
 }
 
@@ -58,13 +60,13 @@ PR_DEV float fma64f(float a, float b, float c) {
     float u = __uint_as_float((ex - 24u) << 23);
     float ad = fabsf(r2);
     bool bad = !(ad <= u);  // NaN / out-of-bound residual (overflow inside the EFT)
-    if (special | bad) return fma64f_slow(a, b, c);
+    if (__builtin_expect(special | bad, 0)) return fma64f_slow(a, b, c);
     // A double-rounding hazard puts s within 2^-29 u of a midpoint, which
     // makes r2 = RN32(s - r1) exactly +-u (or +-u/2 below a power of two).
     if (ad != u && ad != 0.5f * u) return r1;
     // r2 on a midpoint: s is exactly the midpoint (harmless) iff r3 == 0.
     float r3 = __fsub_rn(z1, __fsub_rn(r2, g));
-    if (r3 == 0.0f) return r1;
+    if (__builtin_expect(r3 == 0.0f, 1)) return r1;
     return fma64f_slow(a, b, c);
 }
 
