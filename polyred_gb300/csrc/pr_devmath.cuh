@@ -198,7 +198,7 @@ PR_DEV bool is_odd_int(double x) {
     long long i = (long long)xi;
     return (i & 1) == 1;
 }
-PR_DEV double go_pow(double x, double y) {
+__device__ __noinline__ double go_pow(double x, double y) {
     if (y == 0 || x == 1) return 1;
     if (y == 1) return x;
     if (isnan(x) || isnan(y)) return __longlong_as_double(0x7ff8000000000000ll);
@@ -293,10 +293,29 @@ PR_DEV double go_satan(double x) {
     if (x > Tan3pio8) return __dadd_rn(__dsub_rn(PiOver2, go_xatan(__ddiv_rn(1.0, x))), Morebits);
     return __dadd_rn(__dadd_rn(PiOver4, go_xatan(__ddiv_rn(__dsub_rn(x, 1.0), __dadd_rn(x, 1.0)))), 0.5 * Morebits);
 }
-PR_DEV double go_atan(double x) {
+__device__ __noinline__ double go_atan(double x) {
     if (x == 0) return x;
     if (x > 0) return go_satan(x);
     return -go_satan(-x);
+}
+
+// float32(Go math.Atan(x)) for a positive normal float32 x. For small x,
+// Atan(x) = x - x^3/3 + O(x^5) lies below x by less than half the gap to the
+// float32 below x whenever x^3 <= that gap (a 1.5x margin over x^3/3, far
+// above the float64 error of Go's Cephes evaluation), so it rounds back to x.
+// Other arguments take the float64 algorithm.
+PR_DEV float atan_f32(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t e = b >> 23;
+    if (e >= 1u && e < 255u) {
+        // gap to the next float32 below x: 2^(E-23), or 2^(E-24) at a power of two
+        const uint32_t ge = (b & 0x7fffffu) ? e - 23u : e - 24u;
+        if ((int)ge >= 1) {
+            const float gap = __uint_as_float(ge << 23);
+            if (__fmul_rn(__fmul_rn(x, x), x) <= __fmul_rn(gap, 0.999f)) return x;
+        }
+    }
+    return __double2float_rn(go_atan((double)x));
 }
 
 }  // namespace prd

@@ -804,11 +804,8 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
 
 // ---------------------------------------------------------------- AO
 
-// Tap offsets float32(dir*t) for the 8 march directions (material/ao.go:28,
-// :51 dir.Scale(t, t, 1, 1)) and, per t, a multiplier m[t] >= 1/(t - 0.01)
-// that bounds the ratio elev/dist from above (see ao_kernel).
-__constant__ float2 c_ao_q[8][100];
-__constant__ float c_ao_rbound[100];
+// The 8 march directions (material/ao.go:28): cos/sin of the float32 angle.
+__constant__ float c_ao_dir[2][8];
 
 // distance of material/ao.go:52, p.Sub(cur).Len() with z = w = 0
 PR_DEV float ao_distance(float pxf, float pyf, float cx, float cy) {
@@ -824,17 +821,20 @@ PR_DEV float ao_distance(float pxf, float pyf, float cx, float cy) {
 // dist < 1) makes the direction NaN, as Go's math.Max propagates NaN.
 //
 // Exactness of the fast paths:
-//  * cur = p + float32(dir*t) stays within (-101, W+100) x (-101, H+100), so
-//    Go's int() is a 32-bit truncation here (trunc_small).
+//  * cur = p + float32(dir*t) (dir.Scale(t,t,1,1) then Add) stays within
+//    (-101, W+100) x (-101, H+100); Go's int(cur) is in [0, W) exactly when
+//    -1 < cur < W, and equals floor(max(cur, 0)) there.
 //  * cur moves monotonically in t, so once a tap leaves the buffer every
-//    later tap does too (the reference returns there).
+//    later tap does too (the reference returns there): `alive` masks them.
 //  * |cur - (p + dir*t)| < 2^-9 for buffers up to 16384 wide and |dir| = 1
-//    within 1e-7, so dist >= t - 0.002 for t >= 1; a tap with
-//    elev * m[t] <= best cannot raise best, and is skipped without computing
-//    its distance. t = 0 always has dist = 0 and is skipped by the reference.
+//    within 1e-7, so dist >= t - 0.002 for t >= 1: a tap with
+//    elev <= best * (t - 0.0101) * (1 - 2^-20) cannot raise best and needs
+//    neither its distance nor its division. t = 0 has dist = 0 and is always
+//    skipped by the reference.
 __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParams P) {
     const uint32_t n = P.cnt->n_ao;
     const int W = P.W, H = P.H;
+    const float fW = (float)W, fH = (float)H;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const uint32_t i = P.list[j];
         const int r = (int)(i / (uint32_t)W);
@@ -844,40 +844,29 @@ __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParam
         const float pxf = small_u2f((uint32_t)x), pyf = small_u2f((uint32_t)y);
         float total = 0.0f;
         for (int k = 0; k < P.n_dirs; k++) {
+            const float dX = c_ao_dir[0][k], dY = c_ao_dir[1][k];
             float best = 0.0f;
-            bool nanr = false, done = false;
-            for (int t0 = 1; t0 < 100 && !done; t0 += 4) {
-                float sd[4], cxs[4], cys[4];
-                bool inb[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int t = t0 + u;
-                    const float2 q = c_ao_q[k][t < 100 ? t : 99];
-                    cxs[u] = __fadd_rn(pxf, q.x);
-                    cys[u] = __fadd_rn(pyf, q.y);
-                    const int ix = trunc_small(cxs[u]), iy = trunc_small(cys[u]);
-                    inb[u] = t < 100 && (unsigned)ix < (unsigned)W && (unsigned)iy < (unsigned)H;
-                    const size_t idx = inb[u] ? (size_t)(H - 1 - iy) * W + ix : (size_t)i;
-                    sd[u] = __ldg(P.depth + idx);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if (!inb[u]) {
-                        done = true;
-                        break;
-                    }
-                    const int t = t0 + u;
-                    const float elev = __fsub_rn(sd[u], z);
-                    if (elev > 0.0f) {
-                        if (__fmul_rn(elev, c_ao_rbound[t]) > best) {
-                            const float d = ao_distance(pxf, pyf, cxs[u], cys[u]);
-                            if (d >= 1.0f) best = fmaxf(best, __fdiv_rn(elev, d));
-                        }
-                    } else if (isnan(elev)) {
-                        if (t >= 2 || ao_distance(pxf, pyf, cxs[u], cys[u]) >= 1.0f) {
+            bool nanr = false, alive = true;
+            float tf = 0.0f;
+#pragma unroll 4
+            for (int t = 1; t < 100; t++) {
+                tf = __fadd_rn(tf, 1.0f);
+                const float cx = __fadd_rn(pxf, __fmul_rn(dX, tf));
+                const float cy = __fadd_rn(pyf, __fmul_rn(dY, tf));
+                alive = alive && cx > -1.0f && cx < fW && cy > -1.0f && cy < fH;
+                const uint32_t ix = __float_as_uint(__fadd_rz(fmaxf(cx, 0.0f), 8388608.0f)) - 0x4B000000u;
+                const uint32_t iy = __float_as_uint(__fadd_rz(fmaxf(cy, 0.0f), 8388608.0f)) - 0x4B000000u;
+                const size_t idx = alive ? (size_t)(H - 1 - (int)iy) * W + ix : (size_t)i;
+                const float elev = __fsub_rn(__ldg(P.depth + idx), z);
+                const float thr = __fmul_rn(best, __fmul_rn(__fsub_rn(tf, 0.0101f), 0.99999905f));
+                if (__builtin_expect(alive && !(elev <= thr), 0)) {
+                    const float d = ao_distance(pxf, pyf, cx, cy);
+                    if (d >= 1.0f) {
+                        if (isnan(elev)) {
                             nanr = true;
-                            done = true;
-                            break;
+                            alive = false;
+                        } else {
+                            best = fmaxf(best, __fdiv_rn(elev, d));
                         }
                     }
                 }
@@ -886,7 +875,7 @@ __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParam
             if (nanr)
                 ma = __uint_as_float(0x7fc00000u);
             else
-                ma = best > 0.0f ? __double2float_rn(go_atan((double)best)) : 0.0f;
+                ma = best > 0.0f ? atan_f32(best) : 0.0f;
             total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));  // HalfPi - angle
         }
         total = __fdiv_rn(total, 12.5663706143591729539f);  // (Pi/2)*8 as float32
@@ -960,18 +949,12 @@ int launch_ao(const AoParams& p, int n_blocks, void* stream) {
     return check(cudaGetLastError());
 }
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream) {
-    float2 q[8][100];
-    float rb[100];
-    for (int k = 0; k < 8; k++)
-        for (int t = 0; t < 100; t++) {
-            float ft = (float)t;
-            q[k][t] = k < n ? make_float2(cosv[k] * ft, sinv[k] * ft) : make_float2(0.0f, 0.0f);
-        }
-    rb[0] = 0.0f;
-    for (int t = 1; t < 100; t++) rb[t] = (float)((1.0 / ((double)t - 0.01)) * (1.0 + 0x1p-20));
-    cudaError_t e = cudaMemcpyToSymbolAsync(c_ao_q, q, sizeof(q), 0, cudaMemcpyHostToDevice, (cudaStream_t)stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyToSymbolAsync(c_ao_rbound, rb, sizeof(rb), 0, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+    float d[2][8] = {};
+    for (int k = 0; k < n && k < 8; k++) {
+        d[0][k] = cosv[k];
+        d[1][k] = sinv[k];
+    }
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_ao_dir, d, sizeof(d), 0, cudaMemcpyHostToDevice, (cudaStream_t)stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     return check(e);
 }
