@@ -825,7 +825,8 @@ PR_DEV float ao_distance(float pxf, float pyf, float cx, float cy) {
 //    (-101, W+100) x (-101, H+100); Go's int(cur) is in [0, W) exactly when
 //    -1 < cur < W, and equals floor(max(cur, 0)) there.
 //  * cur moves monotonically in t, so once a tap leaves the buffer every
-//    later tap does too (the reference returns there): `alive` masks them.
+//    later tap does too (the reference returns there): the first such tap is
+//    found by binary search and the march stops before it.
 //  * |cur - (p + dir*t)| < 2^-9 for buffers up to 16384 wide and |dir| = 1
 //    within 1e-7, so dist >= t - 0.002 for t >= 1: a tap with
 //    elev <= best * (t - 0.0101) * (1 - 2^-20) cannot raise best and needs
@@ -845,28 +846,52 @@ __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParam
         float total = 0.0f;
         for (int k = 0; k < P.n_dirs; k++) {
             const float dX = c_ao_dir[0][k], dY = c_ao_dir[1][k];
-            float best = 0.0f;
-            bool nanr = false, alive = true;
-            float tf = 0.0f;
-#pragma unroll 4
-            for (int t = 1; t < 100; t++) {
-                tf = __fadd_rn(tf, 1.0f);
+            // Taps 1 .. t_end-1 lie inside the buffer (monotone in t): find
+            // the first tap outside by binary search.
+            int lo = 1, hi = 100;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                const float tf = small_u2f((uint32_t)mid);
                 const float cx = __fadd_rn(pxf, __fmul_rn(dX, tf));
                 const float cy = __fadd_rn(pyf, __fmul_rn(dY, tf));
-                alive = alive && cx > -1.0f && cx < fW && cy > -1.0f && cy < fH;
-                const uint32_t ix = __float_as_uint(__fadd_rz(fmaxf(cx, 0.0f), 8388608.0f)) - 0x4B000000u;
-                const uint32_t iy = __float_as_uint(__fadd_rz(fmaxf(cy, 0.0f), 8388608.0f)) - 0x4B000000u;
-                const size_t idx = alive ? (size_t)(H - 1 - (int)iy) * W + ix : (size_t)i;
-                const float elev = __fsub_rn(__ldg(P.depth + idx), z);
-                const float thr = __fmul_rn(best, __fmul_rn(__fsub_rn(tf, 0.0101f), 0.99999905f));
-                if (__builtin_expect(alive && !(elev <= thr), 0)) {
-                    const float d = ao_distance(pxf, pyf, cx, cy);
-                    if (d >= 1.0f) {
-                        if (isnan(elev)) {
-                            nanr = true;
-                            alive = false;
-                        } else {
-                            best = fmaxf(best, __fdiv_rn(elev, d));
+                if (cx > -1.0f && cx < fW && cy > -1.0f && cy < fH)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            const int t_end = lo;
+            float best = 0.0f;
+            bool nanr = false;
+            for (int t0 = 1; t0 < t_end && !nanr; t0 += 4) {
+                const float tf0 = small_u2f((uint32_t)t0);
+                // skip bound for every tap of the group (smallest t gives the smallest bound)
+                const float thr = __fmul_rn(best, __fmul_rn(__fsub_rn(tf0, 0.0101f), 0.99999905f));
+                float el[4], cxs[4], cys[4];
+                bool cand = false;
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const float tf = __fadd_rn(tf0, (float)u);
+                    cxs[u] = __fadd_rn(pxf, __fmul_rn(dX, tf));
+                    cys[u] = __fadd_rn(pyf, __fmul_rn(dY, tf));
+                    const bool valid = t0 + u < t_end;
+                    const uint32_t ix = __float_as_uint(__fadd_rz(fmaxf(cxs[u], 0.0f), 8388608.0f)) - 0x4B000000u;
+                    const uint32_t iy = __float_as_uint(__fadd_rz(fmaxf(cys[u], 0.0f), 8388608.0f)) - 0x4B000000u;
+                    const size_t idx = valid ? (size_t)(H - 1 - (int)iy) * W + ix : (size_t)i;
+                    el[u] = __fsub_rn(__ldg(P.depth + idx), z);
+                    if (!valid) el[u] = -1.0f;
+                    cand = cand || !(el[u] <= thr);
+                }
+                if (cand) {
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        if (!(el[u] <= thr) && !nanr) {
+                            const float d = ao_distance(pxf, pyf, cxs[u], cys[u]);
+                            if (d >= 1.0f) {
+                                if (isnan(el[u]))
+                                    nanr = true;
+                                else
+                                    best = fmaxf(best, __fdiv_rn(el[u], d));
+                            }
                         }
                     }
                 }
