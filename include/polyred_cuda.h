@@ -247,6 +247,52 @@ int pr_shadow_camera(const float light_pos[3], const float scene_center[3],
                      const float cam_view[16], const float cam_proj[16],
                      float out_view[16], float out_proj[16]);
 
+/* ---- allocation-free depth map ------------------------------------------
+ * No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory: a host whose device memory
+ * is all owned by another allocator (for example a framework's fixed caching
+ * pool), or a frame loop that cannot pay for cudaMalloc/cudaFree (cudaFree
+ * synchronises the whole device). It runs the shadow-map raster — the
+ * drawDepth pass of render/shadow.go, the same kernels pr_render uses for
+ * shadow maps — on the caller's device triangles into the caller's device
+ * depth map, which is read and then updated like the reference's persistent
+ * maps. It allocates nothing: all scratch lives in one static 16 MiB device
+ * array of the library, which every GPU that loads the library keeps until
+ * the process exits.
+ *
+ * Limits (larger inputs are rejected with PR_ERR_INVALID_ARG, or
+ * PR_ERR_OVERFLOW for the task count, leaving the map unchanged):
+ * n_tris <= PR_NOALLOC_MAX_TRIS, n_objects <= PR_NOALLOC_MAX_OBJECTS,
+ * width*height <= PR_NOALLOC_MAX_TEXELS, raster tasks (1024-pixel chunks of
+ * the triangles' pixel boxes) <= PR_NOALLOC_MAX_TASKS.
+ *
+ * The first call on a device looks up the array's device address, so make
+ * that call before any stream capture. Every call uses the same array: calls
+ * whose work overlaps on the GPU (other streams, other host threads) race and
+ * corrupt each other. The call returns when its work on `stream` is done.
+ */
+#define PR_NOALLOC_MAX_TRIS    65536
+#define PR_NOALLOC_MAX_OBJECTS 256
+#define PR_NOALLOC_MAX_TEXELS  1048576
+#define PR_NOALLOC_MAX_TASKS   262144
+
+typedef struct pr_depth_map_desc {
+    uint32_t size;
+    uint32_t n_tris;
+    uint32_t n_objects;
+    int32_t  width, height;
+    uint32_t reserved;
+    const float*     pos;      /* DEVICE [n_tris][3][4] Vertex.Pos */
+    const pr_object* objects;  /* HOST [n_objects]: first_tri, n_tris, model */
+    float view[16];            /* light camera View (row-major) */
+    float proj[16];            /* light camera Proj */
+    float* depth;              /* DEVICE [height][width] map, texel x + y*width */
+    void*  stream;             /* cudaStream_t; NULL = the default stream */
+} pr_depth_map_desc;
+
+int pr_depth_map_noalloc(const pr_depth_map_desc* desc);
+
 #ifdef __cplusplus
 }
 #endif

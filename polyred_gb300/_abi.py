@@ -86,6 +86,19 @@ class pr_stats(C.Structure):
                 ("ms_total", C.c_float)]
 
 
+PR_NOALLOC_MAX_TRIS = 65536
+PR_NOALLOC_MAX_OBJECTS = 256
+PR_NOALLOC_MAX_TEXELS = 1048576
+PR_NOALLOC_MAX_TASKS = 262144
+
+
+class pr_depth_map_desc(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("n_tris", C.c_uint32), ("n_objects", C.c_uint32), ("width", C.c_int32),
+                ("height", C.c_int32), ("reserved", C.c_uint32), ("pos", C.c_void_p),
+                ("objects", C.POINTER(pr_object)), ("view", F16), ("proj", F16), ("depth", C.c_void_p),
+                ("stream", C.c_void_p)]
+
+
 # Every entry point include/polyred_cuda.h declares: (name, restype, argtypes).
 VP = C.c_void_p
 FP = C.POINTER(C.c_float)
@@ -108,6 +121,7 @@ ENTRY_POINTS = [
     ("pr_mat4_mul", C.c_int, [FP, FP, FP]),
     ("pr_mat4_inv", C.c_int, [FP, FP]),
     ("pr_shadow_camera", C.c_int, [FP, FP, FP, FP, FP, FP]),
+    ("pr_depth_map_noalloc", C.c_int, [C.POINTER(pr_depth_map_desc)]),
 ]
 
 

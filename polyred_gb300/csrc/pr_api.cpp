@@ -522,6 +522,8 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
 
 }  // namespace
 
+int prk::set_last_error(int status, const char* msg) { return fail(status, "%s", msg); }
+
 extern "C" {
 
 int pr_abi_version(void) { return PR_ABI_VERSION; }

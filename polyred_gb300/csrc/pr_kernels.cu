@@ -14,7 +14,11 @@
 // Compiled with -fmad=false -prec-div=true -prec-sqrt=true -ftz=false.
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <mutex>
+
 #include "pr_devmath.cuh"
+#include "pr_hostmath.h"
 #include "pr_kernels.cuh"
 
 using namespace prd;
@@ -1001,3 +1005,174 @@ int sm_count() {
 }
 
 }  // namespace prk
+
+namespace prk {
+
+// ===========================================================================
+// Allocation-free depth-map raster (pr_depth_map_noalloc).
+//
+// For callers that must not allocate device memory themselves: a host whose
+// device memory is entirely owned by another allocator (a framework's fixed
+// caching pool), or a frame loop that cannot afford cudaMalloc/cudaFree
+// (cudaFree synchronises the whole device). It runs the shadow-map raster
+// (setup_shadow_kernel + raster_kernel, the drawDepth pass) with every byte
+// of scratch carved from the fixed array below, which each GPU that loads the
+// library keeps until the process exits.
+//
+// Calls share the array: two calls whose work overlaps on the GPU (different
+// streams, or different host threads) race on it and corrupt each other's
+// results. Each call clears the parts that must start at zero.
+// ===========================================================================
+
+namespace {
+
+constexpr uint32_t kNoAllocMaxTris = 65536;
+constexpr uint32_t kNoAllocMaxObjects = 256;
+constexpr uint32_t kNoAllocMaxTexels = 1u << 20;  // e.g. 1024 x 1024
+constexpr uint32_t kNoAllocMaxTasks = 4u * kNoAllocMaxTris;
+
+constexpr size_t kNaCounters = 0;                                   // Counters
+constexpr size_t kNaObjFirst = 256;                                 // u32 [max_objects + 1]
+constexpr size_t kNaObjModel = kNaObjFirst + 4096;                  // f32 [max_objects][16]
+constexpr size_t kNaRecords = kNaObjModel + kNoAllocMaxObjects * 64; // RasterRec [max_tris]
+constexpr size_t kNaTasks = kNaRecords + (size_t)kNoAllocMaxTris * sizeof(RasterRec);
+constexpr size_t kNaKeys = kNaTasks + (size_t)kNoAllocMaxTasks * sizeof(uint2);
+constexpr size_t kNaLastNan = kNaKeys + (size_t)kNoAllocMaxTexels * 4;
+constexpr size_t kNaBytes = kNaLastNan + (size_t)kNoAllocMaxTexels * 4;
+static_assert(kNaBytes <= (16u << 20), "scratch layout exceeds 16 MiB");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[16u << 20];
+
+__global__ void encode_map_kernel(const float* depth, uint32_t* keys, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = depth[i];
+    keys[i] = isnan(d) ? 0u : fkey(d);  // key 0 stands for NaN (below every value)
+}
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {};
+
+}  // namespace
+
+}  // namespace prk
+
+extern "C" int pr_depth_map_noalloc(const pr_depth_map_desc* d) {
+    using namespace prk;
+    auto err = [](int code, const char* msg) { return set_last_error(code, msg); };
+    if (!d) return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: desc is NULL");
+    if (d->size < sizeof(pr_depth_map_desc)) return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: desc->size too small");
+    if (d->n_tris > kNoAllocMaxTris)
+        return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: n_tris exceeds PR_NOALLOC_MAX_TRIS (65536)");
+    if (d->n_objects > kNoAllocMaxObjects)
+        return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: n_objects exceeds PR_NOALLOC_MAX_OBJECTS (256)");
+    if (d->width <= 0 || d->height <= 0 || (uint64_t)d->width * (uint64_t)d->height > kNoAllocMaxTexels)
+        return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: width*height must be in 1..PR_NOALLOC_MAX_TEXELS (1048576)");
+    if (!d->depth || (d->n_tris > 0 && (!d->pos || !d->objects || d->n_objects == 0)))
+        return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: NULL input or output pointer");
+    uint32_t expect = 0;
+    for (uint32_t o = 0; o < d->n_objects; o++) {
+        if (d->objects[o].first_tri != expect)
+            return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: objects must tile the triangles in order");
+        expect += d->objects[o].n_tris;
+    }
+    if (expect != d->n_tris) return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: objects do not cover n_tris");
+
+    // Once per device, with that device current: the device address of the
+    // scratch array (its host-side name is not a device address).
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return err(PR_ERR_NO_DEVICE, "pr_depth_map_noalloc: no current CUDA device");
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: cudaGetSymbolAddress failed");
+            g_noalloc_addr[dev] = p;
+        }
+        base = (unsigned char*)g_noalloc_addr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)d->stream;
+    Counters* cnt = (Counters*)(base + kNaCounters);
+    uint32_t* obj_first = (uint32_t*)(base + kNaObjFirst);
+    float* obj_model = (float*)(base + kNaObjModel);
+    RasterRec* rrec = (RasterRec*)(base + kNaRecords);
+    uint2* tasks = (uint2*)(base + kNaTasks);
+    uint32_t* keys = (uint32_t*)(base + kNaKeys);
+    uint32_t* lastnan = (uint32_t*)(base + kNaLastNan);
+    const size_t n = (size_t)d->width * d->height;
+
+    // object tables (host -> the scratch array)
+    uint32_t first[kNoAllocMaxObjects + 1];
+    float model[kNoAllocMaxObjects * 16];
+    for (uint32_t o = 0; o < d->n_objects; o++) {
+        first[o] = d->objects[o].first_tri;
+        std::memcpy(model + o * 16, d->objects[o].model, 64);
+    }
+    first[d->n_objects] = d->n_tris;
+    cudaError_t e = cudaSuccess;
+    if (d->n_objects > 0) {
+        e = cudaMemcpyAsync(obj_first, first, (d->n_objects + 1) * 4, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(obj_model, model, d->n_objects * 64, cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(Counters), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(lastnan, 0, n * 4, st);
+    if (e != cudaSuccess) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: scratch initialisation failed");
+    encode_map_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d->depth, keys, n);
+
+    SetupParams sp{};
+    sp.pos = (const float4*)d->pos;
+    sp.obj_first = obj_first;
+    sp.obj_model = obj_model;
+    sp.n_tris = d->n_tris;
+    sp.n_objects = d->n_objects;
+    sp.W = d->width;
+    sp.H = d->height;
+    sp.perspective = 0;
+    prh::M4 pv = prh::mulm(prh::M4{{d->proj[0], d->proj[1], d->proj[2], d->proj[3], d->proj[4], d->proj[5], d->proj[6],
+                                     d->proj[7], d->proj[8], d->proj[9], d->proj[10], d->proj[11], d->proj[12],
+                                     d->proj[13], d->proj[14], d->proj[15]}},
+                           prh::M4{{d->view[0], d->view[1], d->view[2], d->view[3], d->view[4], d->view[5], d->view[6],
+                                     d->view[7], d->view[8], d->view[9], d->view[10], d->view[11], d->view[12],
+                                     d->view[13], d->view[14], d->view[15]}});
+    prh::M4 vp = prh::viewport((float)d->width, (float)d->height);
+    std::memcpy(sp.pv, pv.m, 64);
+    std::memcpy(sp.viewport, vp.m, 64);
+    sp.rrec = rrec;
+    sp.cap_rec = kNoAllocMaxTris;
+    sp.tasks = tasks;
+    sp.cap_tasks = kNoAllocMaxTasks;
+    sp.cnt = cnt;
+    int rc = launch_setup_shadow(sp, st);
+    RasterParams rp{};
+    rp.rrec = rrec;
+    rp.tasks = tasks;
+    rp.cnt = cnt;
+    rp.cnt_w = cnt;
+    rp.W = d->width;
+    rp.H = d->height;
+    rp.mode = kShadow;
+    rp.smap = keys;
+    rp.lastnan = lastnan;
+    if (!rc) rc = launch_raster(rp, sm_count() * 8, st);
+    if (!rc) rc = launch_shadow_fixup_reset(d->width, d->height, lastnan, keys, cnt, st);
+    rp.mode = kShadowFixup;
+    if (!rc) rc = launch_raster(rp, sm_count() * 8, st);
+    if (rc) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: kernel launch failed");
+    Counters h{};
+    e = cudaMemcpyAsync(&h, cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: execution failed");
+    if (h.overflow)
+        return err(PR_ERR_OVERFLOW, "pr_depth_map_noalloc: more raster tasks than PR_NOALLOC_MAX_TASKS (262144); "
+                                    "the depth map was left unchanged");
+    rc = launch_decode_shadow(keys, d->depth, n, st);
+    if (!rc) {
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = (int)e;
+    }
+    if (rc) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: decode failed");
+    return PR_OK;
+}

@@ -168,4 +168,6 @@ int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* strea
 int launch_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n,
                      void* stream);
 int sm_count();
+// Records a status and its detail as the calling thread's last error.
+int set_last_error(int status, const char* msg);
 }  // namespace prk
