@@ -73,7 +73,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -122,9 +122,9 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per launch of the shade kernel from the committed ncu
-    summary (profiles/shade_kernel_sphere_field_1080p.txt), or None."""
-    p = os.path.join(ROOT, "profiles", "shade_kernel_sphere_field_1080p.txt")
+    """DRAM bytes per launch of the AO kernel from the committed ncu summary
+    (profiles/ao_kernel_sphere_field_1080p.txt), or None."""
+    p = os.path.join(ROOT, "profiles", "ao_kernel_sphere_field_1080p.txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -191,7 +191,7 @@ def cpu_baseline_sample():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -261,7 +261,7 @@ def main():
     clocks.start()
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    phases = {"ms_shadow": [], "ms_setup": [], "ms_raster": [], "ms_shade": []}
+    phases = {"ms_shadow": [], "ms_setup": [], "ms_raster": [], "ms_shade": [], "ms_ao": [], "n_ao_pixels": []}
     launches = 0
     ev0.record(stream)
     for _ in range(args.steps):
@@ -302,12 +302,14 @@ def main():
     h2d = sum(getattr(flat, n).nbytes for n in ("pos", "nor", "uv", "col", "mat_id"))
     d2h = W * H * (4 + 4 + 4)
 
-    # roofline of the dominant kernel: the deferred shade kernel
-    # (per pixel: winner id 4 B + depth 4 B read, RGBA8 4 B + tri-ID 4 B + depth 4 B written)
+    # roofline of the dominant kernel, ao_kernel (AmbientOcclusionShade):
+    # algorithmic bytes per launch = the depth buffer read once (4 B/px) +
+    # per AO pixel its list entry (4 B) and its colour read and written (8 B)
     peak, peak_kind = measured_peaks()
-    shade_ms = ph.get("ms_shade", 0.0)
-    alg_bytes = W * H * 20
-    achieved = alg_bytes / (shade_ms / 1e3) / 1e9 if shade_ms > 0 else 0.0
+    ao_ms = ph.get("ms_ao", 0.0)
+    n_ao = ph.get("n_ao_pixels", 0.0)
+    alg_bytes = W * H * 4 + n_ao * 12
+    achieved = alg_bytes / (ao_ms / 1e3) / 1e9 if ao_ms > 0 else 0.0
     traffic = ncu_traffic()
 
     if rank == 0:
@@ -324,8 +326,9 @@ def main():
                 "phases_ms": ph,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak if peak else None, "traffic": traffic,
-                             "kernel": "shade_kernel", "peak_source": peak_kind,
-                             "algorithmic_bytes": alg_bytes},
+                             "kernel": "ao_kernel", "peak_source": peak_kind,
+                             "algorithmic_bytes": alg_bytes,
+                             "note": "compute-bound: 8 x 99 dependent depth taps per pixel (L1/L2 resident)"},
                 "gpu_launches": launches,
                 "clocks": clk}
         if world == 1 and not args.no_cpu_baseline:

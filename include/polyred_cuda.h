@@ -185,6 +185,8 @@ typedef struct pr_stats {
     uint32_t n_kernel_launches;
     uint32_t reserved;
     float    ms_shadow, ms_setup, ms_raster, ms_shade, ms_total;
+    float    ms_ao;            /* ambient occlusion part of ms_shade */
+    uint32_t n_ao_pixels;
 } pr_stats;
 
 /* ---- entry points ------------------------------------------------------ */

@@ -83,7 +83,7 @@ class pr_stats(C.Structure):
                 ("n_clipped_tris", C.c_uint32), ("n_raster_tasks", C.c_uint32), ("n_nan_fragments", C.c_uint32),
                 ("n_kernel_launches", C.c_uint32), ("reserved", C.c_uint32), ("ms_shadow", C.c_float),
                 ("ms_setup", C.c_float), ("ms_raster", C.c_float), ("ms_shade", C.c_float),
-                ("ms_total", C.c_float)]
+                ("ms_total", C.c_float), ("ms_ao", C.c_float), ("n_ao_pixels", C.c_uint32)]
 
 
 PR_NOALLOC_MAX_TRIS = 65536

@@ -239,6 +239,8 @@ void collect_stats(Ctx* c) {
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->stats.ms_raster = ms;
     cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); c->stats.ms_shade = ms;
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); c->stats.ms_total = ms;
+    cudaEventElapsedTime(&ms, c->ev[5], c->ev[4]); c->stats.ms_ao = ms;
+    c->stats.n_ao_pixels = c->h_cnt[0].n_ao;
 }
 
 int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
@@ -451,6 +453,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         }
         KTRY(prk::launch_shade(sp, st));
         launches += 1;
+        CUDA_TRY(cudaEventRecord(c->ev[5], st));
         if (sp.rgba) {
             // AmbientOcclusionShade + gamma for the pixels the shade kernel listed
             prk::AoParams ap{};
