@@ -3,9 +3,9 @@
 
 1. float32(Go Atan(x)) == x for positive float32 x with x^3 <= 0.999 * gap,
    gap = distance to the float32 below x.
-2. The march distance of material/ao.go:52 satisfies dist >= t - 0.002 for
+2. The march distance of material/ao.go:52 satisfies |dist - t| <= 0.002 for
    every direction and tap t >= 1 at pixel coordinates below 16384, which is
-   what lets a tap with elev * m[t] <= best be skipped.
+   what lets the kernel bound elev/dist from both sides without computing it.
 """
 import ctypes as C
 
@@ -43,6 +43,7 @@ def test_ao_distance_lower_bound(oracle_lib):
     P = np.concatenate([rng.integers(0, 16384, 4000), np.arange(0, 200)]).astype(F)
     t = np.arange(1, 100, dtype=F)
     worst = np.inf
+    worst_hi = -np.inf
     for k in range(8):
         qx = (F(cosv[k]) * t).astype(F)
         qy = (F(sinv[k]) * t).astype(F)
@@ -55,4 +56,6 @@ def test_ao_distance_lower_bound(oracle_lib):
             d2 = (dx.astype(np.float64) * dx + (dy * dy).astype(F).astype(np.float64)).astype(F)
             dist = np.sqrt(d2.astype(np.float64)).astype(F)
             worst = min(worst, float(np.min(dist - t)))
+            worst_hi = max(worst_hi, float(np.max(dist - t)))
     assert worst >= -0.002, worst
+    assert worst_hi <= 0.002, worst_hi
