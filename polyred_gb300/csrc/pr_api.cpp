@@ -105,6 +105,7 @@ struct Ctx {
     DevBuf<float> depth_ao;
     DevBuf<uint32_t> ao_list;
     int n_ao_dirs = 0;
+    float ao_cos[8] = {}, ao_sin[8] = {};
     // shadow maps (persistent across frames)
     int SW = 0, SH = 0, n_slights = 0;
     DevBuf<uint32_t> smap, lastnan;
@@ -461,6 +462,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
             ap.H = H;
             ap.gamma_on = (f->flags & PR_FRAME_GAMMA) ? 1 : 0;
             ap.n_dirs = c->n_ao_dirs;
+            prh::ao_classify(c->ao_cos, c->ao_sin, c->n_ao_dirs, W, H, ap.dir_fast, ap.dir_tiny);
             ap.depth = c->depth_ao.p;
             ap.list = c->ao_list.p;
             ap.cnt = dcnt;
@@ -574,9 +576,8 @@ int pr_create(int device, void** out_ctx) {
     }
     c->n_sms = prk::sm_count();
     {
-        float cs[8], sn[8];
-        prh::ao_directions(cs, sn, &c->n_ao_dirs);
-        int e = prk::set_ao_tables(cs, sn, c->n_ao_dirs, c->stream);
+        prh::ao_directions(c->ao_cos, c->ao_sin, &c->n_ao_dirs);
+        int e = prk::set_ao_tables(c->ao_cos, c->ao_sin, c->n_ao_dirs, c->stream);
         if (e) {
             pr_destroy(c);
             return fail(PR_ERR_CUDA, "AO table upload: %s", cudaGetErrorString((cudaError_t)e));
@@ -753,6 +754,17 @@ int pr_shadow_camera(const float light_pos[3], const float scene_center[3], cons
         return fail(PR_ERR_SINGULAR, "camera matrix is singular");
     std::memcpy(out_view, v.m, 64);
     std::memcpy(out_proj, p.m, 64);
+    return PR_OK;
+}
+
+// Test hook (not part of the public header): the AO kernel's float32 Atan
+// and its certified Pow(T, 10000) colour scaling, each beside the float64
+// algorithm, on n device-resident inputs (col, o_fast, o_ref: 4 bytes each).
+int pr_debug_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const uint8_t* col,
+                      uint8_t* o_fast, uint8_t* o_ref, int n) {
+    int e = prk::launch_ao_probe(x, atan_fast, atan_ref, T, col, o_fast, o_ref, n, nullptr);
+    if (e) return fail(PR_ERR_CUDA, "ao probe launch: %s", cudaGetErrorString((cudaError_t)e));
+    CUDA_TRY(cudaDeviceSynchronize());
     return PR_OK;
 }
 

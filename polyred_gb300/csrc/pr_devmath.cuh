@@ -299,11 +299,19 @@ __device__ __noinline__ double go_atan(double x) {
     return -go_satan(-x);
 }
 
-// float32(Go math.Atan(x)) for a positive normal float32 x. For small x,
-// Atan(x) = x - x^3/3 + O(x^5) lies below x by less than half the gap to the
-// float32 below x whenever x^3 <= that gap (a 1.5x margin over x^3/3, far
-// above the float64 error of Go's Cephes evaluation), so it rounds back to x.
-// Other arguments take the float64 algorithm.
+// float32(Go math.Atan(x)) for a positive normal float32 x.
+//  * Small x: Atan(x) = x - x^3/3 + O(x^5) lies below x by less than half the
+//    gap to the float32 below x whenever x^3 <= that gap (a 1.5x margin over
+//    x^3/3, far above the float64 error of Go's Cephes evaluation), so it
+//    rounds back to x.
+//  * x <= 1/16: Atan(x) = x - c with c = x^3/3 - x^5/5 + ... + x^11/11
+//    (truncation below 3e-16 x). c is evaluated in float32 with relative error
+//    below 1e-6; s = RN(x - c) and the exact residual e = (x - c) - s
+//    (Fast2Sum) place Atan(x), and Go's float64 value of it (relative error
+//    far below 1e-14), within |e| + delta of s, delta = 1e-6 c + 1e-14 x. When
+//    that interval lies strictly inside the rounding interval of s, the
+//    float32 rounding of Go's result is s.
+//  * Otherwise, the float64 algorithm.
 PR_DEV float atan_f32(float x) {
     const uint32_t b = __float_as_uint(x);
     const uint32_t e = b >> 23;
@@ -314,8 +322,67 @@ PR_DEV float atan_f32(float x) {
             const float gap = __uint_as_float(ge << 23);
             if (__fmul_rn(__fmul_rn(x, x), x) <= __fmul_rn(gap, 0.999f)) return x;
         }
+        if (x <= 0.0625f && e >= 40u) {
+            const float x2 = __fmul_rn(x, x);
+            float p = __fsub_rn(0.111111111f, __fmul_rn(x2, 0.0909090909f));
+            p = __fsub_rn(0.142857143f, __fmul_rn(x2, p));
+            p = __fsub_rn(0.2f, __fmul_rn(x2, p));
+            p = __fsub_rn(0.333333333f, __fmul_rn(x2, p));
+            const float c = __fmul_rn(__fmul_rn(x, x2), p);
+            const float s = __fsub_rn(x, c);
+            const float z = __fsub_rn(s, x);
+            const float err = __fsub_rn(-c, z);  // (x - c) - s exactly (Fast2Sum, |c| < |x|)
+            const float delta = __fadd_ru(__fmul_ru(c, 1e-6f), __fmul_ru(x, 1e-14f));
+            const uint32_t bs = __float_as_uint(s);
+            const uint32_t es = bs >> 23;
+            const float hu = __uint_as_float((es - 24u) << 23);                                // half ulp above s
+            const float hd = (bs & 0x7fffffu) ? hu : __uint_as_float((es - 25u) << 23);      // half gap below s
+            if (__fadd_ru(err, delta) < hu && __fsub_rd(err, delta) > -hd) return s;
+        }
     }
     return __double2float_rn(go_atan((double)x));
+}
+
+// The three colour channels of material/ao.go:34-37 after
+// total = math.Pow(T, 10000): uint8(float32(Pow(T, 10000)) * float32(ch)).
+// Pow runs in float32 with a certified error bound, and its float64 form only
+// when that bound leaves a channel undecided:
+//  * T NaN: Pow is NaN and so is every product; Go's uint8 of NaN is 0 (the
+//    low byte of the out-of-range int32). T == 1: Pow is exactly 1.
+//  * 1 - T >= 6e-4: Pow(T, 10000) <= 0.9994^10000 < 0.00248, so every
+//    product is below 255 * 0.00248 < 1 and truncates to 0.
+//  * otherwise, with d = 1 - T exact: ln T = -(d + d u), u = d/2 + d^2/3 +
+//    d^3/4 (truncation below 2e-17 after the factor 10000), 10000 ln T as an
+//    unevaluated float pair, p = exp(hi) (1 + lo) with expf (2 ulp). |p/P - 1|
+//    stays below 4e-7 (P Go's float64 result, itself within 1e-11 of the exact
+//    power after its 27 roundings); float32(P) lies in
+//    [RD(p(1 - 1e-6)), RU(p(1 + 1e-6))], the
+//    product is monotone in it, and where both ends truncate alike the channel
+//    is decided.
+PR_DEV uint3 ao_scale(float T, uint32_t c0, uint32_t c1, uint32_t c2) {
+    if (isnan(T)) return make_uint3(0u, 0u, 0u);
+    if (T == 1.0f) return make_uint3(c0, c1, c2);
+    const float d = __fsub_rn(1.0f, T);
+    if (d >= 6e-4f) return make_uint3(0u, 0u, 0u);
+    if (d > -1e-4f) {
+        const float u = __fmul_rn(d, __fadd_rn(0.5f, __fmul_rn(d, __fadd_rn(0.333333333f, __fmul_rn(d, 0.25f)))));
+        const float h1 = __fmul_rn(10000.0f, d);
+        const float l1 = __fmaf_rn(10000.0f, d, -h1);  // 10000 d = h1 + l1 exactly
+        const float w = __fmul_rn(h1, u);
+        const float sh = __fadd_rn(h1, w);             // Fast2Sum: |w| < |h1|
+        const float e2 = __fsub_rn(w, __fsub_rn(sh, h1));
+        const float lo = -__fadd_rn(e2, l1);
+        const float E = expf(-sh);
+        const float p = __fmaf_rn(E, lo, E);
+        const float plo = __fmul_rd(p, 0.999999f), phi = __fmul_ru(p, 1.000001f);
+        const uint32_t a0 = go_f2u8(__fmul_rn(plo, small_u2f(c0))), b0 = go_f2u8(__fmul_rn(phi, small_u2f(c0)));
+        const uint32_t a1 = go_f2u8(__fmul_rn(plo, small_u2f(c1))), b1 = go_f2u8(__fmul_rn(phi, small_u2f(c1)));
+        const uint32_t a2 = go_f2u8(__fmul_rn(plo, small_u2f(c2))), b2 = go_f2u8(__fmul_rn(phi, small_u2f(c2)));
+        if (__builtin_expect(a0 == b0 && a1 == b1 && a2 == b2, 1)) return make_uint3(a0, a1, a2);
+    }
+    const float P = __double2float_rn(go_pow((double)T, 10000.0));
+    return make_uint3(go_f2u8(__fmul_rn(P, small_u2f(c0))), go_f2u8(__fmul_rn(P, small_u2f(c1))),
+                      go_f2u8(__fmul_rn(P, small_u2f(c2))));
 }
 
 }  // namespace prd

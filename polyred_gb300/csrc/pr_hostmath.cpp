@@ -206,4 +206,38 @@ void ao_directions(float cosv[8], float sinv[8], int* n) {
     *n = k;
 }
 
+void ao_classify(const float cosv[8], const float sinv[8], int n, int W, int H, int8_t fast[8], int8_t tiny[8]) {
+    // Tap coordinates RN(x + a) stay below M = max(W, H) + 100 < 2^(E+1), where
+    // half an ulp is at most 2^(E-24). A component whose a = RN(c t) is, for
+    // every t <= 99, an integer or more than that below the next integer never
+    // rounds up across an integer: int(RN(x + a)) = x + floor(a) for x >= 0.
+    const int M = (W > H ? W : H) + 100;
+    int E = 0;
+    while ((2 << E) <= M) E++;
+    const float h = std::ldexp(1.0f, E - 24);
+    for (int k = 0; k < 8; k++) {
+        fast[k] = 0;
+        tiny[k] = 0;
+        if (k >= n) continue;
+        const float comp[2] = {cosv[k], sinv[k]};
+        bool ok = true;
+        int nt = 0;
+        for (int a = 0; a < 2; a++) {
+            const float c = comp[a];
+            if (c < 0.0f && -c * 99.0f < 1.0f) {  // every a_t in (-1, 0)
+                tiny[k] = (int8_t)(a + 1);
+                nt++;
+                continue;
+            }
+            for (int t = 1; t < 100; t++) {
+                const float at = c * (float)t;
+                if (at != std::floor(at) && std::ceil(at) - at <= h) ok = false;
+            }
+        }
+        if (nt > 1) ok = false;
+        fast[k] = ok ? 1 : 0;
+        if (!ok) tiny[k] = 0;
+    }
+}
+
 }  // namespace prh

@@ -22,5 +22,8 @@ bool shadow_camera(const float light_pos[3], const float center[3], const M4& ca
                    M4* out_view, M4* out_proj);          // render/shadow.go:41-85
 void gamma_table(uint8_t out[256]);                      // shader/gamma.go:13-18 + color/srgb.go
 void ao_directions(float cosv[8], float sinv[8], int* n); // material/ao.go:28
+// Which AO directions may use the device's tap offset table on a W x H frame
+// (fast[k]), and which component is tiny and negative (tiny[k]: 0, 1 = x, 2 = y).
+void ao_classify(const float cosv[8], const float sinv[8], int n, int W, int H, int8_t fast[8], int8_t tiny[8]);
 
 }  // namespace prh

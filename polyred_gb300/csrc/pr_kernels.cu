@@ -811,115 +811,259 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
 // The 8 march directions (material/ao.go:28): cos/sin of the float32 angle.
 __constant__ float c_ao_dir[2][8];
 
+constexpr int kAoTaps = 100;     // t = 0 .. 99 (material/ao.go:44)
+constexpr int kAoTable = 100;    // tap offsets for t = 2 .. 101 (t >= 100: padding, offset 0)
+constexpr float kAoSkip = 1.0f - 0x1p-20f;
+
 // distance of material/ao.go:52, p.Sub(cur).Len() with z = w = 0
 PR_DEV float ao_distance(float pxf, float pyf, float cx, float cy) {
     const float ddx = __fsub_rn(pxf, cx), ddy = __fsub_rn(pyf, cy);
     return __fsqrt_rn(fma64f(ddx, ddx, __fmul_rn(ddy, ddy)));
 }
 
+// The exact ratio elevation/distance of tap t >= 2 (distance >= 1.998).
+__device__ __noinline__ float ao_exact_ratio(int t, float el, float pxf, float pyf, float dX, float dY) {
+    const float tf = small_u2f((uint32_t)t);
+    const float cx = __fadd_rn(pxf, __fmul_rn(dX, tf)), cy = __fadd_rn(pyf, __fmul_rn(dY, tf));
+    return __fdiv_rn(el, ao_distance(pxf, pyf, cx, cy));
+}
+
+// One tap evaluated from its float coordinates, as the reference does:
+// cur = p + dir*t, int(cur) (in [0, W) for the taps the caller passes), the
+// distance check and the ratio. A tap that cannot raise best past the lower
+// bound lb (elev <= lb (1 - 2^-20) (t - 0.0101), using dist >= t - 0.002)
+// needs neither its distance nor its division. Returns false for a NaN
+// elevation at dist >= 1.
+PR_DEV bool ao_tap_exact(int t, float pxf, float pyf, float dX, float dY, int W, int H, const float* depth,
+                         float z, float lb, float& best) {
+    const float tf = small_u2f((uint32_t)t);
+    const float cx = __fadd_rn(pxf, __fmul_rn(dX, tf)), cy = __fadd_rn(pyf, __fmul_rn(dY, tf));
+    const uint32_t ix = __float_as_uint(__fadd_rz(fmaxf(cx, 0.0f), 8388608.0f)) - 0x4B000000u;
+    const uint32_t iy = __float_as_uint(__fadd_rz(fmaxf(cy, 0.0f), 8388608.0f)) - 0x4B000000u;
+    const float el = __fsub_rn(__ldg(depth + ((size_t)(H - 1 - (int)iy) * W + ix)), z);
+    if (el <= __fmul_rn(__fmul_rd(lb, kAoSkip), __fsub_rd(tf, 0.0101f))) return true;
+    const float d = ao_distance(pxf, pyf, cx, cy);
+    if (d < 1.0f) return true;
+    if (isnan(el)) return false;
+    best = fmaxf(best, __fdiv_rn(el, d));
+    return true;
+}
+
+// maxElevationAngle's march for taps 2 .. 101 in groups of four, from a
+// shared table of index offsets (see ao_kernel). Taps whose elevation passes
+// the skip test are candidates; a candidate's ratio is first approximated
+// (f32 distance and rsqrtf, relative error below 1e-6, taken as 8e-6) and
+// kept as the one pending tap; exact ratios are computed only when two
+// candidates' intervals overlap and, once, for the final pending tap. best is
+// exact throughout, lb <= the largest exact ratio seen so far.
+template <bool TINY>
+PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const float* s_tm, int k, const float* p0,
+                           const float* pA, int tstar, float z, float pxf, float pyf, float dX, float dY, float& best) {
+    float lb = best;
+    int pt = 0;
+    float pel = 0.0f, phi = 0.0f;
+    bool nan_seen = false;
+    for (int g = 0; g < n_groups; g++) {
+        const int t0 = 4 * g + 2;
+        const int4 o = *reinterpret_cast<const int4*>(&s_off[k][4 * g]);
+        const float4 tm = *reinterpret_cast<const float4*>(&s_tm[4 * g]);
+        const float lbs = __fmul_rd(lb, kAoSkip);
+        const float* q0 = (TINY && t0 < tstar) ? pA : p0;
+        const float* q1 = (TINY && t0 + 1 < tstar) ? pA : p0;
+        const float* q2 = (TINY && t0 + 2 < tstar) ? pA : p0;
+        const float* q3 = (TINY && t0 + 3 < tstar) ? pA : p0;
+        float el[4];
+        el[0] = __fsub_rn(__ldg(q0 + o.x), z);
+        el[1] = __fsub_rn(__ldg(q1 + o.y), z);
+        el[2] = __fsub_rn(__ldg(q2 + o.z), z);
+        el[3] = __fsub_rn(__ldg(q3 + o.w), z);
+        const bool c0 = !(el[0] <= __fmul_rn(lbs, tm.x));
+        const bool c1 = !(el[1] <= __fmul_rn(lbs, tm.y));
+        const bool c2 = !(el[2] <= __fmul_rn(lbs, tm.z));
+        const bool c3 = !(el[3] <= __fmul_rn(lbs, tm.w));
+        if (c0 | c1 | c2 | c3) {
+            const bool cu[4] = {c0, c1, c2, c3};
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (!cu[u]) continue;
+                const float e = el[u];
+                if (isnan(e)) {
+                    nan_seen = true;
+                    continue;
+                }
+                const int t = t0 + u;
+                const float tf = small_u2f((uint32_t)t);
+                const float cx = __fadd_rn(pxf, __fmul_rn(dX, tf)), cy = __fadd_rn(pyf, __fmul_rn(dY, tf));
+                const float ddx = __fsub_rn(pxf, cx), ddy = __fsub_rn(pyf, cy);
+                const float r = __fmul_rn(e, rsqrtf(__fmaf_rn(ddx, ddx, __fmul_rn(ddy, ddy))));
+                if (!(r >= 0x1p-100f)) {  // outside the relative error bound's range: exact now
+                    best = fmaxf(best, ao_exact_ratio(t, e, pxf, pyf, dX, dY));
+                    lb = fmaxf(lb, best);
+                    continue;
+                }
+                const float rlo = __fmul_rd(r, 0.999992f), rhi = __fmul_ru(r, 1.000008f);
+                if (rhi <= lb) continue;  // cannot exceed what is already held
+                if (pt != 0 && !(rlo >= phi))  // overlaps the pending tap: settle it
+                    best = fmaxf(best, ao_exact_ratio(pt, pel, pxf, pyf, dX, dY));
+                pt = t;
+                pel = e;
+                phi = rhi;
+                lb = fmaxf(best, rlo);
+            }
+            if (nan_seen) return false;
+        }
+    }
+    if (pt != 0) best = fmaxf(best, ao_exact_ratio(pt, pel, pxf, pyf, dX, dY));
+    return true;
+}
+
 // AmbientOcclusionShade (material/ao.go:20-73) for the pixels the shade
-// kernel listed. Per direction, maxangle is the Max over taps of
-// float32(Atan(elev/dist)); Atan and the rounding to float32 are monotone, so
-// it is float32(Atan(best)) with best the largest ratio, and only positive
-// ratios can exceed the initial 0. A NaN ratio (at a tap not skipped for
-// dist < 1) makes the direction NaN, as Go's math.Max propagates NaN.
+// kernel listed, one thread per pixel. Per direction, maxangle is the Max
+// over taps of float32(Atan(elev/dist)); Atan and the rounding to float32 are
+// monotone, so it is float32(Atan(best)) with best the largest ratio, and
+// only positive ratios can exceed the initial 0. A NaN ratio (at a tap not
+// skipped for dist < 1) makes the direction, and so the pixel, NaN.
 //
-// Exactness of the fast paths:
-//  * cur = p + float32(dir*t) (dir.Scale(t,t,1,1) then Add) stays within
-//    (-101, W+100) x (-101, H+100); Go's int(cur) is in [0, W) exactly when
-//    -1 < cur < W, and equals floor(max(cur, 0)) there.
-//  * cur moves monotonically in t, so once a tap leaves the buffer every
-//    later tap does too (the reference returns there): the first such tap is
-//    found by binary search and the march stops before it.
-//  * |cur - (p + dir*t)| < 2^-9 for buffers up to 16384 wide and |dir| = 1
-//    within 1e-7, so dist >= t - 0.002 for t >= 1: a tap with
-//    elev <= best * (t - 0.0101) * (1 - 2^-20) cannot raise best and needs
-//    neither its distance nor its division. t = 0 has dist = 0 and is always
-//    skipped by the reference.
+// Tap positions. cur = p + float32(dir*t) (dir.Scale(t,t,1,1) then Add) and
+// Go's int(cur) is in [0, W) exactly when -1 < cur < W; cur moves
+// monotonically in t, so the first tap outside the buffer (where the
+// reference returns) bounds the march, and is found by binary search unless
+// tap 99 is inside. For x >= 0 and a = float32(dX t):
+//  * a "regular" component (a an integer, or at least 2^-10 below the next
+//    integer for every t <= 99, which holds for all 8 directions) has
+//    int(RN(x + a)) = x + floor(a) for coordinates below 16384, since
+//    RN(x + a) cannot round up to the next integer;
+//  * a tiny negative component (-1 < a < 0: the cos of float32(Pi/2) and the
+//    sin of float32(Pi)) has int(RN(x - |a|)) = x while |a| is at most half
+//    the gap below x, else x - 1; |a| grows with t, so the switch happens at
+//    one tap t*, found by binary search.
+// So while cur >= 0, the depth index of tap t is the pixel's index plus a
+// per-(direction, t) offset from a table, plus a correction before t* for a
+// tiny component. Taps with cur < 0 (int truncates toward zero there) and
+// the last taps that do not fill a group of four take the float path.
+// Tap 1 always takes it: its distance may fall below 1 (diagonals).
 __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParams P) {
-    const uint32_t n = P.cnt->n_ao;
+    __shared__ __align__(16) int s_off[8][kAoTable];
+    __shared__ __align__(16) float s_tm[kAoTable];
     const int W = P.W, H = P.H;
+    for (int e = threadIdx.x; e < 8 * kAoTable; e += blockDim.x) {
+        const int k = e / kAoTable, q = e - k * kAoTable, t = q + 2;
+        int o = 0;
+        if (t < kAoTaps && k < P.n_dirs) {
+            const float tf = small_u2f((uint32_t)t);
+            const int fx = (int)floorf(__fmul_rn(c_ao_dir[0][k], tf));
+            const int fy = (int)floorf(__fmul_rn(c_ao_dir[1][k], tf));
+            o = fx - fy * W;
+        }
+        s_off[k][q] = o;
+    }
+    for (int q = threadIdx.x; q < kAoTable; q += blockDim.x) s_tm[q] = __fsub_rd(small_u2f((uint32_t)(q + 2)), 0.0101f);
+    __syncthreads();
+
+    const uint32_t n = P.cnt->n_ao;
     const float fW = (float)W, fH = (float)H;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const uint32_t i = P.list[j];
         const int r = (int)(i / (uint32_t)W);
         const int x = (int)i - r * W;
         const int y = H - 1 - r;
-        const float z = P.depth[i];
+        const float* p0 = P.depth + i;
+        const float z = *p0;
         const float pxf = small_u2f((uint32_t)x), pyf = small_u2f((uint32_t)y);
         float total = 0.0f;
+        bool nanpix = false;
         for (int k = 0; k < P.n_dirs; k++) {
             const float dX = c_ao_dir[0][k], dY = c_ao_dir[1][k];
-            // Taps 1 .. t_end-1 lie inside the buffer (monotone in t): find
-            // the first tap outside by binary search.
-            int lo = 1, hi = 100;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                const float tf = small_u2f((uint32_t)mid);
-                const float cx = __fadd_rn(pxf, __fmul_rn(dX, tf));
-                const float cy = __fadd_rn(pyf, __fmul_rn(dY, tf));
-                if (cx > -1.0f && cx < fW && cy > -1.0f && cy < fH)
-                    lo = mid + 1;
-                else
-                    hi = mid;
-            }
-            const int t_end = lo;
-            float best = 0.0f;
-            bool nanr = false;
-            for (int t0 = 1; t0 < t_end && !nanr; t0 += 4) {
-                const float tf0 = small_u2f((uint32_t)t0);
-                // skip bound for every tap of the group (smallest t gives the smallest bound)
-                const float thr = __fmul_rn(best, __fmul_rn(__fsub_rn(tf0, 0.0101f), 0.99999905f));
-                float el[4], cxs[4], cys[4];
-                bool cand = false;
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const float tf = __fadd_rn(tf0, (float)u);
-                    cxs[u] = __fadd_rn(pxf, __fmul_rn(dX, tf));
-                    cys[u] = __fadd_rn(pyf, __fmul_rn(dY, tf));
-                    const bool valid = t0 + u < t_end;
-                    const uint32_t ix = __float_as_uint(__fadd_rz(fmaxf(cxs[u], 0.0f), 8388608.0f)) - 0x4B000000u;
-                    const uint32_t iy = __float_as_uint(__fadd_rz(fmaxf(cys[u], 0.0f), 8388608.0f)) - 0x4B000000u;
-                    const size_t idx = valid ? (size_t)(H - 1 - (int)iy) * W + ix : (size_t)i;
-                    el[u] = __fsub_rn(__ldg(P.depth + idx), z);
-                    if (!valid) el[u] = -1.0f;
-                    cand = cand || !(el[u] <= thr);
-                }
-                if (cand) {
-#pragma unroll
-                    for (int u = 0; u < 4; u++) {
-                        if (!(el[u] <= thr) && !nanr) {
-                            const float d = ao_distance(pxf, pyf, cxs[u], cys[u]);
-                            if (d >= 1.0f) {
-                                if (isnan(el[u]))
-                                    nanr = true;
-                                else
-                                    best = fmaxf(best, __fdiv_rn(el[u], d));
-                            }
-                        }
+            int t_end = kAoTaps, t_fast = kAoTaps;
+            {
+                const float cx = __fadd_rn(pxf, __fmul_rn(dX, 99.0f)), cy = __fadd_rn(pyf, __fmul_rn(dY, 99.0f));
+                if (!(cx >= 0.0f && cx < fW && cy >= 0.0f && cy < fH)) {
+                    // first tap outside (-1, W) x (-1, H), then first tap with cur < 0
+                    int lo = 1, hi = kAoTaps;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        const float tf = small_u2f((uint32_t)mid);
+                        const float mx = __fadd_rn(pxf, __fmul_rn(dX, tf)), my = __fadd_rn(pyf, __fmul_rn(dY, tf));
+                        if (mx > -1.0f && mx < fW && my > -1.0f && my < fH)
+                            lo = mid + 1;
+                        else
+                            hi = mid;
                     }
+                    t_end = lo;
+                    lo = 1;
+                    hi = t_end;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        const float tf = small_u2f((uint32_t)mid);
+                        const float mx = __fadd_rn(pxf, __fmul_rn(dX, tf)), my = __fadd_rn(pyf, __fmul_rn(dY, tf));
+                        if (mx >= 0.0f && my >= 0.0f)
+                            lo = mid + 1;
+                        else
+                            hi = mid;
+                    }
+                    t_fast = lo;
                 }
             }
-            float ma;
-            if (nanr)
-                ma = __uint_as_float(0x7fc00000u);
-            else
-                ma = best > 0.0f ? atan_f32(best) : 0.0f;
+            if (!P.dir_fast[k]) t_fast = 1;
+            float best = 0.0f;
+            bool ok = true;
+            if (t_end > 1) ok = ao_tap_exact(1, pxf, pyf, dX, dY, W, H, P.depth, z, 0.0f, best);
+            int t = 2;
+            if (ok && t_fast > 2) {
+                const int n_groups = t_fast == kAoTaps ? kAoTable / 4 : (t_fast - 2) >> 2;
+                const int tiny = P.dir_tiny[k];
+                if (tiny) {
+                    // t*: first tap with |a| above half the gap below the coordinate
+                    const float cf = fabsf(tiny == 1 ? dX : dY);
+                    const uint32_t vb = __float_as_uint(tiny == 1 ? pxf : pyf);
+                    const float h = __uint_as_float(((vb >> 23) - ((vb & 0x7fffffu) ? 24u : 25u)) << 23);
+                    int lo = 1, hi = kAoTaps;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (__fmul_rn(cf, small_u2f((uint32_t)mid)) > h)
+                            hi = mid;
+                        else
+                            lo = mid + 1;
+                    }
+                    const float* pA = p0 + (tiny == 1 ? 1 : -W);
+                    ok = ao_fast_groups<true>(n_groups, s_off, s_tm, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
+                } else {
+                    ok = ao_fast_groups<false>(n_groups, s_off, s_tm, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
+                }
+                t = 2 + 4 * n_groups;
+            }
+            for (; ok && t < t_end; t++) ok = ao_tap_exact(t, pxf, pyf, dX, dY, W, H, P.depth, z, best, best);
+            if (!ok) {
+                nanpix = true;
+                break;
+            }
+            const float ma = best > 0.0f ? atan_f32(best) : 0.0f;
             total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));  // HalfPi - angle
         }
-        total = __fdiv_rn(total, 12.5663706143591729539f);  // (Pi/2)*8 as float32
-        total = __double2float_rn(go_pow((double)total, 10000.0));
+        const float T = nanpix ? __uint_as_float(0x7fc00000u) : __fdiv_rn(total, 12.5663706143591729539f);
         const uchar4 c = P.rgba[i];
-        uint32_t c0 = go_f2u8(__fmul_rn(total, small_u2f(c.x)));
-        uint32_t c1 = go_f2u8(__fmul_rn(total, small_u2f(c.y)));
-        uint32_t c2 = go_f2u8(__fmul_rn(total, small_u2f(c.z)));
+        uint3 o = ao_scale(T, c.x, c.y, c.z);
         if (P.gamma_on) {
-            c0 = P.gamma[c0];
-            c1 = P.gamma[c1];
-            c2 = P.gamma[c2];
+            o.x = P.gamma[o.x];
+            o.y = P.gamma[o.y];
+            o.z = P.gamma[o.z];
         }
-        P.rgba[i] = make_uchar4(c0, c1, c2, c.w);
+        P.rgba[i] = make_uchar4(o.x, o.y, o.z, c.w);
     }
+}
+
+__global__ void ao_probe_kernel(const float* x, float* atan_fast, float* atan_ref, const float* T, const uchar4* col,
+                                uchar4* o_fast, uchar4* o_ref, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    atan_fast[i] = atan_f32(x[i]);
+    atan_ref[i] = __double2float_rn(go_atan((double)x[i]));
+    const uchar4 c = col[i];
+    const uint3 a = ao_scale(T[i], c.x, c.y, c.z);
+    o_fast[i] = make_uchar4(a.x, a.y, a.z, c.w);
+    const float P = __double2float_rn(go_pow((double)T[i], 10000.0));
+    o_ref[i] = make_uchar4(go_f2u8(__fmul_rn(P, small_u2f(c.x))), go_f2u8(__fmul_rn(P, small_u2f(c.y))),
+                           go_f2u8(__fmul_rn(P, small_u2f(c.z))), c.w);
 }
 
 __global__ void fma_probe_kernel(const float* a, const float* b, const float* c, float* out, float* out_ref, int n) {
@@ -990,6 +1134,13 @@ int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream) {
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream) {
     if (n == 0) return 0;
     decode_shadow_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(smap, out, n);
+    return check(cudaGetLastError());
+}
+int launch_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const void* col, void* o_fast,
+                    void* o_ref, int n, void* stream) {
+    if (n <= 0) return 0;
+    ao_probe_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x, atan_fast, atan_ref, T, (const uchar4*)col,
+                                                                        (uchar4*)o_fast, (uchar4*)o_ref, n);
     return check(cudaGetLastError());
 }
 int launch_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n, void* stream) {

@@ -148,6 +148,8 @@ struct AoParams {
     const Counters* cnt;
     uchar4* rgba;
     uint8_t gamma[256];
+    int8_t dir_fast[8];  // 1: the tap offset table is exact for this frame size
+    int8_t dir_tiny[8];  // 1 / 2: the x / y component lies in (-1/99, 0)
 };
 
 }  // namespace prk
@@ -165,6 +167,8 @@ int launch_shade(const ShadeParams& p, void* stream);
 int launch_ao(const AoParams& p, int n_blocks, void* stream);
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
+int launch_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const void* col, void* o_fast,
+                    void* o_ref, int n, void* stream);
 int launch_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n,
                      void* stream);
 int sm_count();

@@ -42,3 +42,46 @@ def test_fma64f_matches_fp64(native_lib):
         assert rc == 0
         o, r = out.cpu().numpy(), ref.cpu().numpy()
         assert np.array_equal(o.view(np.uint32), r.view(np.uint32))
+
+
+def _ao_probe(native_lib, x, T, col):
+    import torch
+    n = len(x)
+    tx = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+    tT = torch.from_numpy(np.ascontiguousarray(T, np.float32)).cuda()
+    tc = torch.from_numpy(np.ascontiguousarray(col, np.uint8)).cuda()
+    af, ar = torch.empty_like(tx), torch.empty_like(tx)
+    of, orf = torch.empty_like(tc), torch.empty_like(tc)
+    rc = native_lib.pr_debug_ao_probe(tx.data_ptr(), af.data_ptr(), ar.data_ptr(), tT.data_ptr(), tc.data_ptr(),
+                                      of.data_ptr(), orf.data_ptr(), n)
+    assert rc == 0
+    return af.cpu().numpy(), ar.cpu().numpy(), of.cpu().numpy(), orf.cpu().numpy()
+
+
+def test_ao_atan_and_pow_shortcuts(native_lib):
+    """The AO kernel's float32 Atan (series with a certified rounding check)
+    and its float32 Pow(T, 10000) colour scaling give the float64
+    algorithm's bits on every input, including Pow values constructed to put
+    a channel's product on an integer."""
+    g = np.random.default_rng(11)
+    n = 1 << 20
+    x = np.concatenate([
+        np.exp(g.uniform(np.log(1e-6), np.log(1.5), n // 2)),
+        g.uniform(2e-4, 0.07, n // 2),
+    ]).astype(np.float32)
+    # T near 1 over the whole certified range, and T with Pow(T, 10000) * c
+    # within a few ulps of an integer m
+    d = np.concatenate([g.uniform(-1e-4, 7e-4, n // 2), np.exp(g.uniform(np.log(1e-9), np.log(7e-4), n // 4))])
+    c = g.integers(1, 256, n // 4)
+    m = np.minimum(g.integers(1, 256, n // 4), c)
+    Tm = np.power(m / c, 1e-4)
+    Tm = (Tm.astype(np.float32).view(np.int32) + g.integers(-3, 4, n // 4).astype(np.int32)).view(np.float32)
+    special = np.float32([1.0, np.nan, 0.0, 0.5, 0.9994, 1.00011])
+    T = np.concatenate([special, (1.0 - d[:n // 2 + n // 4 - len(special)]).astype(np.float32), Tm])
+    assert len(T) == n
+    col = g.integers(0, 256, (n, 4)).astype(np.uint8)
+    col[n // 2 + n // 4:, 0] = c
+    af, ar, of, orf = _ao_probe(native_lib, x, T, col)
+    assert np.array_equal(af.view(np.uint32), ar.view(np.uint32)), int((af != ar).sum())
+    bad = np.flatnonzero((of != orf).any(1))
+    assert len(bad) == 0, (len(bad), T[bad[:4]], col[bad[:4]], of[bad[:4]], orf[bad[:4]])

@@ -59,3 +59,41 @@ def test_ao_distance_lower_bound(oracle_lib):
             worst_hi = max(worst_hi, float(np.max(dist - t)))
     assert worst >= -0.002, worst
     assert worst_hi <= 0.002, worst_hi
+
+
+def _half_gap_below(x):
+    """Half the gap from integer x >= 1 to the float32 below it."""
+    e = np.floor(np.log2(x)).astype(np.int64)
+    pow2 = (x == np.exp2(e))
+    return np.where(pow2, np.exp2(e - 25.0), np.exp2(e - 24.0))
+
+
+def test_ao_tap_offsets(oracle_lib):
+    """The AO kernel's table of tap offsets: for each direction component
+    c and tap t <= 99, with a = float32(c t) and every pixel coordinate x up to
+    16483 whose tap stays at RN(x + a) >= 0, int(RN(x + a)) equals
+    x + floor(a), plus one while |a| <= half the gap below x when c is tiny
+    and negative. It also checks the classification the host makes (every
+    component regular or tiny-negative, so all 8 directions use the table)."""
+    cosv, sinv, n = (C.c_float * 8)(), (C.c_float * 8)(), C.c_int()
+    oracle_lib.orc_ao_directions(cosv, sinv, C.byref(n))
+    x = np.arange(0, 16484, dtype=F)
+    h_mx = 2.0 ** (13 - 24)  # half an ulp below 2^14 > 16483 + 100
+    n_tiny = 0
+    for k in range(n.value):
+        for c in (F(cosv[k]), F(sinv[k])):
+            tiny = c < 0 and F(-c * F(99)) < 1
+            n_tiny += tiny
+            for t in range(1, 100):
+                a = F(c * F(t))
+                if not tiny and a != np.floor(a):
+                    assert np.ceil(a) - a > h_mx, (k, t, a)
+                cx = (x + a).astype(F)
+                m = cx >= 0
+                ref = np.floor(cx[m]).astype(np.int64)
+                pred = x[m].astype(np.int64) + int(np.floor(a))
+                if tiny:
+                    xs = x[m].astype(np.float64)
+                    pred = pred + ((xs >= 1) & (abs(float(a)) <= _half_gap_below(np.maximum(xs, 1)))).astype(np.int64)
+                assert np.array_equal(ref, pred), (k, t, float(a), np.flatnonzero(ref != pred)[:5])
+    assert n_tiny == 2
