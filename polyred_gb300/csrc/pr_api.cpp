@@ -462,13 +462,13 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
             ap.H = H;
             ap.gamma_on = (f->flags & PR_FRAME_GAMMA) ? 1 : 0;
             ap.n_dirs = c->n_ao_dirs;
-            prh::ao_classify(c->ao_cos, c->ao_sin, c->n_ao_dirs, W, H, ap.dir_fast, ap.dir_tiny);
+            ap.ao_half_ulp = prh::ao_classify(c->ao_cos, c->ao_sin, c->n_ao_dirs, W, H, ap.dir_fast, ap.dir_tiny);
             ap.depth = c->depth_ao.p;
             ap.list = c->ao_list.p;
             ap.cnt = dcnt;
             ap.rgba = sp.rgba;
             std::memcpy(ap.gamma, sp.gamma, 256);
-            KTRY(prk::launch_ao(ap, c->n_sms * 8, st));
+            KTRY(prk::launch_ao(ap, st));
             launches += 1;
         }
         CUDA_TRY(cudaEventRecord(c->ev[4], st));

@@ -206,7 +206,7 @@ void ao_directions(float cosv[8], float sinv[8], int* n) {
     *n = k;
 }
 
-void ao_classify(const float cosv[8], const float sinv[8], int n, int W, int H, int8_t fast[8], int8_t tiny[8]) {
+float ao_classify(const float cosv[8], const float sinv[8], int n, int W, int H, int8_t fast[8], int8_t tiny[8]) {
     // Tap coordinates RN(x + a) stay below M = max(W, H) + 100 < 2^(E+1), where
     // half an ulp is at most 2^(E-24). A component whose a = RN(c t) is, for
     // every t <= 99, an integer or more than that below the next integer never
@@ -238,6 +238,7 @@ void ao_classify(const float cosv[8], const float sinv[8], int n, int W, int H, 
         fast[k] = ok ? 1 : 0;
         if (!ok) tiny[k] = 0;
     }
+    return h;
 }
 
 }  // namespace prh

@@ -24,6 +24,8 @@ void gamma_table(uint8_t out[256]);                      // shader/gamma.go:13-1
 void ao_directions(float cosv[8], float sinv[8], int* n); // material/ao.go:28
 // Which AO directions may use the device's tap offset table on a W x H frame
 // (fast[k]), and which component is tiny and negative (tiny[k]: 0, 1 = x, 2 = y).
-void ao_classify(const float cosv[8], const float sinv[8], int n, int W, int H, int8_t fast[8], int8_t tiny[8]);
+// Returns half an ulp of float32 at max(W, H) + 100, which bounds the
+// rounding of every tap coordinate.
+float ao_classify(const float cosv[8], const float sinv[8], int n, int W, int H, int8_t fast[8], int8_t tiny[8]);
 
 }  // namespace prh

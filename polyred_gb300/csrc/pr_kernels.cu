@@ -814,6 +814,7 @@ __constant__ float c_ao_dir[2][8];
 constexpr int kAoTaps = 100;     // t = 0 .. 99 (material/ao.go:44)
 constexpr int kAoTable = 100;    // tap offsets for t = 2 .. 101 (t >= 100: padding, offset 0)
 constexpr float kAoSkip = 1.0f - 0x1p-20f;
+constexpr int kAoThreads = 256;
 
 // distance of material/ao.go:52, p.Sub(cur).Len() with z = w = 0
 PR_DEV float ao_distance(float pxf, float pyf, float cx, float cy) {
@@ -849,16 +850,18 @@ PR_DEV bool ao_tap_exact(int t, float pxf, float pyf, float dX, float dY, int W,
     return true;
 }
 
-// maxElevationAngle's march for taps 2 .. 101 in groups of four, from a
-// shared table of index offsets (see ao_kernel). Taps whose elevation passes
-// the skip test are candidates; a candidate's ratio is first approximated
-// (f32 distance and rsqrtf, relative error below 1e-6, taken as 8e-6) and
-// kept as the one pending tap; exact ratios are computed only when two
-// candidates' intervals overlap and, once, for the final pending tap. best is
-// exact throughout, lb <= the largest exact ratio seen so far.
+// maxElevationAngle's march for taps 2 .. 101 in groups of four, from shared
+// tables of index offsets and of bounds on 1/dist (see ao_kernel): the exact
+// ratio RN(elev/dist) of a tap lies in [RD(elev rlo), RU(elev rhi)]. A tap
+// whose upper bound does not exceed lb cannot raise the maximum; the others
+// are candidates, of which one is held pending by its interval. Exact ratios
+// are computed only when a new candidate's interval overlaps the pending one
+// and, once, for the final pending tap. best is exact throughout and lb <= the
+// largest exact ratio seen so far.
 template <bool TINY>
-PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const float* s_tm, int k, const float* p0,
-                           const float* pA, int tstar, float z, float pxf, float pyf, float dX, float dY, float& best) {
+PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const float (*s_rlo)[kAoTable],
+                           const float (*s_rhi)[kAoTable], int k, const float* p0, const float* pA, int tstar, float z,
+                           float pxf, float pyf, float dX, float dY, float& best) {
     float lb = best;
     int pt = 0;
     float pel = 0.0f, phi = 0.0f;
@@ -866,51 +869,49 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
     for (int g = 0; g < n_groups; g++) {
         const int t0 = 4 * g + 2;
         const int4 o = *reinterpret_cast<const int4*>(&s_off[k][4 * g]);
-        const float4 tm = *reinterpret_cast<const float4*>(&s_tm[4 * g]);
-        const float lbs = __fmul_rd(lb, kAoSkip);
+        const float4 rh = *reinterpret_cast<const float4*>(&s_rhi[k][4 * g]);
         const float* q0 = (TINY && t0 < tstar) ? pA : p0;
         const float* q1 = (TINY && t0 + 1 < tstar) ? pA : p0;
         const float* q2 = (TINY && t0 + 2 < tstar) ? pA : p0;
         const float* q3 = (TINY && t0 + 3 < tstar) ? pA : p0;
-        float el[4];
+        float el[4], hi[4];
         el[0] = __fsub_rn(__ldg(q0 + o.x), z);
         el[1] = __fsub_rn(__ldg(q1 + o.y), z);
         el[2] = __fsub_rn(__ldg(q2 + o.z), z);
         el[3] = __fsub_rn(__ldg(q3 + o.w), z);
-        const bool c0 = !(el[0] <= __fmul_rn(lbs, tm.x));
-        const bool c1 = !(el[1] <= __fmul_rn(lbs, tm.y));
-        const bool c2 = !(el[2] <= __fmul_rn(lbs, tm.z));
-        const bool c3 = !(el[3] <= __fmul_rn(lbs, tm.w));
+        hi[0] = __fmul_ru(el[0], rh.x);
+        hi[1] = __fmul_ru(el[1], rh.y);
+        hi[2] = __fmul_ru(el[2], rh.z);
+        hi[3] = __fmul_ru(el[3], rh.w);
+        const bool c0 = !(hi[0] <= lb), c1 = !(hi[1] <= lb), c2 = !(hi[2] <= lb), c3 = !(hi[3] <= lb);
         if (c0 | c1 | c2 | c3) {
+            const float4 rl = *reinterpret_cast<const float4*>(&s_rlo[k][4 * g]);
+            const float lo[4] = {rl.x, rl.y, rl.z, rl.w};
             const bool cu[4] = {c0, c1, c2, c3};
+            // Branch-free: each candidate becomes the pending tap; a pending
+            // tap it overlaps is recorded and settled after the group (rare).
+            int st[4];
+            float sel[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                if (!cu[u]) continue;
-                const float e = el[u];
-                if (isnan(e)) {
-                    nan_seen = true;
-                    continue;
-                }
-                const int t = t0 + u;
-                const float tf = small_u2f((uint32_t)t);
-                const float cx = __fadd_rn(pxf, __fmul_rn(dX, tf)), cy = __fadd_rn(pyf, __fmul_rn(dY, tf));
-                const float ddx = __fsub_rn(pxf, cx), ddy = __fsub_rn(pyf, cy);
-                const float r = __fmul_rn(e, rsqrtf(__fmaf_rn(ddx, ddx, __fmul_rn(ddy, ddy))));
-                if (!(r >= 0x1p-100f)) {  // outside the relative error bound's range: exact now
-                    best = fmaxf(best, ao_exact_ratio(t, e, pxf, pyf, dX, dY));
-                    lb = fmaxf(lb, best);
-                    continue;
-                }
-                const float rlo = __fmul_rd(r, 0.999992f), rhi = __fmul_ru(r, 1.000008f);
-                if (rhi <= lb) continue;  // cannot exceed what is already held
-                if (pt != 0 && !(rlo >= phi))  // overlaps the pending tap: settle it
-                    best = fmaxf(best, ao_exact_ratio(pt, pel, pxf, pyf, dX, dY));
-                pt = t;
-                pel = e;
-                phi = rhi;
-                lb = fmaxf(best, rlo);
+                nan_seen |= isnan(el[u]);
+                const bool take = cu[u] & !isnan(el[u]);
+                const float rlo = __fmul_rd(el[u], lo[u]);
+                const bool ov = take & (pt != 0) & !(rlo >= phi);
+                st[u] = ov ? pt : 0;
+                sel[u] = pel;
+                pt = take ? t0 + u : pt;
+                pel = take ? el[u] : pel;
+                phi = take ? hi[u] : phi;
+                lb = take ? fmaxf(lb, rlo) : lb;
             }
             if (nan_seen) return false;
+            if ((st[0] | st[1] | st[2] | st[3]) != 0) {
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (st[u]) best = fmaxf(best, ao_exact_ratio(st[u], sel[u], pxf, pyf, dX, dY));
+                lb = fmaxf(lb, best);
+            }
         }
     }
     if (pt != 0) best = fmaxf(best, ao_exact_ratio(pt, pel, pxf, pyf, dX, dY));
@@ -942,25 +943,34 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
 // tiny component. Taps with cur < 0 (int truncates toward zero there) and
 // the last taps that do not fill a group of four take the float path.
 // Tap 1 always takes it: its distance may fall below 1 (diagonals).
-__global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParams P) {
+__global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant__ AoParams P) {
     __shared__ __align__(16) int s_off[8][kAoTable];
-    __shared__ __align__(16) float s_tm[kAoTable];
+    __shared__ __align__(16) float s_rlo[8][kAoTable];
+    __shared__ __align__(16) float s_rhi[8][kAoTable];
+    const uint32_t n = P.cnt->n_ao;
+    if (blockIdx.x * blockDim.x >= n) return;  // whole block: no pixel of the list
     const int W = P.W, H = P.H;
     for (int e = threadIdx.x; e < 8 * kAoTable; e += blockDim.x) {
         const int k = e / kAoTable, q = e - k * kAoTable, t = q + 2;
         int o = 0;
+        float rlo = 0.0f, rhi = 0.0f;
         if (t < kAoTaps && k < P.n_dirs) {
             const float tf = small_u2f((uint32_t)t);
-            const int fx = (int)floorf(__fmul_rn(c_ao_dir[0][k], tf));
-            const int fy = (int)floorf(__fmul_rn(c_ao_dir[1][k], tf));
-            o = fx - fy * W;
+            const float ax = __fmul_rn(c_ao_dir[0][k], tf), ay = __fmul_rn(c_ao_dir[1][k], tf);
+            o = (int)floorf(ax) - (int)floorf(ay) * W;
+            // |dist - |(ax, ay)|| <= sqrt(2) (h + 2^-18) + 2.5e-7 |(ax, ay)|: h bounds the rounding of
+            // cur = RN(p + a), 2^-18 that of p - cur, the rest the float32 steps of both distances
+            const float d0 = __fsqrt_rn(__fmaf_rn(ax, ax, __fmul_rn(ay, ay)));
+            const float dl = __fadd_ru(__fmul_ru(1.5f, __fadd_ru(P.ao_half_ulp, 4e-6f)), __fmul_ru(d0, 4e-7f));
+            rlo = __frcp_rd(__fadd_ru(d0, dl));
+            rhi = __frcp_ru(__fsub_rd(d0, dl));
         }
         s_off[k][q] = o;
+        s_rlo[k][q] = rlo;
+        s_rhi[k][q] = rhi;
     }
-    for (int q = threadIdx.x; q < kAoTable; q += blockDim.x) s_tm[q] = __fsub_rd(small_u2f((uint32_t)(q + 2)), 0.0101f);
     __syncthreads();
 
-    const uint32_t n = P.cnt->n_ao;
     const float fW = (float)W, fH = (float)H;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const uint32_t i = P.list[j];
@@ -1004,7 +1014,8 @@ __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParam
                     t_fast = lo;
                 }
             }
-            if (!P.dir_fast[k]) t_fast = 1;
+            // the padding taps 100, 101 read the pixel itself: elev 0 needs a finite depth
+            if (!P.dir_fast[k] || !isfinite(z)) t_fast = 1;
             float best = 0.0f;
             bool ok = true;
             if (t_end > 1) ok = ao_tap_exact(1, pxf, pyf, dX, dY, W, H, P.depth, z, 0.0f, best);
@@ -1026,9 +1037,9 @@ __global__ void __launch_bounds__(256) ao_kernel(const __grid_constant__ AoParam
                             lo = mid + 1;
                     }
                     const float* pA = p0 + (tiny == 1 ? 1 : -W);
-                    ok = ao_fast_groups<true>(n_groups, s_off, s_tm, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
+                    ok = ao_fast_groups<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
                 } else {
-                    ok = ao_fast_groups<false>(n_groups, s_off, s_tm, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
+                    ok = ao_fast_groups<false>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
                 }
                 t = 2 + 4 * n_groups;
             }
@@ -1117,8 +1128,13 @@ int launch_shade(const ShadeParams& p, void* stream) {
     shade_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
     return check(cudaGetLastError());
 }
-int launch_ao(const AoParams& p, int n_blocks, void* stream) {
-    ao_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(p);
+int launch_ao(const AoParams& p, void* stream) {
+    // One pixel per thread for the largest possible list (every pixel): the
+    // block scheduler balances the uneven per-pixel work; blocks past the
+    // list's length exit at once.
+    const size_t n = (size_t)p.W * p.H;
+    if (n == 0) return 0;
+    ao_kernel<<<(unsigned)((n + kAoThreads - 1) / kAoThreads), kAoThreads, 0, (cudaStream_t)stream>>>(p);
     return check(cudaGetLastError());
 }
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream) {

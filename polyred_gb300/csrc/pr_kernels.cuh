@@ -150,6 +150,7 @@ struct AoParams {
     uint8_t gamma[256];
     int8_t dir_fast[8];  // 1: the tap offset table is exact for this frame size
     int8_t dir_tiny[8];  // 1 / 2: the x / y component lies in (-1/99, 0)
+    float ao_half_ulp;   // half an ulp of float32 at max(W, H) + 100
 };
 
 }  // namespace prk
@@ -164,7 +165,7 @@ int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t*
 int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,
                               void* stream);
 int launch_shade(const ShadeParams& p, void* stream);
-int launch_ao(const AoParams& p, int n_blocks, void* stream);
+int launch_ao(const AoParams& p, void* stream);
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
 int launch_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const void* col, void* o_fast,
