@@ -295,6 +295,64 @@ typedef struct pr_depth_map_desc {
 
 int pr_depth_map_noalloc(const pr_depth_map_desc* desc);
 
+/* ---- differentiable deferred shading --------------------------------------
+ * No counterpart in the reference (which has no gradients): an adjoint of
+ * the deferred-shading pass, shade + FragmentShader (render/raster.go:320-356,
+ * shader/blinn_cpu.go:24-106), with visibility held fixed.
+ *
+ * pr_diff_forward renders a frame exactly as pr_render does (shadow maps,
+ * raster, G-buffer, AO) and, from it, a float "radiance" image and a
+ * per-pixel differentiation G-buffer (PR_DGB_FLOATS floats a pixel: the
+ * triangle, its material, the screen barycentric weights of the pixel centre
+ * in the input triangle, the world position, the face normal and the fixed
+ * factor w_shadow * w_ao). Radiance, per pixel and channel c:
+ *   material pixels: fac * clamp(La_c + kd_c Ld_c + ks_c Ls_c, 0, 255), the
+ *     pre-Round value of FragmentShader with kd/ks = Diffuse/255,
+ *     Specular/255 as floats and the interpolated normal n = unit(sum_k b_k N_k)
+ *     (N_k = NormalMatrix * vertex normal), or face normal when flat;
+ *     fac = 0.5^visibles (shadows) * float32(Pow(T, 10000)) (AO);
+ *   material-less pixels: 255 * sum_k p_k C_k, the perspective-correct
+ *     interpolation of the vertex colours C_k (in [0,1]);
+ *   background: the background colour.
+ * pr_diff_backward takes dL/d(radiance) and that G-buffer, recomputes every
+ * interpolated attribute and per-light term from it (nothing per light is
+ * stored), and returns dL/d of: vertex colours and normals, kd, ks,
+ * shininess, light positions and intensities, ambient intensities. */
+#define PR_DGB_FLOATS 16
+
+typedef struct pr_diff_params {
+    uint32_t size;
+    uint32_t n_materials;        /* entries of kd/ks/shininess (= the scene's) */
+    const float* vertex_color;   /* DEVICE [n_tris][3][4] RGBA in [0,1]; NULL: scene RGBA8 / 255 */
+    const float* vertex_normal;  /* DEVICE [n_tris][3][4] object-space normals; NULL: the scene's */
+    const float* kd;             /* HOST [n_materials][3] in [0,1]; NULL: scene Diffuse / 255 */
+    const float* ks;             /* HOST [n_materials][3]; NULL: scene Specular / 255 */
+    const float* shininess;      /* HOST [n_materials]; NULL: the scene's */
+} pr_diff_params;
+
+typedef struct pr_diff_grads {
+    uint32_t size;
+    uint32_t reserved;
+    float*  vertex_color;        /* DEVICE [n_tris][3][4], overwritten; NULL: not wanted */
+    float*  vertex_normal;       /* DEVICE [n_tris][3][4] (w = 0), overwritten; NULL: not wanted */
+    double* kd;                  /* HOST [n_materials][3] */
+    double* ks;                  /* HOST [n_materials][3] */
+    double* shininess;           /* HOST [n_materials] */
+    double* light_pos;           /* HOST [n_lights][3] (0 for directional lights) */
+    double* light_intensity;     /* HOST [n_lights] */
+    double* ambient;             /* HOST [n_ambient] */
+} pr_diff_grads;
+
+/* radiance: DEVICE [H][W][4] (alpha = the frame's alpha); gbuf: DEVICE
+ * [H][W][PR_DGB_FLOATS]; out: optional further outputs (device pointers,
+ * PR_OUT_DEVICE_PTRS), as pr_render. Rows top-down. Returns when done. */
+int pr_diff_forward(void* ctx, const pr_frame_desc* frame, const pr_diff_params* params, float* radiance,
+                    float* gbuf, pr_outputs* out);
+/* frame and params as given to the pr_diff_forward that produced gbuf;
+ * grad_radiance: DEVICE [H][W][4] (alpha ignored). Returns when done. */
+int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params* params, const float* gbuf,
+                     const float* grad_radiance, pr_diff_grads* grads);
+
 #ifdef __cplusplus
 }
 #endif

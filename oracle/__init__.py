@@ -14,7 +14,7 @@ _lib = None
 
 
 def build(force=False):
-    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "oracle.h", "gomath.h", "vecmath.h")]
+    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "adjoint.cpp", "oracle.h", "gomath.h", "vecmath.h")]
     if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in srcs):
         subprocess.run(["sh", os.path.join(HERE, "build.sh")], check=True)
     return LIB
@@ -60,3 +60,115 @@ def render(scene_desc, frame_desc, outputs_desc, shadow_state=None, threads=1):
     rc = lib.orc_render(C.byref(scene_desc), C.byref(frame_desc), ptr, int(threads), C.byref(outputs_desc), None)
     if rc != 0:
         raise RuntimeError(f"oracle render failed: {rc}")
+
+
+# ---- FP64 differentiable shading (adjoint.cpp) ----------------------------
+
+class orc_diff_in(C.Structure):
+    _fields_ = [
+        ("W", C.c_int32), ("H", C.c_int32),
+        ("gbuf", C.c_void_p),
+        ("n_tris", C.c_uint32), ("n_objects", C.c_uint32),
+        ("vcol", C.c_void_p), ("vnor", C.c_void_p),
+        ("obj_first", C.c_void_p), ("obj_normal", C.c_void_p),
+        ("n_mats", C.c_int32), ("n_lights", C.c_int32),
+        ("kd", C.c_void_p), ("ks", C.c_void_p), ("shin", C.c_void_p), ("tex", C.c_void_p),
+        ("ltype", C.c_void_p), ("lpos", C.c_void_p), ("ldir", C.c_void_p), ("lint", C.c_void_p),
+        ("lcol", C.c_void_p),
+        ("n_amb", C.c_int32), ("only_tri", C.c_int32),
+        ("amb", C.c_void_p),
+        ("cam", C.c_double * 3), ("bg", C.c_double * 4),
+        ("only_mat", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class orc_diff_out(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("vcol", "vnor", "kd", "ks", "shin", "lpos", "lint", "amb")]
+
+
+def normal_matrices(flat):
+    """Per-object (Model^-1)^T as the reference's Mat4.Inv / T compute them."""
+    import numpy as np
+    lib = load()
+    out = np.zeros((max(flat.n_objects, 1), 16), np.float32)
+    for o in range(flat.n_objects):
+        m = np.array(flat.objects[o].model[:], np.float32)
+        inv = np.zeros(16, np.float32)
+        if lib.orc_mat4_inv(m.ctypes.data, inv.ctypes.data) != 0:
+            raise ValueError(f"object {o}: singular model matrix")
+        out[o] = inv.reshape(4, 4).T.reshape(16)
+    return out
+
+
+class DiffInputs:
+    """orc_diff_in over numpy arrays (parameters in float64) it keeps alive."""
+
+    def __init__(self, flat, gbuf, params, frame, normal_mats, only_tri=-1, only_mat=-1):
+        import numpy as np
+        f = frame
+        H, W = int(f.height), int(f.width)
+        self.a = {}
+        k = self.a
+        k["gbuf"] = np.ascontiguousarray(gbuf, np.float32).reshape(H * W, 16)
+        for name in ("vertex_color", "vertex_normal", "kd", "ks", "shininess", "light_pos", "light_intensity",
+                     "ambient"):
+            k[name] = np.ascontiguousarray(params[name], np.float64)
+        first = np.array([flat.objects[o].first_tri for o in range(flat.n_objects)], np.uint32)
+        k["first"] = first
+        k["nmat"] = np.ascontiguousarray(normal_mats, np.float32)
+        k["tex"] = np.array([list(flat.materials[m].texture) for m in range(flat.n_materials)] or [[0] * 4], np.uint8)
+        nl = int(f.n_lights)
+        k["ltype"] = np.array([f.lights[l].type for l in range(nl)] or [0], np.int32)
+        k["ldir"] = np.array([list(f.lights[l].dir) for l in range(nl)] or [[0] * 3], np.float32)
+        k["lcol"] = np.array([list(f.lights[l].color) for l in range(nl)] or [[0] * 4], np.uint8)
+        s = orc_diff_in()
+        s.W, s.H = W, H
+        s.gbuf = k["gbuf"].ctypes.data
+        s.n_tris, s.n_objects = flat.n_tris, flat.n_objects
+        s.vcol, s.vnor = k["vertex_color"].ctypes.data, k["vertex_normal"].ctypes.data
+        s.obj_first, s.obj_normal = first.ctypes.data, k["nmat"].ctypes.data
+        s.n_mats, s.n_lights = flat.n_materials, nl
+        s.kd, s.ks, s.shin, s.tex = (k["kd"].ctypes.data, k["ks"].ctypes.data, k["shininess"].ctypes.data,
+                                     k["tex"].ctypes.data)
+        s.ltype, s.lpos, s.ldir = k["ltype"].ctypes.data, k["light_pos"].ctypes.data, k["ldir"].ctypes.data
+        s.lint, s.lcol = k["light_intensity"].ctypes.data, k["lcol"].ctypes.data
+        s.n_amb = int(f.n_ambient)
+        s.amb = k["ambient"].ctypes.data
+        s.cam[:] = [float(c) for c in f.cam_pos]
+        s.bg[:] = [float(c) for c in f.background]
+        s.only_tri, s.only_mat = only_tri, only_mat
+        self.s = s
+
+    def param(self, name):
+        """The float64 parameter array (edit in place for finite differences)."""
+        return self.a[name]
+
+
+def diff_forward64(inp, target=None, want_radiance=True):
+    """(loss, radiance[H, W, 4]) in float64."""
+    import numpy as np
+    lib = load()
+    lib.orc_diff_forward64.restype = C.c_double
+    lib.orc_diff_forward64.argtypes = [C.POINTER(orc_diff_in), C.c_void_p, C.c_void_p]
+    rad = np.zeros((inp.s.H, inp.s.W, 4), np.float64) if want_radiance else None
+    tgt = None if target is None else np.ascontiguousarray(target, np.float32)
+    loss = lib.orc_diff_forward64(C.byref(inp.s), None if rad is None else rad.ctypes.data,
+                                  None if tgt is None else tgt.ctypes.data)
+    return loss, rad
+
+
+def diff_backward64(inp, grad):
+    """Gradients of sum(grad * radiance) in float64, shaped like the parameters."""
+    import numpy as np
+    lib = load()
+    lib.orc_diff_backward64.restype = None
+    lib.orc_diff_backward64.argtypes = [C.POINTER(orc_diff_in), C.c_void_p, C.POINTER(orc_diff_out)]
+    g = np.ascontiguousarray(grad, np.float64)
+    names = {"vcol": "vertex_color", "vnor": "vertex_normal", "kd": "kd", "ks": "ks", "shin": "shininess",
+             "lpos": "light_pos", "lint": "light_intensity", "amb": "ambient"}
+    res = {v: np.zeros_like(inp.a[v]) for v in names.values()}
+    o = orc_diff_out()
+    for k, v in names.items():
+        setattr(o, k, res[v].ctypes.data)
+    lib.orc_diff_backward64(C.byref(inp.s), g.ctypes.data, C.byref(o))
+    return res

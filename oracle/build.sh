@@ -6,4 +6,4 @@ set -e
 here=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$here/build"
 ${CXX:-g++} -O2 -std=c++17 -ffp-contract=off -fno-fast-math -fPIC -shared -pthread \
-    -o "$here/build/liboracle.so" "$here/oracle.cpp"
+    -o "$here/build/liboracle.so" "$here/oracle.cpp" "$here/adjoint.cpp"

@@ -102,6 +102,39 @@ class pr_depth_map_desc(C.Structure):
 # Every entry point include/polyred_cuda.h declares: (name, restype, argtypes).
 VP = C.c_void_p
 FP = C.POINTER(C.c_float)
+PR_DGB_FLOATS = 16
+# differentiation G-buffer pixel flags (float 2 of a pixel)
+DGB_LIT, DGB_FLAT, DGB_CONST, DGB_UNLIT = 1, 2, 4, 8
+DP = C.POINTER(C.c_double)
+
+
+class pr_diff_params(C.Structure):
+    _fields_ = [
+        ("size", C.c_uint32),
+        ("n_materials", C.c_uint32),
+        ("vertex_color", VP),
+        ("vertex_normal", VP),
+        ("kd", FP),
+        ("ks", FP),
+        ("shininess", FP),
+    ]
+
+
+class pr_diff_grads(C.Structure):
+    _fields_ = [
+        ("size", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("vertex_color", VP),
+        ("vertex_normal", VP),
+        ("kd", DP),
+        ("ks", DP),
+        ("shininess", DP),
+        ("light_pos", DP),
+        ("light_intensity", DP),
+        ("ambient", DP),
+    ]
+
+
 ENTRY_POINTS = [
     ("pr_abi_version", C.c_int, []),
     ("pr_error_string", C.c_char_p, [C.c_int]),
@@ -122,6 +155,10 @@ ENTRY_POINTS = [
     ("pr_mat4_inv", C.c_int, [FP, FP]),
     ("pr_shadow_camera", C.c_int, [FP, FP, FP, FP, FP, FP]),
     ("pr_depth_map_noalloc", C.c_int, [C.POINTER(pr_depth_map_desc)]),
+    ("pr_diff_forward", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_diff_params), VP, VP,
+                                  C.POINTER(pr_outputs)]),
+    ("pr_diff_backward", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_diff_params), VP, VP,
+                                   C.POINTER(pr_diff_grads)]),
 ]
 
 

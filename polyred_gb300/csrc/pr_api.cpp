@@ -118,6 +118,11 @@ struct Ctx {
     DevBuf<float> o_depth, o_shadow;
     DevBuf<float4> o_nor, o_fnor, o_wpos, o_uvd;
     DevBuf<int32_t> o_mat;
+    // differentiable shading
+    DevBuf<float> tri_scr;                 // [n_tris][12]
+    DevBuf<float> d_kd, d_ks, d_shin;      // [n_mats][3], [n_mats][3], [n_mats]
+    DevBuf<float4> d_vcol;                 // scene colours / 255, when the caller gives none
+    DevBuf<double> d_acc;
     pr_stats stats{};
     cudaEvent_t ev[6] = {};
     int n_sms = 1;
@@ -244,7 +249,12 @@ void collect_stats(Ctx* c) {
     c->stats.n_ao_pixels = c->h_cnt[0].n_ao;
 }
 
-int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
+// Extra outputs of a differentiable forward frame.
+struct DiffHooks {
+    float4* dgb;  // [H][W][4] differentiation G-buffer
+};
+
+int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, const DiffHooks* dh = nullptr) {
     int rc = validate_frame(c, f);
     if (rc) return rc;
     if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
@@ -281,12 +291,8 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         if (!c->smap_valid || c->SW != SW || c->SH != SH || c->n_slights != NL) {
             size_t n = (size_t)SW * SH * std::max(NL, 1);
             if ((rc = c->smap.ensure(n))) return rc;
-            // key of +0.0f is 0x80000000: fill bytes 00 00 00 80
-            std::vector<uint32_t> zero_keys((size_t)SW * SH, 0x80000000u);
-            for (int l = 0; l < std::max(NL, 1); l++)
-                CUDA_TRY(cudaMemcpyAsync(c->smap.p + (size_t)SW * SH * l, zero_keys.data(), zero_keys.size() * 4,
-                                         cudaMemcpyHostToDevice, st));
-            CUDA_TRY(cudaStreamSynchronize(st));
+            // the orderable key of +0.0f is 0x80000000
+            KTRY(prk::launch_fill_u32(c->smap.p, 0x80000000u, n, st));
             c->SW = SW;
             c->SH = SH;
             c->n_slights = NL;
@@ -365,6 +371,10 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         mp.cap_tasks = c->cap_tasks;
         mp.first_rec = c->first_rec.p;
         mp.cnt = dcnt;
+        if (dh) {
+            if ((rc = c->tri_scr.ensure((size_t)std::max<uint32_t>(c->n_tris, 1) * 12))) return rc;
+            mp.tri_scr = c->tri_scr.p;
+        }
         CUDA_TRY(cudaMemsetAsync(c->keys.p, 0, npx * 8, st));
         CUDA_TRY(cudaMemsetAsync(c->nanseq.p, 0xff, npx * 4, st));
         CUDA_TRY(cudaMemsetAsync(c->beaten.p, 0, npx * 4, st));
@@ -430,6 +440,10 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
         prh::gamma_table(sp.gamma);
         sp.ao_list = c->ao_list.p;
         sp.cnt_w = dcnt;
+        if (dh) {
+            sp.tri_scr = c->tri_scr.p;
+            sp.dgb = dh->dgb;
+        }
         // outputs: device pointers directly, or ctx staging buffers
         if (out_dev) {
             sp.rgba = (uchar4*)out->rgba;
@@ -467,6 +481,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync) {
             ap.list = c->ao_list.p;
             ap.cnt = dcnt;
             ap.rgba = sp.rgba;
+            ap.dgb = dh ? dh->dgb : nullptr;
             std::memcpy(ap.gamma, sp.gamma, 256);
             KTRY(prk::launch_ao(ap, st));
             launches += 1;
@@ -601,6 +616,8 @@ int pr_destroy(void* ctx) {
     c->smap.release(); c->lastnan.release(); c->cnt.release();
     c->o_rgba.release(); c->o_vcol.release(); c->o_tri.release(); c->o_depth.release(); c->o_shadow.release();
     c->o_nor.release(); c->o_fnor.release(); c->o_wpos.release(); c->o_uvd.release(); c->o_mat.release();
+    c->tri_scr.release(); c->d_kd.release(); c->d_ks.release(); c->d_shin.release(); c->d_vcol.release();
+    c->d_acc.release();
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
     for (auto& ev : c->ev)
         if (ev) cudaEventDestroy(ev);
@@ -754,6 +771,169 @@ int pr_shadow_camera(const float light_pos[3], const float scene_center[3], cons
         return fail(PR_ERR_SINGULAR, "camera matrix is singular");
     std::memcpy(out_view, v.m, 64);
     std::memcpy(out_proj, p.m, 64);
+    return PR_OK;
+}
+
+// ---- differentiable shading ----
+
+namespace {
+
+// Device parameters of a differentiable call: the caller's or the scene's.
+int diff_setup(Ctx* c, const pr_frame_desc* f, const pr_diff_params* prm, prk::DiffParamsK& K) {
+    int rc;
+    const uint32_t nm = (uint32_t)c->materials.size();
+    if (prm && prm->size < sizeof(pr_diff_params)) return fail(PR_ERR_INVALID_ARG, "params->size too small");
+    if (prm && prm->n_materials != nm && (prm->kd || prm->ks || prm->shininess))
+        return fail(PR_ERR_INVALID_ARG, "params->n_materials (%u) differs from the scene's (%u)", prm->n_materials, nm);
+    if (nm > (uint32_t)prk::kDiffMaxMats) return fail(PR_ERR_UNSUPPORTED, "more than %d materials", prk::kDiffMaxMats);
+    if (f->n_lights > (uint32_t)prk::kMaxLights || f->n_ambient > (uint32_t)prk::kMaxAmbient)
+        return fail(PR_ERR_INVALID_ARG, "too many lights");
+    std::vector<float> kd(3 * std::max<uint32_t>(nm, 1)), ks(kd.size()), sh(std::max<uint32_t>(nm, 1));
+    for (uint32_t m = 0; m < nm; m++) {
+        for (int k = 0; k < 3; k++) {
+            kd[3 * m + k] = (prm && prm->kd) ? prm->kd[3 * m + k] : c->materials[m].diffuse[k] / 255.0f;
+            ks[3 * m + k] = (prm && prm->ks) ? prm->ks[3 * m + k] : c->materials[m].specular[k] / 255.0f;
+        }
+        sh[m] = (prm && prm->shininess) ? prm->shininess[m] : c->materials[m].shininess;
+    }
+    cudaStream_t st = c->stream;
+    if ((rc = c->d_kd.ensure(kd.size())) || (rc = c->d_ks.ensure(ks.size())) || (rc = c->d_shin.ensure(sh.size())))
+        return rc;
+    CUDA_TRY(cudaMemcpyAsync(c->d_kd.p, kd.data(), kd.size() * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(c->d_ks.p, ks.data(), ks.size() * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(c->d_shin.p, sh.data(), sh.size() * 4, cudaMemcpyHostToDevice, st));
+    const size_t nv = (size_t)c->n_tris * 3;
+    const float4* vcol = prm ? (const float4*)prm->vertex_color : nullptr;
+    if (!vcol) {
+        if ((rc = c->d_vcol.ensure(std::max<size_t>(nv, 1)))) return rc;
+        KTRY(prk::launch_col_to_float(c->col.p, c->d_vcol.p, nv, st));
+        vcol = c->d_vcol.p;
+    }
+    K.W = f->width;
+    K.H = f->height;
+    K.vcol = vcol;
+    K.vnor = (prm && prm->vertex_normal) ? (const float4*)prm->vertex_normal : c->nor.p;
+    K.obj_first = c->obj_first.p;
+    K.n_objects = (uint32_t)c->objects.size();
+    K.obj_normal = c->obj_normal.p;
+    K.n_mats = (int)nm;
+    K.kd = c->d_kd.p;
+    K.ks = c->d_ks.p;
+    K.shin = c->d_shin.p;
+    K.mats = c->dmats.p;
+    K.n_lights = (int)f->n_lights;
+    K.n_ambient = (int)f->n_ambient;
+    for (uint32_t l = 0; l < f->n_lights; l++) {
+        const pr_light& L = f->lights[l];
+        prk::LightK& Q = K.lights[l];
+        Q.type = L.type;
+        Q.cast = L.cast_shadow ? 1 : 0;
+        for (int k = 0; k < 3; k++) {
+            Q.pos[k] = L.pos[k];
+            Q.dir[k] = L.dir[k];
+            Q.color[k] = (float)L.color[k];
+        }
+        Q.intensity = L.intensity;
+    }
+    for (uint32_t e = 0; e < f->n_ambient; e++) K.ambient[e] = f->ambient[e];
+    for (int k = 0; k < 3; k++) K.cam[k] = f->cam_pos[k];
+    for (int k = 0; k < 4; k++) K.bg[k] = (float)f->background[k];
+    return PR_OK;
+}
+
+}  // namespace
+
+int pr_diff_forward(void* ctx, const pr_frame_desc* frame, const pr_diff_params* params, float* radiance, float* gbuf,
+                    pr_outputs* out) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(PR_ERR_INVALID_ARG, "ctx is NULL");
+    if (!radiance || !gbuf) return fail(PR_ERR_INVALID_ARG, "radiance and gbuf are required");
+    if (out && (out->size < sizeof(pr_outputs) || !(out->flags & PR_OUT_DEVICE_PTRS)))
+        return fail(PR_ERR_INVALID_ARG, "out must hold device pointers (PR_OUT_DEVICE_PTRS)");
+    std::lock_guard<std::mutex> lk(c->mu);
+    int rc = validate_frame(c, frame);
+    if (rc) return rc;
+    if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
+    if ((rc = set_device(c))) return rc;
+    // the AO factors need the colour pass: render into ctx storage when the caller wants no image
+    pr_outputs o{};
+    if (out) o = *out;
+    o.size = sizeof(pr_outputs);
+    o.flags = PR_OUT_DEVICE_PTRS;
+    const size_t npx = (size_t)frame->width * frame->height;
+    if (!o.rgba) {
+        if ((rc = c->o_rgba.ensure(npx * 4))) return rc;
+        o.rgba = c->o_rgba.p;
+    }
+    DiffHooks dh{(float4*)gbuf};
+    rc = PR_ERR_OVERFLOW;
+    for (int attempt = 0; attempt < 4 && rc == PR_ERR_OVERFLOW; attempt++) {
+        rc = render_impl(c, frame, &o, true, &dh);
+        if (rc == PR_ERR_OVERFLOW) {
+            uint32_t need_rec = 0, need_tasks = 0;
+            for (int k = 0; k <= prk::kMaxLights; k++) {
+                need_rec = std::max(need_rec, c->h_cnt[k].need_rec);
+                need_tasks = std::max(need_tasks, c->h_cnt[k].need_tasks);
+            }
+            int r2 = ensure_work(c, need_rec + need_rec / 4, need_tasks + need_tasks / 4);
+            if (r2) return r2;
+        }
+    }
+    if (rc) return rc;
+    prk::DiffParamsK K{};
+    if ((rc = diff_setup(c, frame, params, K))) return rc;
+    K.dgb = (const float4*)gbuf;
+    K.radiance = (float4*)radiance;
+    KTRY(prk::launch_diff(K, false, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return PR_OK;
+}
+
+int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params* params, const float* gbuf,
+                     const float* grad_radiance, pr_diff_grads* grads) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(PR_ERR_INVALID_ARG, "ctx is NULL");
+    if (!gbuf || !grad_radiance || !grads) return fail(PR_ERR_INVALID_ARG, "gbuf, grad_radiance and grads are required");
+    if (grads->size < sizeof(pr_diff_grads)) return fail(PR_ERR_INVALID_ARG, "grads->size too small");
+    std::lock_guard<std::mutex> lk(c->mu);
+    int rc = validate_frame(c, frame);
+    if (rc) return rc;
+    if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
+    if ((rc = set_device(c))) return rc;
+    prk::DiffParamsK K{};
+    if ((rc = diff_setup(c, frame, params, K))) return rc;
+    cudaStream_t st = c->stream;
+    const size_t nv = (size_t)c->n_tris * 3;
+    if (grads->vertex_color) CUDA_TRY(cudaMemsetAsync(grads->vertex_color, 0, nv * 16, st));
+    if (grads->vertex_normal) CUDA_TRY(cudaMemsetAsync(grads->vertex_normal, 0, nv * 16, st));
+    const int nm = K.n_mats, nl = K.n_lights, na = K.n_ambient;
+    const size_t n_acc = (size_t)nm * 7 + (size_t)nl * 4 + na;
+    if ((rc = c->d_acc.ensure(std::max<size_t>(n_acc, 1)))) return rc;
+    CUDA_TRY(cudaMemsetAsync(c->d_acc.p, 0, std::max<size_t>(n_acc, 1) * 8, st));
+    K.dgb = (const float4*)gbuf;
+    K.grad = (const float4*)grad_radiance;
+    K.g_vcol = (float4*)grads->vertex_color;
+    K.g_vnor = (float4*)grads->vertex_normal;
+    K.g_acc = c->d_acc.p;
+    KTRY(prk::launch_diff(K, true, st));
+    std::vector<double> acc(std::max<size_t>(n_acc, 1));
+    CUDA_TRY(cudaMemcpyAsync(acc.data(), c->d_acc.p, acc.size() * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (int m = 0; m < nm; m++) {
+        for (int k = 0; k < 3; k++) {
+            if (grads->kd) grads->kd[3 * m + k] = acc[7 * m + k];
+            if (grads->ks) grads->ks[3 * m + k] = acc[7 * m + 3 + k];
+        }
+        if (grads->shininess) grads->shininess[m] = acc[7 * m + 6];
+    }
+    for (int l = 0; l < nl; l++) {
+        const double* a = acc.data() + 7 * nm + 4 * l;
+        for (int k = 0; k < 3; k++)
+            if (grads->light_pos) grads->light_pos[3 * l + k] = frame->lights[l].type == PR_LIGHT_POINT ? a[k] : 0.0;
+        if (grads->light_intensity) grads->light_intensity[l] = a[3];
+    }
+    for (int e = 0; e < na; e++)
+        if (grads->ambient) grads->ambient[e] = acc[7 * nm + 4 * nl + e];
     return PR_OK;
 }
 

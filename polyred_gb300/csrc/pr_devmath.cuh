@@ -31,7 +31,7 @@ namespace prd {
 // ---------------------------------------------------------------------------
 // Kept out of line: if the compiler predicated this into the fast path, the
 // FP64 pipe (2 lanes/clk/SM on GB300) would be occupied on every call.
-__device__ __noinline__ float fma64f_slow(float a, float b, float c) {
+static __device__ __noinline__ float fma64f_slow(float a, float b, float c) {
     return __double2float_rn(__fma_rn((double)a, (double)b, (double)c));
 }
 
@@ -198,7 +198,7 @@ PR_DEV bool is_odd_int(double x) {
     long long i = (long long)xi;
     return (i & 1) == 1;
 }
-__device__ __noinline__ double go_pow(double x, double y) {
+static __device__ __noinline__ double go_pow(double x, double y) {
     if (y == 0 || x == 1) return 1;
     if (y == 1) return x;
     if (isnan(x) || isnan(y)) return __longlong_as_double(0x7ff8000000000000ll);
@@ -293,7 +293,7 @@ PR_DEV double go_satan(double x) {
     if (x > Tan3pio8) return __dadd_rn(__dsub_rn(PiOver2, go_xatan(__ddiv_rn(1.0, x))), Morebits);
     return __dadd_rn(__dadd_rn(PiOver4, go_xatan(__ddiv_rn(__dsub_rn(x, 1.0), __dadd_rn(x, 1.0)))), 0.5 * Morebits);
 }
-__device__ __noinline__ double go_atan(double x) {
+static __device__ __noinline__ double go_atan(double x) {
     if (x == 0) return x;
     if (x > 0) return go_satan(x);
     return -go_satan(-x);

@@ -335,6 +335,12 @@ __global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__
     int matid = -1;
     bool contained = false;
     const bool ok = t < P.n_tris && transform_main(P, t, v, recipw, &matid, &contained);
+    if (ok && P.tri_scr) {
+        float4* s = reinterpret_cast<float4*>(P.tri_scr + 12 * (size_t)t);
+        s[0] = make_float4(v[0].pos.x, v[0].pos.y, recipw[0], v[1].pos.x);
+        s[1] = make_float4(v[1].pos.y, recipw[1], v[2].pos.x, v[2].pos.y);
+        s[2] = make_float4(recipw[2], 0.0f, 0.0f, 0.0f);
+    }
     __syncwarp();
     const bool emit = ok && contained, clip = ok && !contained;
     uint32_t tot;
@@ -620,6 +626,42 @@ __global__ void decode_shadow_kernel(const uint32_t* smap, float* out, size_t n)
 // Go math.Pow(0.5, n) for an integer 0 <= n <= 16 is exactly 2^-n.
 PR_DEV float pow_half(int n) { return __uint_as_float((uint32_t)(127 - n) << 23); }
 
+// The differentiation G-buffer of one covered pixel: triangle, material,
+// flags, fixed factor (shadow now, AO multiplied in later), the screen
+// barycentric weights of the pixel centre in the input triangle (for a
+// material-less pixel: its perspective-correct weights), alpha, world
+// position and face normal.
+PR_DEV void diff_gbuffer_pixel(const ShadeParams& P, size_t i, uint32_t seq, int matid, const pr_material* mat,
+                               float shadow_w, uint32_t alpha, V4 wp, V4 fn, float fx, float fy) {
+    const uint32_t t = seq >> 3;
+    const float4* S = reinterpret_cast<const float4*>(P.tri_scr + 12 * (size_t)t);
+    const float4 s0 = S[0], s1 = S[1], s2 = S[2];
+    const float x0 = s0.x, y0 = s0.y, w0 = s0.z, x1 = s0.w, y1 = s1.x, w1 = s1.y, x2 = s1.z, y2 = s1.w, w2 = s2.x;
+    const float den = (y1 - y2) * (x0 - x2) + (x2 - x1) * (y0 - y2);
+    float b0 = ((y1 - y2) * (fx - x2) + (x2 - x1) * (fy - y2)) / den;
+    float b1 = ((y2 - y0) * (fx - x2) + (x0 - x2) * (fy - y2)) / den;
+    float b2 = 1.0f - b0 - b1;
+    uint32_t fl;
+    if (mat) {
+        fl = P.n_lights ? kDgbLit : kDgbConst;
+        if (mat->flags & PR_MAT_FLAT_SHADING) fl |= kDgbFlat;
+    } else {
+        fl = kDgbUnlit;
+        const bool persp = (P.flags & PR_FRAME_PERSPECTIVE) != 0;
+        const float q0 = persp ? w0 * b0 : b0, q1 = persp ? w1 * b1 : b1, q2 = persp ? w2 * b2 : b2;
+        const float inv = 1.0f / (q0 + q1 + q2);
+        b0 = q0 * inv;
+        b1 = q1 * inv;
+        b2 = q2 * inv;
+        shadow_w = 1.0f;
+    }
+    float4* D = P.dgb + 4 * i;
+    D[0] = make_float4(__uint_as_float(t), __int_as_float(matid), __uint_as_float(fl), shadow_w);
+    D[1] = make_float4(b0, b1, b2, small_u2f(alpha));
+    D[2] = make_float4(wp.x, wp.y, wp.z, 1.0f);
+    D[3] = make_float4(fn.x, fn.y, fn.z, fn.w);
+}
+
 __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = blockIdx.y * blockDim.y + threadIdx.y;
@@ -640,6 +682,13 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
         if (P.guvd) P.guvd[i] = make_float4(0, 0, 0, 0);
         if (P.gvcol) P.gvcol[i] = make_uchar4(0, 0, 0, 0);
         if (P.gmat) P.gmat[i] = -1;
+        if (P.dgb) {
+            float4* D = P.dgb + 4 * i;
+            D[0] = make_float4(__uint_as_float(kNone), __int_as_float(-1), 0.0f, 1.0f);
+            D[1] = make_float4(0.0f, 0.0f, 0.0f, small_u2f(c3));
+            D[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            D[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
     } else {
         const uint32_t ridx = P.first_rec[seq >> 3] + (seq & 7u);
         const float4* rp = reinterpret_cast<const float4*>(P.rrec + ridx);
@@ -701,6 +750,7 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
         if (P.gmat) P.gmat[i] = matid;
 
         c0 = vc[0]; c1 = vc[1]; c2 = vc[2]; c3 = vc[3];
+        float shadow_w = 1.0f;
         const pr_material* mat = (matid >= 0 && (uint32_t)matid < P.n_mats) ? &P.mats[matid] : nullptr;
         if (mat) {
             // FragmentShader (shader/blinn_cpu.go:24-106), uniform texture
@@ -772,6 +822,7 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
                     }
                 }
                 float w = pow_half(occl);
+                shadow_w = w;
                 c0 = go_f2u8(__fmul_rn(small_u2f(c0), w));
                 c1 = go_f2u8(__fmul_rn(small_u2f(c1), w));
                 c2 = go_f2u8(__fmul_rn(small_u2f(c2), w));
@@ -780,6 +831,7 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
             // on a compacted list of these pixels.
             ao_pending = (mat->flags & PR_MAT_AO) && P.rgba && P.ao_list;
         }
+        if (P.dgb) diff_gbuffer_pixel(P, i, seq, matid, mat, shadow_w, c3, wp, fn, fx, fy);
     }
     if (ao_pending) {
         P.rgba[i] = make_uchar4(c0, c1, c2, c3);  // pre-AO, pre-gamma colour
@@ -1053,6 +1105,12 @@ __global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant
         }
         const float T = nanpix ? __uint_as_float(0x7fc00000u) : __fdiv_rn(total, 12.5663706143591729539f);
         const uchar4 c = P.rgba[i];
+        if (P.dgb) {
+            // float32(Pow(T, 10000)) as a fixed factor of the differentiable radiance (0 for NaN, as the
+            // reference's uint8(NaN) darkens the pixel)
+            const float fa = isnan(T) ? 0.0f : (T == 1.0f ? 1.0f : powf(T, 10000.0f));
+            P.dgb[4 * i].w *= fa;
+        }
         uint3 o = ao_scale(T, c.x, c.y, c.z);
         if (P.gamma_on) {
             o.x = P.gamma[o.x];

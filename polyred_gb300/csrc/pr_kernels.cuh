@@ -87,6 +87,7 @@ struct SetupParams {
     uint32_t cap_tasks;
     uint32_t* first_rec;
     Counters* cnt;
+    float* tri_scr;              // differentiation only: [n_tris][12] screen x, y, recipw per vertex
 };
 
 enum RasterMode { kMain = 0, kMainFixup = 1, kShadow = 2, kShadowFixup = 3 };
@@ -137,7 +138,13 @@ struct ShadeParams {
     int32_t* gmat;
     uint32_t* ao_list;          // pixels whose material has AO (null: AO off)
     Counters* cnt_w;
+    // differentiation only (null otherwise)
+    const float* tri_scr;       // [n_tris][12] from the main setup
+    float4* dgb;                // [H][W][4] differentiation G-buffer
 };
+
+// Differentiation G-buffer pixel flags (float4 0, .z)
+constexpr uint32_t kDgbLit = 1u, kDgbFlat = 2u, kDgbConst = 4u, kDgbUnlit = 8u;
 
 struct AoParams {
     int W, H;
@@ -151,6 +158,34 @@ struct AoParams {
     int8_t dir_fast[8];  // 1: the tap offset table is exact for this frame size
     int8_t dir_tiny[8];  // 1 / 2: the x / y component lies in (-1/99, 0)
     float ao_half_ulp;   // half an ulp of float32 at max(W, H) + 100
+    float4* dgb;         // differentiation only: multiply the G-buffer's factor by the AO factor
+};
+
+// Differentiable shading (pr_diff.cu)
+constexpr int kDiffMaxMats = 256;
+struct DiffParamsK {
+    int W, H;
+    const float4* dgb;
+    const float4* vcol;          // [n_tris*3] RGBA in [0,1]
+    const float4* vnor;          // [n_tris*3] object-space normals
+    const uint32_t* obj_first;
+    uint32_t n_objects;
+    const float* obj_normal;     // [n_objects][16]
+    int n_mats;
+    const float* kd;             // [n_mats][3]
+    const float* ks;             // [n_mats][3]
+    const float* shin;           // [n_mats]
+    const pr_material* mats;     // texture texel, flags
+    int n_lights, n_ambient;
+    LightK lights[kMaxLights];
+    float ambient[kMaxAmbient];
+    float cam[3];
+    float bg[4];
+    float4* radiance;            // forward output
+    const float4* grad;          // backward input
+    float4* g_vcol;              // backward outputs (may be null)
+    float4* g_vnor;
+    double* g_acc;               // [n_mats*7 + n_lights*4 + n_ambient]: kd3 ks3 shin | pos3 I | ambient
 };
 
 }  // namespace prk
@@ -166,6 +201,9 @@ int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* s
                               void* stream);
 int launch_shade(const ShadeParams& p, void* stream);
 int launch_ao(const AoParams& p, void* stream);
+int launch_diff(const DiffParamsK& p, bool backward, void* stream);
+int launch_col_to_float(const uchar4* col, float4* out, size_t n, void* stream);
+int launch_fill_u32(uint32_t* p, uint32_t v, size_t n, void* stream);
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
 int launch_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const void* col, void* o_fast,

@@ -163,6 +163,43 @@ def sphere_field(n_spheres=256, lon=63, lat=32, seed=0x5EED0002, width=1920, hei
     return s, cam
 
 
+def ground_grid(n=64, size=24.0, y=-11.0, seed=0x5EED0005):
+    """An n x n quad grid (2 n^2 triangles) on y = const facing +y, with
+    random per-vertex colours and MaterialID -1 (shown with its vertex
+    colours, as model/plane.go's ground)."""
+    g = np.random.default_rng(seed)
+    h = size / 2
+    xs = np.linspace(-h, h, n + 1)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    P = np.stack([X, np.full_like(X, y), Z], -1)
+    C = g.integers(40, 216, (n + 1, n + 1, 4))
+    C[..., 3] = 255
+    pos, col = [], []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = (i, j + 1), (i + 1, j + 1), (i + 1, j), (i, j)
+            for tri in ((a, b, c), (a, c, d)):
+                pos.append([P[v] for v in tri])
+                col.append([C[v] for v in tri])
+    pos = np.asarray(pos)
+    nt = len(pos)
+    p4 = np.ones((nt, 3, 4), F32)
+    p4[..., :3] = pos
+    nor = np.zeros((nt, 3, 4), F32)
+    nor[..., 1] = 1
+    uv = np.zeros((nt, 3, 2), F32)
+    return sc.Mesh(p4, nor, uv, np.asarray(col, np.uint8), np.full(nt, -1, np.int32))
+
+
+def diff_scene(width=1920, height=1080, n_spheres=256, lon=63, lat=32, grid=64):
+    """The differentiation workload: the 1M-triangle sphere field (AO off,
+    both lights casting shadows) over a vertex-coloured ground grid, so that
+    per-vertex colours, normals, materials and lights all reach the image."""
+    s, cam = sphere_field(n_spheres=n_spheres, lon=lon, lat=lat, width=width, height=height, ao=False)
+    s.add(sc.Geometry(ground_grid(grid)))
+    return s, cam
+
+
 def triangle_soup(n_tris, width, height, seed=0x5EED0003, back_fraction=0.30, fov=60.0):
     """Small-triangle stress soup: centroids uniform on screen, view depth
     U[0.1, 100], area ~ LogNormal(ln 1 px^2, 1.0), random shape/orientation,
