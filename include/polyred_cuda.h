@@ -295,6 +295,54 @@ typedef struct pr_depth_map_desc {
 
 int pr_depth_map_noalloc(const pr_depth_map_desc* desc);
 
+/* ---- batched rendering ------------------------------------------------------
+ * No counterpart in the reference, where one Renderer renders one view at a
+ * time: many views, each with its own scene (uploaded once to the batch),
+ * camera, lights and outputs, rendered as one GPU job. Every view is the
+ * first Render() of a fresh renderer: its shadow maps start zeroed. Results
+ * are those pr_render gives for the view on a fresh context, bit for bit.
+ *
+ * The work runs as a fixed sequence of multi-view launches, captured once
+ * per batch shape in a CUDA graph and relaunched: triangle setup of every
+ * shadow pass (one per view and casting light) and of every view, then one
+ * persistent raster launch over a global queue of (pass, 32-task) work
+ * items, then resolve, shading and AO of every view. pr_batch_tune times the
+ * raster task size and the persistent grid over candidates and keeps the
+ * fastest, and sizes the record and task capacities from the needs it saw.
+ * Each view's outputs must be device pointers (PR_OUT_DEVICE_PTRS) with rgba
+ * set; shadow_maps output is not supported in a batch. */
+typedef struct pr_batch_view {
+    uint32_t scene;            /* index from pr_batch_add_scene */
+    uint32_t reserved;
+    const pr_frame_desc* frame;
+    pr_outputs* out;
+} pr_batch_view;
+
+typedef struct pr_batch_stats {
+    uint32_t size;
+    uint32_t n_views;
+    uint32_t n_passes;           /* raster passes: views + casting lights of each */
+    uint32_t n_kernel_launches;  /* kernels in the batch's sequence */
+    uint32_t graph_reused;       /* 1: the last batch relaunched a captured graph */
+    uint32_t n_fallback_views;   /* views re-rendered alone (NaN depth in a shadow pass) */
+    uint32_t n_retries;          /* re-runs after a capacity grew */
+    uint32_t task_px;            /* pixels per raster task */
+    uint32_t raster_blocks;      /* persistent raster grid */
+    uint32_t reserved;
+    double   ms_total;           /* device time of the last batch (CUDA events) */
+    uint64_t device_bytes;       /* device memory held by the batch's work buffers */
+} pr_batch_stats;
+
+int pr_batch_create(int device, void** out_batch);
+int pr_batch_destroy(void* batch);
+int pr_batch_add_scene(void* batch, const pr_scene_desc* scene, uint32_t* out_index);
+int pr_batch_render(void* batch, uint32_t n_views, const pr_batch_view* views);
+/* Renders the batch under each candidate setting and keeps the fastest;
+ * writes a JSON report (timings per candidate, chosen setting, capacities)
+ * into report[report_cap] when report is not NULL. */
+int pr_batch_tune(void* batch, uint32_t n_views, const pr_batch_view* views, char* report, size_t report_cap);
+int pr_batch_get_stats(void* batch, pr_batch_stats* out);
+
 /* ---- differentiable deferred shading --------------------------------------
  * No counterpart in the reference (which has no gradients): an adjoint of
  * the deferred-shading pass, shade + FragmentShader (render/raster.go:320-356,

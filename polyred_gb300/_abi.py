@@ -135,6 +135,32 @@ class pr_diff_grads(C.Structure):
     ]
 
 
+class pr_batch_view(C.Structure):
+    _fields_ = [
+        ("scene", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("frame", C.POINTER(pr_frame_desc)),
+        ("out", C.POINTER(pr_outputs)),
+    ]
+
+
+class pr_batch_stats(C.Structure):
+    _fields_ = [
+        ("size", C.c_uint32),
+        ("n_views", C.c_uint32),
+        ("n_passes", C.c_uint32),
+        ("n_kernel_launches", C.c_uint32),
+        ("graph_reused", C.c_uint32),
+        ("n_fallback_views", C.c_uint32),
+        ("n_retries", C.c_uint32),
+        ("task_px", C.c_uint32),
+        ("raster_blocks", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("ms_total", C.c_double),
+        ("device_bytes", C.c_uint64),
+    ]
+
+
 ENTRY_POINTS = [
     ("pr_abi_version", C.c_int, []),
     ("pr_error_string", C.c_char_p, [C.c_int]),
@@ -155,6 +181,12 @@ ENTRY_POINTS = [
     ("pr_mat4_inv", C.c_int, [FP, FP]),
     ("pr_shadow_camera", C.c_int, [FP, FP, FP, FP, FP, FP]),
     ("pr_depth_map_noalloc", C.c_int, [C.POINTER(pr_depth_map_desc)]),
+    ("pr_batch_create", C.c_int, [C.c_int, C.POINTER(VP)]),
+    ("pr_batch_destroy", C.c_int, [VP]),
+    ("pr_batch_add_scene", C.c_int, [VP, C.POINTER(pr_scene_desc), C.POINTER(C.c_uint32)]),
+    ("pr_batch_render", C.c_int, [VP, C.c_uint32, C.POINTER(pr_batch_view)]),
+    ("pr_batch_tune", C.c_int, [VP, C.c_uint32, C.POINTER(pr_batch_view), C.c_char_p, C.c_size_t]),
+    ("pr_batch_get_stats", C.c_int, [VP, C.POINTER(pr_batch_stats)]),
     ("pr_diff_forward", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_diff_params), VP, VP,
                                   C.POINTER(pr_outputs)]),
     ("pr_diff_backward", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_diff_params), VP, VP,

@@ -249,6 +249,56 @@ void collect_stats(Ctx* c) {
     c->stats.n_ao_pixels = c->h_cnt[0].n_ao;
 }
 
+// The frame-level fields of the deferred pass: size, flags, materials,
+// lights (render/raster.go:275-295), camera, background, matrices, gamma.
+void fill_shade_frame(const Ctx* c, const pr_frame_desc* f, const M4& s2w, int SW, int SH, prk::ShadeParams& sp) {
+    sp.W = f->width;
+    sp.H = f->height;
+    sp.flags = f->flags;
+    sp.mats = c->dmats.p;
+    sp.n_mats = (uint32_t)c->materials.size();
+    sp.n_lights = (int)f->n_lights;
+    sp.n_ambient = (int)f->n_ambient;
+    for (uint32_t l = 0; l < f->n_lights; l++) {
+        const pr_light& L = f->lights[l];
+        prk::LightK& K = sp.lights[l];
+        K.type = L.type;
+        K.cast = L.cast_shadow ? 1 : 0;
+        for (int k = 0; k < 3; k++) {
+            K.pos[k] = L.pos[k];
+            K.dir[k] = L.dir[k];
+            K.color[k] = (float)L.color[k];
+        }
+        K.intensity = L.intensity;
+        std::memcpy(K.lview, L.shadow_view, 64);
+        std::memcpy(K.lproj, L.shadow_proj, 64);
+    }
+    for (uint32_t e = 0; e < f->n_ambient; e++) sp.ambient[e] = f->ambient[e];
+    for (int k = 0; k < 3; k++) sp.cam[k] = f->cam_pos[k];
+    std::memcpy(sp.background, f->background, 4);
+    std::memcpy(sp.s2w, s2w.m, 64);
+    M4 svp = prh::viewport((float)SW, (float)SH);
+    std::memcpy(sp.shadow_vp, svp.m, 64);
+    sp.SW = SW;
+    sp.SH = SH;
+    prh::gamma_table(sp.gamma);
+}
+
+// Matrices of a frame (render/raster.go:232-246, 281-295).
+struct FrameMats {
+    M4 pv, vp, vp_inv, proj_inv, view_inv, s2w;
+};
+int frame_mats(const pr_frame_desc* f, FrameMats& m) {
+    M4 view = loadm(f->view), proj = loadm(f->proj);
+    m.vp = prh::viewport((float)f->width, (float)f->height);
+    if (!prh::inv(view, &m.view_inv)) return fail(PR_ERR_SINGULAR, "view matrix is singular");
+    if (!prh::inv(proj, &m.proj_inv)) return fail(PR_ERR_SINGULAR, "projection matrix is singular");
+    if (!prh::inv(m.vp, &m.vp_inv)) return fail(PR_ERR_SINGULAR, "viewport matrix is singular");
+    m.pv = prh::mulm(proj, view);
+    m.s2w = prh::mulm(prh::mulm(m.view_inv, m.proj_inv), m.vp_inv);
+    return PR_OK;
+}
+
 // Extra outputs of a differentiable forward frame.
 struct DiffHooks {
     float4* dgb;  // [H][W][4] differentiation G-buffer
@@ -402,42 +452,13 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         std::unique_ptr<prk::ShadeParams> sp_owner(new (std::nothrow) prk::ShadeParams());
         if (!sp_owner) return fail(PR_ERR_OOM, "host allocation failed");
         prk::ShadeParams& sp = *sp_owner;
-        sp.W = W;
-        sp.H = H;
-        sp.flags = f->flags;
+        fill_shade_frame(c, f, s2w, SW, SH, sp);
         sp.win = c->win.p;
         sp.depth_ao = c->depth_ao.p;
         sp.first_rec = c->first_rec.p;
         sp.rrec = c->rrec.p;
         sp.arec = c->arec.p;
-        sp.mats = c->dmats.p;
-        sp.n_mats = (uint32_t)c->materials.size();
-        sp.n_lights = NL;
-        sp.n_ambient = (int)f->n_ambient;
-        for (int l = 0; l < NL; l++) {
-            const pr_light& L = f->lights[l];
-            prk::LightK& K = sp.lights[l];
-            K.type = L.type;
-            K.cast = L.cast_shadow ? 1 : 0;
-            for (int k = 0; k < 3; k++) {
-                K.pos[k] = L.pos[k];
-                K.dir[k] = L.dir[k];
-                K.color[k] = (float)L.color[k];
-            }
-            K.intensity = L.intensity;
-            std::memcpy(K.lview, L.shadow_view, 64);
-            std::memcpy(K.lproj, L.shadow_proj, 64);
-        }
-        for (uint32_t e = 0; e < f->n_ambient; e++) sp.ambient[e] = f->ambient[e];
-        for (int k = 0; k < 3; k++) sp.cam[k] = f->cam_pos[k];
-        std::memcpy(sp.background, f->background, 4);
-        std::memcpy(sp.s2w, s2w.m, 64);
-        M4 svp = prh::viewport((float)SW, (float)SH);
-        std::memcpy(sp.shadow_vp, svp.m, 64);
-        sp.SW = SW;
-        sp.SH = SH;
         sp.smaps = shadows ? c->smap.p : nullptr;
-        prh::gamma_table(sp.gamma);
         sp.ao_list = c->ao_list.p;
         sp.cnt_w = dcnt;
         if (dh) {
@@ -955,6 +976,614 @@ int pr_debug_fma_probe(const float* a, const float* b, const float* c, float* ou
     int e = prk::launch_fma_probe(a, b, c, out, out_ref, n, nullptr);
     if (e) return fail(PR_ERR_CUDA, "fma probe launch: %s", cudaGetErrorString((cudaError_t)e));
     CUDA_TRY(cudaDeviceSynchronize());
+    return PR_OK;
+}
+
+}  // extern "C"
+
+// ---- batched rendering ----
+
+namespace {
+
+struct Batch {
+    std::mutex mu;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int n_sms = 1;
+    std::vector<Ctx*> scenes;
+    // tuning
+    uint32_t task_shift = prk::kTaskShift;
+    int raster_bps = 8;
+    // learned capacities, per view of the last shape (records / tasks of the view's main pass and of its shadow passes)
+    std::vector<uint32_t> cap_main_rec, cap_main_tasks, cap_shadow_tasks;
+    // work buffers
+    DevBuf<prk::RasterRec> rrec;
+    DevBuf<prk::AttrRec> arec;
+    DevBuf<uint2> tasks;
+    DevBuf<uint32_t> first_rec, clip_list;
+    DevBuf<prk::Counters> cnt;
+    DevBuf<unsigned long long> keys;
+    DevBuf<uint32_t> nanseq, beaten, win, ao_list, chunk, smaps;
+    DevBuf<float> depth_ao;
+    // job tables
+    DevBuf<prk::SetupParams> d_sj, d_mj;
+    DevBuf<prk::RasterParams> d_rj, d_fj;
+    DevBuf<prk::ResolveParams> d_res;
+    DevBuf<prk::ShadeParams> d_sh;
+    DevBuf<prk::AoParams> d_ao;
+    DevBuf<uint32_t> d_blk, d_items, d_fitems, d_queue;
+    prk::Counters* h_cnt = nullptr;
+    size_t h_cnt_n = 0;
+    cudaGraphExec_t gexec = nullptr;
+    std::string gkey;
+    pr_batch_stats stats{};
+};
+
+template <class T>
+size_t dev_bytes(const DevBuf<T>& b) { return b.n * sizeof(T); }
+
+// Host-side plan and job tables of one batch.
+struct BatchPlan {
+    uint32_t V = 0, S = 0;                 // views, shadow passes
+    std::vector<prk::SetupParams> sj, mj;  // shadow setup [S], main setup [V]
+    std::vector<prk::RasterParams> rj, fj; // raster [V + S] (main first), main fix-up [V]
+    std::vector<prk::ResolveParams> res;
+    std::vector<prk::ShadeParams> sh;
+    std::vector<prk::AoParams> ao;
+    std::vector<uint32_t> blk;             // blk_s[S+1] blk_m[V+1] blk_r[V+1] blk_sh[V+1]
+    uint32_t nb_s = 0, nb_m = 0, nb_r = 0, nb_sh = 0;
+    std::vector<int> shadow_view;          // view of each shadow pass
+    size_t n_rec = 0, n_rec_main = 0, n_tasks = 0, n_px = 0, n_smap = 0, n_first = 0;
+    std::string key;
+};
+
+int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) {
+    p = BatchPlan{};
+    p.V = nv;
+    if (b->cap_main_rec.size() != nv) {
+        b->cap_main_rec.assign(nv, 0);
+        b->cap_main_tasks.assign(nv, 0);
+        b->cap_shadow_tasks.assign(nv, 0);
+    }
+    // sizes and offsets
+    std::vector<size_t> rec_m(nv), task_m(nv), px(nv), first(nv), sm(nv);
+    struct SP { uint32_t v, l; size_t rec, task; };
+    std::vector<SP> sps;
+    size_t rec = 0, task = 0, npx = 0, nfirst = 0, nsm = 0;
+    for (uint32_t v = 0; v < nv; v++) {
+        const Ctx* c = b->scenes[views[v].scene];
+        const pr_frame_desc* f = views[v].frame;
+        const uint32_t n = c->n_tris;
+        const uint32_t r0 = n + n / 8 + 1024;
+        const uint32_t cr = std::max(r0, b->cap_main_rec[v]), ct = std::max(r0, b->cap_main_tasks[v]);
+        rec_m[v] = rec;
+        rec += cr;
+        task_m[v] = task;
+        task += ct;
+        b->cap_main_rec[v] = cr;
+        b->cap_main_tasks[v] = ct;
+        px[v] = npx;
+        npx += (size_t)f->width * f->height;
+        first[v] = nfirst;
+        nfirst += std::max<uint32_t>(n, 1);
+    }
+    p.n_rec_main = rec;
+    for (uint32_t v = 0; v < nv; v++) {
+        const Ctx* c = b->scenes[views[v].scene];
+        const pr_frame_desc* f = views[v].frame;
+        const bool shadows = (f->flags & PR_FRAME_SHADOWMAP) != 0;
+        const int SW = f->shadow_width > 0 ? f->shadow_width : f->width;
+        const int SH = f->shadow_height > 0 ? f->shadow_height : f->height;
+        sm[v] = nsm;
+        if (!shadows) continue;
+        nsm += (size_t)SW * SH * std::max<uint32_t>(f->n_lights, 1);
+        const uint32_t n = c->n_tris;
+        const uint32_t ct = std::max(n + n / 8 + 1024, b->cap_shadow_tasks[v]);
+        b->cap_shadow_tasks[v] = ct;
+        for (uint32_t l = 0; l < f->n_lights; l++) {
+            if (!f->lights[l].cast_shadow) continue;
+            sps.push_back({v, l, rec, task});
+            rec += std::max<uint32_t>(n, 1);
+            task += ct;
+        }
+    }
+    p.S = (uint32_t)sps.size();
+    p.n_rec = rec;
+    p.n_tasks = task;
+    p.n_px = npx;
+    p.n_first = nfirst;
+    p.n_smap = nsm;
+    int rc;
+    if ((rc = b->rrec.ensure(std::max<size_t>(rec, 1))) || (rc = b->arec.ensure(std::max<size_t>(p.n_rec_main, 1))) ||
+        (rc = b->tasks.ensure(std::max<size_t>(task, 1))) || (rc = b->first_rec.ensure(nfirst)) ||
+        (rc = b->clip_list.ensure(nfirst)) || (rc = b->cnt.ensure(nv + p.S)) || (rc = b->keys.ensure(npx)) ||
+        (rc = b->nanseq.ensure(npx)) || (rc = b->beaten.ensure(npx)) || (rc = b->win.ensure(npx)) ||
+        (rc = b->ao_list.ensure(npx)) || (rc = b->depth_ao.ensure(npx)) || (rc = b->chunk.ensure(nv)) ||
+        (rc = b->smaps.ensure(std::max<size_t>(nsm, 1))))
+        return rc;
+    if (b->h_cnt_n < nv + p.S) {
+        if (b->h_cnt) cudaFreeHost(b->h_cnt);
+        b->h_cnt = nullptr;
+        b->h_cnt_n = 0;
+        CUDA_TRY(cudaMallocHost((void**)&b->h_cnt, sizeof(prk::Counters) * (nv + p.S)));
+        b->h_cnt_n = nv + p.S;
+    }
+    prk::Counters* dcnt = b->cnt.p;
+    // shadow passes
+    p.sj.resize(p.S);
+    p.rj.resize(nv + p.S);
+    p.shadow_view.resize(p.S);
+    p.blk.push_back(0);
+    for (uint32_t s = 0; s < p.S; s++) {
+        const SP& q = sps[s];
+        Ctx* c = b->scenes[views[q.v].scene];
+        const pr_frame_desc* f = views[q.v].frame;
+        const int SW = f->shadow_width > 0 ? f->shadow_width : f->width;
+        const int SH = f->shadow_height > 0 ? f->shadow_height : f->height;
+        prk::SetupParams& sp = p.sj[s];
+        fill_scene_ptrs(c, sp);
+        sp.W = SW;
+        sp.H = SH;
+        sp.perspective = 0;
+        M4 lpv = prh::mulm(loadm(f->lights[q.l].shadow_proj), loadm(f->lights[q.l].shadow_view));
+        std::memcpy(sp.pv, lpv.m, 64);
+        M4 svp = prh::viewport((float)SW, (float)SH);
+        std::memcpy(sp.viewport, svp.m, 64);
+        sp.rrec = b->rrec.p + q.rec;
+        sp.arec = nullptr;
+        sp.cap_rec = std::max<uint32_t>(c->n_tris, 1);
+        sp.tasks = b->tasks.p + q.task;
+        sp.cap_tasks = b->cap_shadow_tasks[q.v];
+        sp.first_rec = nullptr;
+        sp.cnt = dcnt + nv + s;
+        sp.task_shift = b->task_shift;
+        p.shadow_view[s] = (int)q.v;
+        prk::RasterParams& rp = p.rj[nv + s];
+        rp.rrec = sp.rrec;
+        rp.tasks = sp.tasks;
+        rp.cnt = sp.cnt;
+        rp.cnt_w = sp.cnt;
+        rp.W = SW;
+        rp.H = SH;
+        rp.mode = prk::kShadow;
+        rp.smap = b->smaps.p + sm[q.v] + (size_t)SW * SH * q.l;
+        rp.lastnan = nullptr;  // NaN depth: the view is re-rendered alone
+        rp.task_shift = b->task_shift;
+        p.blk.push_back(p.blk.back() + (c->n_tris + 127) / 128);
+    }
+    p.nb_s = p.blk.back();
+    // main passes
+    p.mj.resize(nv);
+    p.fj.resize(nv);
+    p.res.resize(nv);
+    p.sh.resize(nv);
+    p.ao.resize(nv);
+    const size_t om = p.blk.size();
+    p.blk.push_back(0);
+    for (uint32_t v = 0; v < nv; v++) {
+        Ctx* c = b->scenes[views[v].scene];
+        const pr_frame_desc* f = views[v].frame;
+        FrameMats m;
+        if ((rc = frame_mats(f, m))) return rc;
+        prk::SetupParams& mp = p.mj[v];
+        fill_scene_ptrs(c, mp);
+        mp.W = f->width;
+        mp.H = f->height;
+        mp.perspective = (f->flags & PR_FRAME_PERSPECTIVE) ? 1 : 0;
+        std::memcpy(mp.pv, m.pv.m, 64);
+        std::memcpy(mp.viewport, m.vp.m, 64);
+        std::memcpy(mp.viewport_inv, m.vp_inv.m, 64);
+        std::memcpy(mp.proj_inv, m.proj_inv.m, 64);
+        std::memcpy(mp.view_inv, m.view_inv.m, 64);
+        mp.rrec = b->rrec.p + rec_m[v];
+        mp.arec = b->arec.p + rec_m[v];
+        mp.cap_rec = b->cap_main_rec[v];
+        mp.tasks = b->tasks.p + task_m[v];
+        mp.cap_tasks = b->cap_main_tasks[v];
+        mp.first_rec = b->first_rec.p + first[v];
+        mp.clip_list = b->clip_list.p + first[v];
+        mp.cnt = dcnt + v;
+        mp.task_shift = b->task_shift;
+        p.blk.push_back(p.blk.back() + (c->n_tris + 127) / 128);
+        const size_t o = px[v];
+        prk::RasterParams& rp = p.rj[v];
+        rp.rrec = mp.rrec;
+        rp.tasks = mp.tasks;
+        rp.cnt = mp.cnt;
+        rp.cnt_w = mp.cnt;
+        rp.W = f->width;
+        rp.H = f->height;
+        rp.mode = prk::kMain;
+        rp.keys = b->keys.p + o;
+        rp.nanseq = b->nanseq.p + o;
+        rp.beaten = b->beaten.p + o;
+        rp.task_shift = b->task_shift;
+        p.fj[v] = rp;
+        p.fj[v].mode = prk::kMainFixup;
+        prk::ResolveParams& R = p.res[v];
+        R.W = f->width;
+        R.H = f->height;
+        R.keys = rp.keys;
+        R.nanseq = rp.nanseq;
+        R.beaten = rp.beaten;
+        R.cnt = mp.cnt;
+        R.win = b->win.p + o;
+        R.depth_ao = b->depth_ao.p + o;
+        prk::ShadeParams& sp = p.sh[v];
+        const int SW = f->shadow_width > 0 ? f->shadow_width : f->width;
+        const int SH = f->shadow_height > 0 ? f->shadow_height : f->height;
+        fill_shade_frame(c, f, m.s2w, SW, SH, sp);
+        sp.win = R.win;
+        sp.depth_ao = R.depth_ao;
+        sp.first_rec = mp.first_rec;
+        sp.rrec = mp.rrec;
+        sp.arec = mp.arec;
+        sp.smaps = (f->flags & PR_FRAME_SHADOWMAP) ? b->smaps.p + sm[v] : nullptr;
+        sp.ao_list = b->ao_list.p + o;
+        sp.cnt_w = mp.cnt;
+        const pr_outputs* out = views[v].out;
+        sp.rgba = (uchar4*)out->rgba;
+        sp.tri_id = out->tri_id;
+        sp.depth = out->depth;
+        sp.gnor = (float4*)out->nor;
+        sp.gfnor = (float4*)out->face_nor;
+        sp.gwpos = (float4*)out->world_pos;
+        sp.guvd = (float4*)out->uvd;
+        sp.gvcol = (uchar4*)out->vcol;
+        sp.gmat = out->mat_id;
+        prk::AoParams& ap = p.ao[v];
+        ap.W = f->width;
+        ap.H = f->height;
+        ap.gamma_on = (f->flags & PR_FRAME_GAMMA) ? 1 : 0;
+        ap.n_dirs = c->n_ao_dirs;
+        ap.ao_half_ulp = prh::ao_classify(c->ao_cos, c->ao_sin, c->n_ao_dirs, f->width, f->height, ap.dir_fast,
+                                          ap.dir_tiny);
+        ap.depth = R.depth_ao;
+        ap.list = sp.ao_list;
+        ap.cnt = mp.cnt;
+        ap.rgba = sp.rgba;
+        std::memcpy(ap.gamma, sp.gamma, 256);
+    }
+    p.nb_m = p.blk.back();
+    const size_t orr = p.blk.size();
+    p.blk.push_back(0);
+    for (uint32_t v = 0; v < nv; v++)
+        p.blk.push_back(p.blk.back() + (uint32_t)(((size_t)views[v].frame->width * views[v].frame->height + 255) / 256));
+    p.nb_r = p.blk.back();
+    const size_t osh = p.blk.size();
+    p.blk.push_back(0);
+    for (uint32_t v = 0; v < nv; v++) {
+        const uint32_t tx = (uint32_t)(views[v].frame->width + 31) / 32, ty = (uint32_t)(views[v].frame->height + 7) / 8;
+        p.blk.push_back(p.blk.back() + tx * ty);
+    }
+    p.nb_sh = p.blk.back();
+    (void)om;
+    (void)orr;
+    (void)osh;
+    // the graph's shape: everything a captured launch depends on
+    char kb[128];
+    snprintf(kb, sizeof(kb), "%u/%u/%u/%u/%u/%u/%d/%zu/%zu|", nv, p.S, p.nb_s, p.nb_m, p.nb_r, p.nb_sh, b->raster_bps,
+             p.n_px, p.n_smap);
+    p.key = kb;
+    // every pointer the captured launches take as an argument
+    const void* args[] = {b->cnt.p, b->keys.p, b->nanseq.p, b->beaten.p, b->chunk.p, b->smaps.p, b->h_cnt,
+                          b->d_sj.p, b->d_mj.p, b->d_rj.p, b->d_fj.p, b->d_res.p, b->d_sh.p, b->d_ao.p,
+                          b->d_blk.p, b->d_items.p, b->d_fitems.p, b->d_queue.p};
+    for (const void* a : args) {
+        snprintf(kb, sizeof(kb), "%p,", a);
+        p.key += kb;
+    }
+    for (uint32_t v = 0; v < nv; v++) {
+        char vb[64];
+        const pr_frame_desc* f = views[v].frame;
+        snprintf(vb, sizeof(vb), "%dx%d:%u:%u,", f->width, f->height, (unsigned)(f->flags & PR_FRAME_SHADOWMAP),
+                 f->n_lights);
+        p.key += vb;
+    }
+    return PR_OK;
+}
+
+// The batch's launch sequence on b->st (captured into a graph by the caller).
+int batch_launch(Batch* b, const BatchPlan& p, uint32_t* launches) {
+    cudaStream_t st = b->st;
+    const uint32_t V = p.V, S = p.S;
+    const uint32_t* blk_s = b->d_blk.p;
+    const uint32_t* blk_m = blk_s + (S + 1);
+    const uint32_t* blk_r = blk_m + (V + 1);
+    const uint32_t* blk_sh = blk_r + (V + 1);
+    uint32_t n = 0;
+    CUDA_TRY(cudaMemsetAsync(b->cnt.p, 0, sizeof(prk::Counters) * (V + S), st));
+    CUDA_TRY(cudaMemsetAsync(b->keys.p, 0, p.n_px * 8, st));
+    CUDA_TRY(cudaMemsetAsync(b->nanseq.p, 0xff, p.n_px * 4, st));
+    CUDA_TRY(cudaMemsetAsync(b->beaten.p, 0, p.n_px * 4, st));
+    CUDA_TRY(cudaMemsetAsync(b->chunk.p, 0, V * 4, st));
+    if (p.n_smap) {
+        KTRY(prk::launch_fill_u32(b->smaps.p, 0x80000000u, p.n_smap, st));  // the key of +0.0f
+        n++;
+    }
+    if (S) {
+        KTRY(prk::launch_setup_shadow_batch(b->d_sj.p, blk_s, (int)S, p.nb_s, st));
+        n++;
+    }
+    KTRY(prk::launch_setup_main_batch(b->d_mj.p, blk_m, (int)V, p.nb_m, st));
+    KTRY(prk::launch_clip_batch(b->d_mj.p, blk_m, (int)V, p.nb_m, st));
+    KTRY(prk::launch_batch_scan(b->d_rj.p, (int)(V + S), b->d_items.p, b->d_queue.p, 0, st));
+    KTRY(prk::launch_raster_batch(b->d_rj.p, b->d_items.p, (int)(V + S), b->d_queue.p, b->n_sms * b->raster_bps, st));
+    KTRY(prk::launch_batch_scan(b->d_fj.p, (int)V, b->d_fitems.p, b->d_queue.p + 1, 1, st));
+    KTRY(prk::launch_raster_batch(b->d_fj.p, b->d_fitems.p, (int)V, b->d_queue.p + 1, b->n_sms * b->raster_bps, st));
+    KTRY(prk::launch_resolve_batch(b->d_res.p, blk_r, (int)V, p.nb_r, st));
+    KTRY(prk::launch_shade_batch(b->d_sh.p, blk_sh, (int)V, p.nb_sh, st));
+    KTRY(prk::launch_ao_batch(b->d_ao.p, (int)V, b->chunk.p, b->n_sms * 4, st));
+    n += 10;
+    CUDA_TRY(cudaMemcpyAsync(b->h_cnt, b->cnt.p, sizeof(prk::Counters) * (V + S), cudaMemcpyDeviceToHost, st));
+    *launches = n;
+    return PR_OK;
+}
+
+int batch_run(Batch* b, uint32_t nv, const pr_batch_view* views) {
+    int rc;
+    for (uint32_t v = 0; v < nv; v++) {
+        const pr_batch_view& bv = views[v];
+        if (bv.scene >= b->scenes.size()) return fail(PR_ERR_INVALID_ARG, "view %u: scene %u not added", v, bv.scene);
+        if ((rc = validate_frame(b->scenes[bv.scene], bv.frame))) return rc;
+        const pr_outputs* o = bv.out;
+        if (!o || o->size < sizeof(pr_outputs) || !(o->flags & PR_OUT_DEVICE_PTRS) || !o->rgba)
+            return fail(PR_ERR_INVALID_ARG, "view %u: outputs must be device pointers with rgba set", v);
+        if (o->shadow_maps) return fail(PR_ERR_UNSUPPORTED, "view %u: shadow_maps output is not batched", v);
+    }
+    CUDA_TRY(cudaSetDevice(b->device));
+    b->stats.n_retries = 0;
+    b->stats.n_fallback_views = 0;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        BatchPlan p;
+        if ((rc = batch_plan(b, nv, views, p))) return rc;
+        // device tables (uploaded before every launch; the graph reads them)
+        const size_t nblk = p.blk.size();
+        if ((rc = b->d_sj.ensure(std::max<size_t>(p.S, 1))) || (rc = b->d_mj.ensure(nv)) ||
+            (rc = b->d_rj.ensure(nv + p.S)) || (rc = b->d_fj.ensure(nv)) || (rc = b->d_res.ensure(nv)) ||
+            (rc = b->d_sh.ensure(nv)) || (rc = b->d_ao.ensure(nv)) || (rc = b->d_blk.ensure(nblk)) ||
+            (rc = b->d_items.ensure(nv + p.S + 1)) || (rc = b->d_fitems.ensure(nv + 1)) || (rc = b->d_queue.ensure(2)))
+            return rc;
+        if ((rc = batch_plan(b, nv, views, p))) return rc;  // again: pointers of grown tables
+        cudaStream_t st = b->st;
+        if (p.S) CUDA_TRY(cudaMemcpyAsync(b->d_sj.p, p.sj.data(), p.S * sizeof(prk::SetupParams), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b->d_mj.p, p.mj.data(), nv * sizeof(prk::SetupParams), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b->d_rj.p, p.rj.data(), (nv + p.S) * sizeof(prk::RasterParams), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b->d_fj.p, p.fj.data(), nv * sizeof(prk::RasterParams), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b->d_res.p, p.res.data(), nv * sizeof(prk::ResolveParams), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b->d_sh.p, p.sh.data(), nv * sizeof(prk::ShadeParams), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b->d_ao.p, p.ao.data(), nv * sizeof(prk::AoParams), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b->d_blk.p, p.blk.data(), nblk * 4, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        uint32_t launches = 0;
+        b->stats.graph_reused = 0;
+        if (b->gexec && b->gkey == p.key) {
+            b->stats.graph_reused = 1;
+            launches = b->stats.n_kernel_launches;
+        } else {
+            if (b->gexec) cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+            b->gkey.clear();
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int lrc = batch_launch(b, p, &launches);
+            cudaError_t ce = cudaStreamEndCapture(st, &g);
+            if (lrc) {
+                if (g) cudaGraphDestroy(g);
+                return lrc;
+            }
+            if (ce != cudaSuccess) return fail(PR_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+            ce = cudaGraphInstantiate(&b->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) return fail(PR_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+            b->gkey = p.key;
+        }
+        CUDA_TRY(cudaEventRecord(b->e0, st));
+        CUDA_TRY(cudaGraphLaunch(b->gexec, st));
+        CUDA_TRY(cudaEventRecord(b->e1, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->e0, b->e1);
+        b->stats.ms_total = ms;
+        b->stats.n_kernel_launches = launches;
+        b->stats.n_views = nv;
+        b->stats.n_passes = nv + p.S;
+        b->stats.task_px = 1u << b->task_shift;
+        b->stats.raster_blocks = (uint32_t)(b->n_sms * b->raster_bps);
+        // capacities: grow the passes that overflowed and run again
+        bool grow = false;
+        for (uint32_t v = 0; v < nv; v++) {
+            const prk::Counters& k = b->h_cnt[v];
+            if (k.overflow & 4u) return fail(PR_ERR_UNSUPPORTED, "view %u: a clipped polygon exceeded 9 vertices", v);
+            if (k.overflow) {
+                grow = true;
+                b->cap_main_rec[v] = std::max(b->cap_main_rec[v], k.need_rec + k.need_rec / 4);
+                b->cap_main_tasks[v] = std::max(b->cap_main_tasks[v], k.need_tasks + k.need_tasks / 4);
+            }
+        }
+        std::vector<char> redo(nv, 0);
+        for (uint32_t s = 0; s < p.S; s++) {
+            const prk::Counters& k = b->h_cnt[nv + s];
+            const int v = p.shadow_view[s];
+            if (k.overflow) {
+                grow = true;
+                b->cap_shadow_tasks[v] = std::max(b->cap_shadow_tasks[v], k.need_tasks + k.need_tasks / 4);
+            } else if (k.nan_flag) {
+                redo[v] = 1;
+            }
+        }
+        size_t bytes = dev_bytes(b->rrec) + dev_bytes(b->arec) + dev_bytes(b->tasks) + dev_bytes(b->first_rec) +
+                       dev_bytes(b->clip_list) + dev_bytes(b->keys) + dev_bytes(b->nanseq) + dev_bytes(b->beaten) +
+                       dev_bytes(b->win) + dev_bytes(b->ao_list) + dev_bytes(b->depth_ao) + dev_bytes(b->smaps);
+        b->stats.device_bytes = bytes;
+        if (grow) {
+            b->stats.n_retries++;
+            continue;
+        }
+        // NaN depth in a shadow pass needs the per-texel fix-up of the single-view path
+        for (uint32_t v = 0; v < nv; v++) {
+            if (!redo[v]) continue;
+            Ctx* c = b->scenes[views[v].scene];
+            std::lock_guard<std::mutex> lk(c->mu);
+            c->smap_valid = false;
+            rc = PR_ERR_OVERFLOW;
+            for (int a = 0; a < 4 && rc == PR_ERR_OVERFLOW; a++) {
+                rc = render_impl(c, views[v].frame, views[v].out, true);
+                if (rc == PR_ERR_OVERFLOW) {
+                    uint32_t nr = 0, nt = 0;
+                    for (int k = 0; k <= prk::kMaxLights; k++) {
+                        nr = std::max(nr, c->h_cnt[k].need_rec);
+                        nt = std::max(nt, c->h_cnt[k].need_tasks);
+                    }
+                    int r2 = ensure_work(c, nr + nr / 4, nt + nt / 4);
+                    if (r2) return r2;
+                }
+            }
+            if (rc) return rc;
+            b->stats.n_fallback_views++;
+        }
+        return PR_OK;
+    }
+    return fail(PR_ERR_OVERFLOW, "batch capacities still exceeded after growth");
+}
+
+}  // namespace
+
+extern "C" {
+
+int pr_batch_create(int device, void** out_batch) {
+    if (!out_batch) return fail(PR_ERR_INVALID_ARG, "out_batch is NULL");
+    *out_batch = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return fail(PR_ERR_NO_DEVICE, "no CUDA device %d", device);
+    Batch* b = new (std::nothrow) Batch();
+    if (!b) return fail(PR_ERR_OOM, "host allocation failed");
+    b->device = device;
+    CUDA_TRY(cudaSetDevice(device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&b->e0));
+    CUDA_TRY(cudaEventCreate(&b->e1));
+    b->n_sms = prk::sm_count();
+    b->stats.size = sizeof(pr_batch_stats);
+    *out_batch = b;
+    return PR_OK;
+}
+
+int pr_batch_destroy(void* batch) {
+    Batch* b = (Batch*)batch;
+    if (!b) return fail(PR_ERR_INVALID_ARG, "batch is NULL");
+    cudaSetDevice(b->device);
+    if (b->st) cudaStreamSynchronize(b->st);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (Ctx* c : b->scenes) pr_destroy(c);
+    b->rrec.release(); b->arec.release(); b->tasks.release(); b->first_rec.release(); b->clip_list.release();
+    b->cnt.release(); b->keys.release(); b->nanseq.release(); b->beaten.release(); b->win.release();
+    b->ao_list.release(); b->chunk.release(); b->smaps.release(); b->depth_ao.release();
+    b->d_sj.release(); b->d_mj.release(); b->d_rj.release(); b->d_fj.release(); b->d_res.release();
+    b->d_sh.release(); b->d_ao.release(); b->d_blk.release(); b->d_items.release(); b->d_fitems.release();
+    b->d_queue.release();
+    if (b->h_cnt) cudaFreeHost(b->h_cnt);
+    if (b->e0) cudaEventDestroy(b->e0);
+    if (b->e1) cudaEventDestroy(b->e1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return PR_OK;
+}
+
+int pr_batch_add_scene(void* batch, const pr_scene_desc* scene, uint32_t* out_index) {
+    Batch* b = (Batch*)batch;
+    if (!b || !scene || !out_index) return fail(PR_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    void* c = nullptr;
+    int rc = pr_create(b->device, &c);
+    if (rc) return rc;
+    if ((rc = pr_scene_upload(c, scene))) {
+        pr_destroy(c);
+        return rc;
+    }
+    CUDA_TRY(cudaStreamSynchronize(((Ctx*)c)->stream));
+    b->scenes.push_back((Ctx*)c);
+    *out_index = (uint32_t)(b->scenes.size() - 1);
+    return PR_OK;
+}
+
+int pr_batch_render(void* batch, uint32_t n_views, const pr_batch_view* views) {
+    Batch* b = (Batch*)batch;
+    if (!b) return fail(PR_ERR_INVALID_ARG, "batch is NULL");
+    if (n_views == 0) return PR_OK;
+    if (!views) return fail(PR_ERR_INVALID_ARG, "views is NULL");
+    std::lock_guard<std::mutex> lk(b->mu);
+    return batch_run(b, n_views, views);
+}
+
+int pr_batch_tune(void* batch, uint32_t n_views, const pr_batch_view* views, char* report, size_t report_cap) {
+    Batch* b = (Batch*)batch;
+    if (!b) return fail(PR_ERR_INVALID_ARG, "batch is NULL");
+    if (n_views == 0 || !views) return fail(PR_ERR_INVALID_ARG, "no views");
+    std::lock_guard<std::mutex> lk(b->mu);
+    const uint32_t shifts[] = {8, 9, 10, 11, 12};
+    const int bps[] = {2, 4, 8};
+    std::string rep = "{\"candidates\": [";
+    double best = 1e30;
+    uint32_t best_shift = b->task_shift;
+    int best_bps = b->raster_bps, rc;
+    bool first = true;
+    for (uint32_t sh : shifts) {
+        for (int g : bps) {
+            b->task_shift = sh;
+            b->raster_bps = g;
+            if ((rc = batch_run(b, n_views, views))) return rc;  // warm-up: capacities, graph
+            double t = 0;
+            for (int k = 0; k < 3; k++) {
+                if ((rc = batch_run(b, n_views, views))) return rc;
+                t += b->stats.ms_total;
+            }
+            t /= 3;
+            char buf[96];
+            snprintf(buf, sizeof(buf), "%s[%u, %d, %.4f]", first ? "" : ", ", 1u << sh, g, t);
+            rep += buf;
+            first = false;
+            if (t < best) {
+                best = t;
+                best_shift = sh;
+                best_bps = g;
+            }
+        }
+    }
+    b->task_shift = best_shift;
+    b->raster_bps = best_bps;
+    // capacities: what the chosen setting needs, with a margin
+    if ((rc = batch_run(b, n_views, views))) return rc;
+    size_t rec = 0, tasks = 0;
+    for (uint32_t v = 0; v < n_views; v++) {
+        const prk::Counters& k = b->h_cnt[v];
+        const uint32_t n = b->scenes[views[v].scene]->n_tris;
+        b->cap_main_rec[v] = std::max(k.n_rec + k.n_rec / 16 + 64, std::min(b->cap_main_rec[v], n + n / 8 + 1024));
+        b->cap_main_tasks[v] = k.n_tasks + k.n_tasks / 16 + 64;
+        rec += b->cap_main_rec[v];
+        tasks += b->cap_main_tasks[v];
+    }
+    if ((rc = batch_run(b, n_views, views))) return rc;
+    char buf[256];
+    snprintf(buf, sizeof(buf),
+             "], \"task_px\": %u, \"raster_blocks_per_sm\": %d, \"ms\": %.4f, \"main_record_capacity\": %zu, "
+             "\"main_task_capacity\": %zu}",
+             1u << b->task_shift, b->raster_bps, b->stats.ms_total, rec, tasks);
+    rep += buf;
+    if (report && report_cap) {
+        std::strncpy(report, rep.c_str(), report_cap - 1);
+        report[report_cap - 1] = 0;
+    }
+    return PR_OK;
+}
+
+int pr_batch_get_stats(void* batch, pr_batch_stats* out) {
+    Batch* b = (Batch*)batch;
+    if (!b || !out) return fail(PR_ERR_INVALID_ARG, "NULL argument");
+    if (out->size < sizeof(pr_batch_stats)) return fail(PR_ERR_INVALID_ARG, "out->size too small");
+    *out = b->stats;
     return PR_OK;
 }
 

@@ -266,12 +266,12 @@ PR_DEV uint32_t warp_reserve(uint32_t* counter, uint32_t n, uint32_t* total) {
     return base + incl - n;
 }
 
-PR_DEV uint32_t n_tasks_of(uint32_t area) { return (area + kTaskPx - 1) / kTaskPx; }
+PR_DEV uint32_t n_tasks_of(uint32_t area, uint32_t shift) { return (area + (1u << shift) - 1u) >> shift; }
 
 // Write the raster tasks of up to 8 records (areas given); all lanes call.
 PR_DEV void emit_tasks_warp(const SetupParams& P, const uint32_t* ridx, const uint32_t* area, int n) {
     uint32_t mine = 0;
-    for (int i = 0; i < n; i++) mine += n_tasks_of(area[i]);
+    for (int i = 0; i < n; i++) mine += n_tasks_of(area[i], P.task_shift);
     uint32_t tot;
     uint32_t o = warp_reserve(&P.cnt->n_tasks, mine, &tot);
     if (mine == 0) return;
@@ -281,7 +281,7 @@ PR_DEV void emit_tasks_warp(const SetupParams& P, const uint32_t* ridx, const ui
         return;
     }
     for (int i = 0; i < n; i++) {
-        uint32_t nt = n_tasks_of(area[i]);
+        uint32_t nt = n_tasks_of(area[i], P.task_shift);
         for (uint32_t c = 0; c < nt; c++) P.tasks[o++] = make_uint2(ridx[i], c);
     }
 }
@@ -328,8 +328,7 @@ PR_DEV bool transform_main(const SetupParams& P, uint32_t t, SubVtx* v, float* r
 
 // cpuForwardPass + draw for triangles fully inside the viewport
 // (render/raster.go:257-269, 380-436); clipped ones go to clip_kernel.
-__global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P, uint32_t* clip_list) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+PR_DEV void setup_main_one(const SetupParams& P, uint32_t t, uint32_t* clip_list) {
     SubVtx v[3];
     float recipw[3];
     int matid = -1;
@@ -359,13 +358,15 @@ __global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__
     }
     emit_tasks_warp(P, &ridx, &area, 1);
 }
+__global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P, uint32_t* clip_list) {
+    setup_main_one(P, blockIdx.x * blockDim.x + threadIdx.x, clip_list);
+}
 
 // clipTriangle (render/clipping.go:70-157) for the listed triangles: fan
 // sub-triangles with seq = tri*8 + i, drawn with the parent's recipw.
-__global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ SetupParams P, const uint32_t* clip_list) {
-    const uint32_t n = P.cnt->n_clipped;
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (blockIdx.x * blockDim.x >= n) return;  // whole block idle (uniform per warp too)
+// j: this thread's entry of the clip list; the whole warp calls (warp
+// reservations), with entries past the list's length idle.
+PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j, uint32_t n) {
     SubVtx v[3];
     float recipw[3];
     int matid = -1;
@@ -409,10 +410,14 @@ __global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ Setup
     }
     emit_tasks_warp(P, ridxs, areas, nw);
 }
+__global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ SetupParams P, const uint32_t* clip_list) {
+    const uint32_t n = P.cnt->n_clipped;
+    if (blockIdx.x * blockDim.x >= n) return;  // whole block idle (uniform per warp too)
+    clip_one(P, clip_list, blockIdx.x * blockDim.x + threadIdx.x, n);
+}
 
 // passShadows / drawDepth for one input triangle (render/shadow.go:137-192)
-__global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+PR_DEV void setup_shadow_one(const SetupParams& P, uint32_t t) {
     bool ok = false;
     SubVtx v[3];
     if (t < P.n_tris) {
@@ -448,6 +453,9 @@ __global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant
     }
     uint32_t ridx = t;
     emit_tasks_warp(P, &ridx, &area, ok ? 1 : 0);
+}
+__global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
+    setup_shadow_one(P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- raster
@@ -493,25 +501,18 @@ PR_DEV bool pixel_depth(const SmRec& r, int px, int py, float* zout) {
     return true;
 }
 
-__global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_constant__ RasterParams P) {
-    __shared__ SmRec s_rec[kRasterWarps][32];
-    __shared__ int s_start[kRasterWarps][32];
-    const Counters* c = P.cnt;
-    if (P.mode == kMainFixup || P.mode == kShadowFixup) {
-        if (c->nan_flag == 0) return;
-    }
-    uint32_t n_tasks = c->n_tasks;
-    if (c->overflow) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t gw = blockIdx.x * kRasterWarps + warp, nw = gridDim.x * kRasterWarps;
-    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) {
+// Tasks [base, base + 32) of one pass, one per lane, pixels spread over the
+// warp by a prefix scan of their counts. s_rec / s_start: this warp's slots.
+PR_DEV void raster_warp(const RasterParams& P, uint32_t base, uint32_t n_tasks, SmRec* s_rec, int* s_start) {
+    const int lane = threadIdx.x & 31;
+    {
         uint32_t ti = base + lane;
         int cnt = 0;
         if (ti < n_tasks) {
             uint2 tk = P.tasks[ti];
             const float4* rp = reinterpret_cast<const float4*>(P.rrec + tk.x);
             float4 q0 = rp[0], q1 = rp[1], q2 = rp[2], q3 = rp[3];
-            SmRec& s = s_rec[warp][lane];
+            SmRec& s = s_rec[lane];
             s.x[0] = q0.x; s.y[0] = q0.y; s.z[0] = q0.z;
             s.x[1] = q0.w; s.y[1] = q1.x; s.z[1] = q1.y;
             s.x[2] = q1.z; s.y[2] = q1.w; s.z[2] = q2.x;
@@ -521,8 +522,8 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
             uint32_t x0 = bx & 0xffffu, x1 = bx >> 16, y0 = by & 0xffffu, y1 = by >> 16;
             if (x0 <= x1 && y0 <= y1) {
                 uint32_t bw = x1 - x0 + 1, area = bw * (y1 - y0 + 1);
-                uint32_t k0 = tk.y * (uint32_t)kTaskPx;
-                if (k0 < area) cnt = (int)min(area - k0, (uint32_t)kTaskPx);
+                uint32_t k0 = tk.y << P.task_shift;
+                if (k0 < area) cnt = (int)min(area - k0, 1u << P.task_shift);
                 s.x0 = x0;
                 s.y0 = y0;
                 s.bw = bw;
@@ -537,18 +538,19 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
             int v = __shfl_up_sync(0xffffffffu, incl, d);
             if (lane >= d) incl += v;
         }
-        s_start[warp][lane] = incl - cnt;
+        s_start[lane] = incl - cnt;
         int total = __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
         for (int g = lane; g < total; g += 32) {
             int j = 0;
 #pragma unroll
             for (int step = 16; step > 0; step >>= 1)
-                if (s_start[warp][j + step] <= g) j += step;
-            const SmRec& r = s_rec[warp][j];
-            // pixel qx0 + l of the task's first row, l < kTaskPx: t < 2^15,
-            // where the multiply-high quotient is exact for bw < 2^15
-            const uint32_t t = r.qx0 + (uint32_t)(g - s_start[warp][j]);
+                if (s_start[j + step] <= g) j += step;
+            const SmRec& r = s_rec[j];
+            // pixel qx0 + l of the task's first row, l < 2^task_shift <= 2^16:
+            // t < 2^17, where the multiply-high quotient is exact for
+            // bw <= 2^15 (t * bw < 2^32)
+            const uint32_t t = r.qx0 + (uint32_t)(g - s_start[j]);
             const uint32_t q = __umulhi(t, r.magic);
             int px = (int)(r.x0 + (t - q * r.bw));
             int py = (int)(r.y0 + r.qy0 + q);
@@ -574,7 +576,7 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
             } else if (P.mode == kShadow) {
                 size_t i = (size_t)px + (size_t)py * P.W;
                 if (zn) {
-                    atomicMax(&P.lastnan[i], r.seq + 1u);
+                    if (P.lastnan) atomicMax(&P.lastnan[i], r.seq + 1u);
                     atomicExch(&P.cnt_w->nan_flag, 1u);
                     atomicAdd(&P.cnt_w->n_nan, 1u);
                 } else {
@@ -590,9 +592,22 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
     }
 }
 
-__global__ void resolve_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
-                               const uint32_t* beaten, const Counters* cnt, uint32_t* win, float* depth_ao) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_constant__ RasterParams P) {
+    __shared__ SmRec s_rec[kRasterWarps][32];
+    __shared__ int s_start[kRasterWarps][32];
+    const Counters* c = P.cnt;
+    if (P.mode == kMainFixup || P.mode == kShadowFixup) {
+        if (c->nan_flag == 0) return;
+    }
+    const uint32_t n_tasks = c->n_tasks;
+    if (c->overflow) return;
+    const int warp = threadIdx.x >> 5;
+    const uint32_t gw = blockIdx.x * kRasterWarps + warp, nw = gridDim.x * kRasterWarps;
+    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) raster_warp(P, base, n_tasks, s_rec[warp], s_start[warp]);
+}
+
+PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
+                        const Counters* cnt, uint32_t* win, float* depth_ao, size_t i) {
     if (i >= (size_t)W * H) return;
     unsigned long long key = keys[i];
     uint32_t w = kNone;
@@ -606,6 +621,10 @@ __global__ void resolve_kernel(int W, int H, const unsigned long long* keys, con
     }
     win[i] = w;
     depth_ao[i] = d;
+}
+__global__ void resolve_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
+                               const uint32_t* beaten, const Counters* cnt, uint32_t* win, float* depth_ao) {
+    resolve_one(W, H, keys, nanseq, beaten, cnt, win, depth_ao, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Shadow NaN fix-up: pixels that saw a NaN-depth fragment restart from NaN
@@ -662,9 +681,7 @@ PR_DEV void diff_gbuffer_pixel(const ShadeParams& P, size_t i, uint32_t seq, int
     D[3] = make_float4(fn.x, fn.y, fn.z, fn.w);
 }
 
-__global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r = blockIdx.y * blockDim.y + threadIdx.y;
+PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
     if (x >= P.W || r >= P.H) return;
     const int W = P.W, H = P.H;
     const int y = H - 1 - r;
@@ -857,6 +874,9 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
     }
     if (P.rgba) P.rgba[i] = make_uchar4(c0, c1, c2, c3);
 }
+__global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
+    shade_one(P, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
 
 // ---------------------------------------------------------------- AO
 
@@ -995,13 +1015,9 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
 // tiny component. Taps with cur < 0 (int truncates toward zero there) and
 // the last taps that do not fill a group of four take the float path.
 // Tap 1 always takes it: its distance may fall below 1 (diagonals).
-__global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant__ AoParams P) {
-    __shared__ __align__(16) int s_off[8][kAoTable];
-    __shared__ __align__(16) float s_rlo[8][kAoTable];
-    __shared__ __align__(16) float s_rhi[8][kAoTable];
-    const uint32_t n = P.cnt->n_ao;
-    if (blockIdx.x * blockDim.x >= n) return;  // whole block: no pixel of the list
-    const int W = P.W, H = P.H;
+// The tap tables of a W x H frame (every thread of the block calls).
+PR_DEV void ao_tables(const AoParams& P, int (*s_off)[kAoTable], float (*s_rlo)[kAoTable], float (*s_rhi)[kAoTable]) {
+    const int W = P.W;
     for (int e = threadIdx.x; e < 8 * kAoTable; e += blockDim.x) {
         const int k = e / kAoTable, q = e - k * kAoTable, t = q + 2;
         int o = 0;
@@ -1021,103 +1037,253 @@ __global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant
         s_rlo[k][q] = rlo;
         s_rhi[k][q] = rhi;
     }
-    __syncthreads();
+}
 
+// One pixel of the AO list.
+PR_DEV void ao_one(const AoParams& P, uint32_t j, const int (*s_off)[kAoTable], const float (*s_rlo)[kAoTable],
+                   const float (*s_rhi)[kAoTable]) {
+    const int W = P.W, H = P.H;
     const float fW = (float)W, fH = (float)H;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t i = P.list[j];
-        const int r = (int)(i / (uint32_t)W);
-        const int x = (int)i - r * W;
-        const int y = H - 1 - r;
-        const float* p0 = P.depth + i;
-        const float z = *p0;
-        const float pxf = small_u2f((uint32_t)x), pyf = small_u2f((uint32_t)y);
-        float total = 0.0f;
-        bool nanpix = false;
-        for (int k = 0; k < P.n_dirs; k++) {
-            const float dX = c_ao_dir[0][k], dY = c_ao_dir[1][k];
-            int t_end = kAoTaps, t_fast = kAoTaps;
-            {
-                const float cx = __fadd_rn(pxf, __fmul_rn(dX, 99.0f)), cy = __fadd_rn(pyf, __fmul_rn(dY, 99.0f));
-                if (!(cx >= 0.0f && cx < fW && cy >= 0.0f && cy < fH)) {
-                    // first tap outside (-1, W) x (-1, H), then first tap with cur < 0
-                    int lo = 1, hi = kAoTaps;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        const float tf = small_u2f((uint32_t)mid);
-                        const float mx = __fadd_rn(pxf, __fmul_rn(dX, tf)), my = __fadd_rn(pyf, __fmul_rn(dY, tf));
-                        if (mx > -1.0f && mx < fW && my > -1.0f && my < fH)
-                            lo = mid + 1;
-                        else
-                            hi = mid;
-                    }
-                    t_end = lo;
-                    lo = 1;
-                    hi = t_end;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        const float tf = small_u2f((uint32_t)mid);
-                        const float mx = __fadd_rn(pxf, __fmul_rn(dX, tf)), my = __fadd_rn(pyf, __fmul_rn(dY, tf));
-                        if (mx >= 0.0f && my >= 0.0f)
-                            lo = mid + 1;
-                        else
-                            hi = mid;
-                    }
-                    t_fast = lo;
+    const uint32_t i = P.list[j];
+    const int r = (int)(i / (uint32_t)W);
+    const int x = (int)i - r * W;
+    const int y = H - 1 - r;
+    const float* p0 = P.depth + i;
+    const float z = *p0;
+    const float pxf = small_u2f((uint32_t)x), pyf = small_u2f((uint32_t)y);
+    float total = 0.0f;
+    bool nanpix = false;
+    for (int k = 0; k < P.n_dirs; k++) {
+        const float dX = c_ao_dir[0][k], dY = c_ao_dir[1][k];
+        int t_end = kAoTaps, t_fast = kAoTaps;
+        {
+            const float cx = __fadd_rn(pxf, __fmul_rn(dX, 99.0f)), cy = __fadd_rn(pyf, __fmul_rn(dY, 99.0f));
+            if (!(cx >= 0.0f && cx < fW && cy >= 0.0f && cy < fH)) {
+                // first tap outside (-1, W) x (-1, H), then first tap with cur < 0
+                int lo = 1, hi = kAoTaps;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    const float tf = small_u2f((uint32_t)mid);
+                    const float mx = __fadd_rn(pxf, __fmul_rn(dX, tf)), my = __fadd_rn(pyf, __fmul_rn(dY, tf));
+                    if (mx > -1.0f && mx < fW && my > -1.0f && my < fH)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
                 }
-            }
-            // the padding taps 100, 101 read the pixel itself: elev 0 needs a finite depth
-            if (!P.dir_fast[k] || !isfinite(z)) t_fast = 1;
-            float best = 0.0f;
-            bool ok = true;
-            if (t_end > 1) ok = ao_tap_exact(1, pxf, pyf, dX, dY, W, H, P.depth, z, 0.0f, best);
-            int t = 2;
-            if (ok && t_fast > 2) {
-                const int n_groups = t_fast == kAoTaps ? kAoTable / 4 : (t_fast - 2) >> 2;
-                const int tiny = P.dir_tiny[k];
-                if (tiny) {
-                    // t*: first tap with |a| above half the gap below the coordinate
-                    const float cf = fabsf(tiny == 1 ? dX : dY);
-                    const uint32_t vb = __float_as_uint(tiny == 1 ? pxf : pyf);
-                    const float h = __uint_as_float(((vb >> 23) - ((vb & 0x7fffffu) ? 24u : 25u)) << 23);
-                    int lo = 1, hi = kAoTaps;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (__fmul_rn(cf, small_u2f((uint32_t)mid)) > h)
-                            hi = mid;
-                        else
-                            lo = mid + 1;
-                    }
-                    const float* pA = p0 + (tiny == 1 ? 1 : -W);
-                    ok = ao_fast_groups<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
-                } else {
-                    ok = ao_fast_groups<false>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
+                t_end = lo;
+                lo = 1;
+                hi = t_end;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    const float tf = small_u2f((uint32_t)mid);
+                    const float mx = __fadd_rn(pxf, __fmul_rn(dX, tf)), my = __fadd_rn(pyf, __fmul_rn(dY, tf));
+                    if (mx >= 0.0f && my >= 0.0f)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
                 }
-                t = 2 + 4 * n_groups;
+                t_fast = lo;
             }
-            for (; ok && t < t_end; t++) ok = ao_tap_exact(t, pxf, pyf, dX, dY, W, H, P.depth, z, best, best);
-            if (!ok) {
-                nanpix = true;
-                break;
+        }
+        // the padding taps 100, 101 read the pixel itself: elev 0 needs a finite depth
+        if (!P.dir_fast[k] || !isfinite(z)) t_fast = 1;
+        float best = 0.0f;
+        bool ok = true;
+        if (t_end > 1) ok = ao_tap_exact(1, pxf, pyf, dX, dY, W, H, P.depth, z, 0.0f, best);
+        int t = 2;
+        if (ok && t_fast > 2) {
+            const int n_groups = t_fast == kAoTaps ? kAoTable / 4 : (t_fast - 2) >> 2;
+            const int tiny = P.dir_tiny[k];
+            if (tiny) {
+                // t*: first tap with |a| above half the gap below the coordinate
+                const float cf = fabsf(tiny == 1 ? dX : dY);
+                const uint32_t vb = __float_as_uint(tiny == 1 ? pxf : pyf);
+                const float h = __uint_as_float(((vb >> 23) - ((vb & 0x7fffffu) ? 24u : 25u)) << 23);
+                int lo = 1, hi = kAoTaps;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__fmul_rn(cf, small_u2f((uint32_t)mid)) > h)
+                        hi = mid;
+                    else
+                        lo = mid + 1;
+                }
+                const float* pA = p0 + (tiny == 1 ? 1 : -W);
+                ok = ao_fast_groups<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
+            } else {
+                ok = ao_fast_groups<false>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
             }
-            const float ma = best > 0.0f ? atan_f32(best) : 0.0f;
-            total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));  // HalfPi - angle
+            t = 2 + 4 * n_groups;
         }
-        const float T = nanpix ? __uint_as_float(0x7fc00000u) : __fdiv_rn(total, 12.5663706143591729539f);
-        const uchar4 c = P.rgba[i];
-        if (P.dgb) {
-            // float32(Pow(T, 10000)) as a fixed factor of the differentiable radiance (0 for NaN, as the
-            // reference's uint8(NaN) darkens the pixel)
-            const float fa = isnan(T) ? 0.0f : (T == 1.0f ? 1.0f : powf(T, 10000.0f));
-            P.dgb[4 * i].w *= fa;
+        for (; ok && t < t_end; t++) ok = ao_tap_exact(t, pxf, pyf, dX, dY, W, H, P.depth, z, best, best);
+        if (!ok) {
+            nanpix = true;
+            break;
         }
-        uint3 o = ao_scale(T, c.x, c.y, c.z);
-        if (P.gamma_on) {
-            o.x = P.gamma[o.x];
-            o.y = P.gamma[o.y];
-            o.z = P.gamma[o.z];
+        const float ma = best > 0.0f ? atan_f32(best) : 0.0f;
+        total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));  // HalfPi - angle
+    }
+    const float T = nanpix ? __uint_as_float(0x7fc00000u) : __fdiv_rn(total, 12.5663706143591729539f);
+    const uchar4 c = P.rgba[i];
+    if (P.dgb) {
+        // float32(Pow(T, 10000)) as a fixed factor of the differentiable radiance (0 for NaN, as the
+        // reference's uint8(NaN) darkens the pixel)
+        const float fa = isnan(T) ? 0.0f : (T == 1.0f ? 1.0f : powf(T, 10000.0f));
+        P.dgb[4 * i].w *= fa;
+    }
+    uint3 o = ao_scale(T, c.x, c.y, c.z);
+    if (P.gamma_on) {
+        o.x = P.gamma[o.x];
+        o.y = P.gamma[o.y];
+        o.z = P.gamma[o.z];
+    }
+    P.rgba[i] = make_uchar4(o.x, o.y, o.z, c.w);
+}
+
+__global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant__ AoParams P) {
+    __shared__ __align__(16) int s_off[8][kAoTable];
+    __shared__ __align__(16) float s_rlo[8][kAoTable];
+    __shared__ __align__(16) float s_rhi[8][kAoTable];
+    const uint32_t n = P.cnt->n_ao;
+    if (blockIdx.x * blockDim.x >= n) return;  // whole block: no pixel of the list
+    ao_tables(P, s_off, s_rlo, s_rhi);
+    __syncthreads();
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        ao_one(P, j, s_off, s_rlo, s_rhi);
+}
+
+// ---------------------------------------------------------------- batches
+
+// The job owning launch block (or item) b: the largest j with start[j] <= b.
+PR_DEV int job_of(const uint32_t* start, int n_jobs, uint32_t b) {
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(128) setup_shadow_batch_kernel(const SetupParams* jobs, const uint32_t* blk, int n_jobs) {
+    const int j = job_of(blk, n_jobs, blockIdx.x);
+    setup_shadow_one(jobs[j], (blockIdx.x - blk[j]) * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(128) setup_main_batch_kernel(const SetupParams* jobs, const uint32_t* blk, int n_jobs) {
+    const int j = job_of(blk, n_jobs, blockIdx.x);
+    setup_main_one(jobs[j], (blockIdx.x - blk[j]) * blockDim.x + threadIdx.x, jobs[j].clip_list);
+}
+__global__ void __launch_bounds__(128) clip_batch_kernel(const SetupParams* jobs, const uint32_t* blk, int n_jobs) {
+    const int j = job_of(blk, n_jobs, blockIdx.x);
+    const SetupParams& P = jobs[j];
+    const uint32_t n = P.cnt->n_clipped;
+    const uint32_t b0 = (blockIdx.x - blk[j]) * blockDim.x;
+    if (b0 >= n) return;  // whole block idle
+    clip_one(P, P.clip_list, b0 + threadIdx.x, n);
+}
+
+// items[j] = warp batches before pass j (one block; a chained scan in
+// chunks of its 1024 threads).
+__global__ void __launch_bounds__(1024) batch_scan_kernel(const RasterParams* jobs, int n_jobs, uint32_t* items,
+                                                          uint32_t* queue, int fixup) {
+    __shared__ uint32_t s[1024];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        *queue = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < n_jobs; base += blockDim.x) {
+        const int j = base + threadIdx.x;
+        uint32_t v = 0;
+        if (j < n_jobs) {
+            const Counters* c = jobs[j].cnt;
+            const bool run = !c->overflow && (!fixup || c->nan_flag);
+            v = run ? (c->n_tasks + 31u) >> 5 : 0u;
         }
-        P.rgba[i] = make_uchar4(o.x, o.y, o.z, c.w);
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int d = 1; d < (int)blockDim.x; d <<= 1) {
+            const uint32_t t = threadIdx.x >= (unsigned)d ? s[threadIdx.x - d] : 0u;
+            __syncthreads();
+            s[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (j < n_jobs) items[j] = carry + s[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += s[threadIdx.x];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) items[n_jobs] = carry;
+}
+
+// Persistent raster over every pass of a batch: each warp takes the next
+// (pass, warp batch) item from the global queue.
+__global__ void __launch_bounds__(kRasterWarps * 32) raster_batch_kernel(const RasterParams* jobs, const uint32_t* items,
+                                                                         int n_jobs, uint32_t* queue) {
+    __shared__ SmRec s_rec[kRasterWarps][32];
+    __shared__ int s_start[kRasterWarps][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t total = items[n_jobs];
+    for (;;) {
+        uint32_t it = 0;
+        if (lane == 0) it = atomicAdd(queue, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= total) break;
+        const int j = job_of(items, n_jobs, it);
+        const RasterParams& P = jobs[j];
+        raster_warp(P, (it - items[j]) * 32u, P.cnt->n_tasks, s_rec[warp], s_start[warp]);
+    }
+}
+
+__global__ void resolve_batch_kernel(const ResolveParams* jobs, const uint32_t* blk, int n_jobs) {
+    const int j = job_of(blk, n_jobs, blockIdx.x);
+    const ResolveParams& R = jobs[j];
+    resolve_one(R.W, R.H, R.keys, R.nanseq, R.beaten, R.cnt, R.win, R.depth_ao,
+                (size_t)(blockIdx.x - blk[j]) * blockDim.x + threadIdx.x);
+}
+
+// 256-thread blocks as 32 x 8 pixel tiles, row-major over each view's tiles.
+__global__ void __launch_bounds__(256) shade_batch_kernel(const ShadeParams* views, const uint32_t* blk, int n_views) {
+    const int v = job_of(blk, n_views, blockIdx.x);
+    const ShadeParams& P = views[v];
+    const uint32_t b = blockIdx.x - blk[v], tiles_x = (uint32_t)(P.W + 31) / 32u;
+    const uint32_t ty = b / tiles_x, tx = b - ty * tiles_x;
+    shade_one(P, (int)(tx * 32u + (threadIdx.x & 31u)), (int)(ty * 8u + (threadIdx.x >> 5)));
+}
+
+// Persistent AO over every view's list, in chunks of one block taken from
+// per-view counters; tap tables rebuilt when the frame size changes.
+__global__ void __launch_bounds__(kAoThreads) ao_batch_kernel(const AoParams* views, int n_views,
+                                                                uint32_t* chunk_ctr) {
+    __shared__ __align__(16) int s_off[8][kAoTable];
+    __shared__ __align__(16) float s_rlo[8][kAoTable];
+    __shared__ __align__(16) float s_rhi[8][kAoTable];
+    __shared__ uint32_t s_chunk;
+    int tab_w = -1, tab_dirs = -1;
+    float tab_h = -1.0f;
+    for (int v = 0; v < n_views; v++) {
+        const AoParams& P = views[v];
+        const uint32_t n = P.cnt->n_ao;
+        if (n == 0) continue;
+        if (P.W != tab_w || P.ao_half_ulp != tab_h || P.n_dirs != tab_dirs) {
+            __syncthreads();
+            ao_tables(P, s_off, s_rlo, s_rhi);
+            __syncthreads();
+            tab_w = P.W;
+            tab_h = P.ao_half_ulp;
+            tab_dirs = P.n_dirs;
+        }
+        for (;;) {
+            if (threadIdx.x == 0) s_chunk = atomicAdd(&chunk_ctr[v], 1u);
+            __syncthreads();
+            const uint32_t c = s_chunk;
+            __syncthreads();
+            if (c * blockDim.x >= n) break;
+            const uint32_t j = c * blockDim.x + threadIdx.x;
+            if (j < n) ao_one(P, j, s_off, s_rlo, s_rhi);
+        }
     }
 }
 
@@ -1184,6 +1350,44 @@ int launch_shade(const ShadeParams& p, void* stream) {
     dim3 blk(32, 8);
     dim3 grd((p.W + 31) / 32, (p.H + 7) / 8);
     shade_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_setup_shadow_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream) {
+    if (n_blocks == 0) return 0;
+    setup_shadow_batch_kernel<<<n_blocks, 128, 0, (cudaStream_t)stream>>>(jobs, blk, n_jobs);
+    return check(cudaGetLastError());
+}
+int launch_setup_main_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream) {
+    if (n_blocks == 0) return 0;
+    setup_main_batch_kernel<<<n_blocks, 128, 0, (cudaStream_t)stream>>>(jobs, blk, n_jobs);
+    return check(cudaGetLastError());
+}
+int launch_clip_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream) {
+    if (n_blocks == 0) return 0;
+    clip_batch_kernel<<<n_blocks, 128, 0, (cudaStream_t)stream>>>(jobs, blk, n_jobs);
+    return check(cudaGetLastError());
+}
+int launch_batch_scan(const RasterParams* jobs, int n_jobs, uint32_t* items, uint32_t* queue, int fixup, void* stream) {
+    batch_scan_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(jobs, n_jobs, items, queue, fixup);
+    return check(cudaGetLastError());
+}
+int launch_raster_batch(const RasterParams* jobs, const uint32_t* items, int n_jobs, uint32_t* queue, int n_blocks,
+                        void* stream) {
+    raster_batch_kernel<<<n_blocks, kRasterWarps * 32, 0, (cudaStream_t)stream>>>(jobs, items, n_jobs, queue);
+    return check(cudaGetLastError());
+}
+int launch_resolve_batch(const ResolveParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream) {
+    if (n_blocks == 0) return 0;
+    resolve_batch_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(jobs, blk, n_jobs);
+    return check(cudaGetLastError());
+}
+int launch_shade_batch(const ShadeParams* views, const uint32_t* blk, int n_views, uint32_t n_blocks, void* stream) {
+    if (n_blocks == 0) return 0;
+    shade_batch_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(views, blk, n_views);
+    return check(cudaGetLastError());
+}
+int launch_ao_batch(const AoParams* views, int n_views, uint32_t* chunk_ctr, int n_blocks, void* stream) {
+    ao_batch_kernel<<<n_blocks, kAoThreads, 0, (cudaStream_t)stream>>>(views, n_views, chunk_ctr);
     return check(cudaGetLastError());
 }
 int launch_ao(const AoParams& p, void* stream) {

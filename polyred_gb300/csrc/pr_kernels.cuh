@@ -14,7 +14,7 @@ namespace prk {
 
 constexpr int kMaxLights = 16;
 constexpr int kMaxAmbient = 16;
-constexpr int kTaskPx = 1024;        // pixels of one raster task (a bbox chunk)
+constexpr uint32_t kTaskShift = 10;  // a raster task is a 2^kTaskShift-pixel chunk of a bbox (default)
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
 // Raster record: what the coverage/depth test of one (sub-)triangle needs.
@@ -88,6 +88,8 @@ struct SetupParams {
     uint32_t* first_rec;
     Counters* cnt;
     float* tri_scr;              // differentiation only: [n_tris][12] screen x, y, recipw per vertex
+    uint32_t task_shift = kTaskShift;  // log2 pixels per raster task (<= 16)
+    uint32_t* clip_list;         // batched main setup: this view's clip list
 };
 
 enum RasterMode { kMain = 0, kMainFixup = 1, kShadow = 2, kShadowFixup = 3 };
@@ -104,6 +106,7 @@ struct RasterParams {
     uint32_t* beaten;          // main fix-up: 1 if a finite fragment precedes nanseq
     uint32_t* smap;            // shadow: orderable depth keys, index x + y*W
     uint32_t* lastnan;         // shadow: 1 + max seq of NaN-depth fragments, 0 if none
+    uint32_t task_shift = kTaskShift;  // as the setup that wrote the tasks
 };
 
 struct ShadeParams {
@@ -202,6 +205,31 @@ int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* s
 int launch_shade(const ShadeParams& p, void* stream);
 int launch_ao(const AoParams& p, void* stream);
 int launch_diff(const DiffParamsK& p, bool backward, void* stream);
+
+// ---- batches: many passes (views, shadow maps) per launch ----
+struct ResolveParams {
+    int W, H;
+    const unsigned long long* keys;
+    const uint32_t* nanseq;
+    const uint32_t* beaten;
+    const Counters* cnt;
+    uint32_t* win;
+    float* depth_ao;
+};
+// Job j of a launch owns blocks [blk[j], blk[j+1]); blk has n_jobs + 1 entries.
+int launch_setup_shadow_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream);
+int launch_setup_main_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream);
+int launch_clip_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream);
+// Per-pass work items (warp batches of 32 tasks) prefixed into items[n_jobs + 1]
+// on the device; fixup: only passes with NaN fragments. Also clears *queue.
+int launch_batch_scan(const RasterParams* jobs, int n_jobs, uint32_t* items, uint32_t* queue, int fixup, void* stream);
+// One persistent launch over the global queue of (pass, warp batch) items.
+int launch_raster_batch(const RasterParams* jobs, const uint32_t* items, int n_jobs, uint32_t* queue, int n_blocks,
+                        void* stream);
+int launch_resolve_batch(const ResolveParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream);
+int launch_shade_batch(const ShadeParams* views, const uint32_t* blk, int n_views, uint32_t n_blocks, void* stream);
+// Persistent; chunk counters [n_views] zeroed by the caller.
+int launch_ao_batch(const AoParams* views, int n_views, uint32_t* chunk_ctr, int n_blocks, void* stream);
 int launch_col_to_float(const uchar4* col, float4* out, size_t n, void* stream);
 int launch_fill_u32(uint32_t* p, uint32_t v, size_t n, void* stream);
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);

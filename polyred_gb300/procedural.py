@@ -131,11 +131,9 @@ def small_scene(width=800, height=500):
     return s, cam
 
 
-def sphere_field(n_spheres=256, lon=63, lat=32, seed=0x5EED0002, width=1920, height=1080, ao=True,
-                 directional_shadow=True):
-    """The 1M-triangle workload: 256 spheres of 3,906 triangles each."""
-    rng = Xoshiro128(seed)
-    materials = [
+def sphere_materials(ao=True):
+    """The four Blinn-Phong materials of the sphere field."""
+    return [
         sc.BlinnPhong(diffuse=sc.color_from_value(0.8, 0.3, 0.2), specular=sc.color_from_value(0.5, 0.5, 0.5),
                       shininess=32, ambient_occlusion=ao, receive_shadow=True),
         sc.BlinnPhong(diffuse=sc.color_from_value(0.2, 0.5, 0.8), specular=sc.color_from_value(0.5, 0.5, 0.5),
@@ -145,6 +143,13 @@ def sphere_field(n_spheres=256, lon=63, lat=32, seed=0x5EED0002, width=1920, hei
         sc.BlinnPhong(diffuse=sc.color_from_value(0.9, 0.9, 0.9), specular=sc.color_from_value(0.5, 0.5, 0.5),
                       shininess=8, ambient_occlusion=ao, receive_shadow=True),
     ]
+
+
+def sphere_field(n_spheres=256, lon=63, lat=32, seed=0x5EED0002, width=1920, height=1080, ao=True,
+                 directional_shadow=True):
+    """The 1M-triangle workload: 256 spheres of 3,906 triangles each."""
+    rng = Xoshiro128(seed)
+    materials = sphere_materials(ao)
     mesh = uv_sphere(lon, lat, 1.0)
     objs = []
     for _ in range(n_spheres):
