@@ -251,6 +251,90 @@ def measure_diff(dev, steps, adam_steps=0):
     return out
 
 
+def measure_batch(reps=3):
+    """The batched workload (32 sphere scenes of 1k-500k triangles, 8 ring
+    views each at 1280x720, 16 casting point lights per scene with 1024^2
+    maps, AO on): views/s of one tuned pr_batch_render against the same 256
+    views rendered one pr_render_async at a time on one context per scene."""
+    import torch
+    from polyred_gb300 import _abi, batch as pb, native, render
+    scenes, specs = pb.config4()
+    b = pb.Batch(0)
+    for s in scenes:
+        b.add_scene(s)
+    arr, outs, keep = b.views(specs, ("rgba",))
+    tune = b.tune(arr)
+    times = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.render(arr)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    st = b.stats()
+    bt = min(times)
+    b.close()
+    del outs, keep
+    # plain: one context per scene, one frame per view (first-frame shadow maps)
+    lib = native.load()
+    devs = []
+    for s in scenes:
+        d = render.Device(0)
+        fl = render.FlatScene(s)
+        desc = fl.desc()
+        native.check(lib.pr_scene_upload(d.handle, C.byref(desc)))
+        devs.append(d)
+    fds, ods, bufs = [], [], []
+    for si, opts, cams in specs:
+        fd = render.FrameDesc(opts, cams)
+        t = torch.empty((opts["height"], opts["width"], 4), dtype=torch.uint8, device="cuda")
+        od = _abi.pr_outputs()
+        od.size = C.sizeof(_abi.pr_outputs)
+        od.flags = _abi.PR_OUT_DEVICE_PTRS
+        od.rgba = t.data_ptr()
+        fds.append(fd)
+        ods.append(od)
+        bufs.append(t)
+
+    def plain_pass():
+        for (si, _, _), fd, od in zip(specs, fds, ods):
+            native.check(lib.pr_shadow_reset(devs[si].handle))
+            native.check(lib.pr_render_async(devs[si].handle, C.byref(fd.desc), C.byref(od)))
+        for d in devs:
+            native.check(lib.pr_sync(d.handle))
+
+    for (si, _, _), fd, od in zip(specs, fds, ods):  # warm-up: synchronous frames size the buffers
+        native.check(lib.pr_shadow_reset(devs[si].handle))
+        native.check(lib.pr_render(devs[si].handle, C.byref(fd.desc), C.byref(od)))
+    pt, ps = [], []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plain_pass()
+        torch.cuda.synchronize()
+        pt.append(time.perf_counter() - t0)
+    for _ in range(reps):  # one synchronous Render() per view
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for (si, _, _), fd, od in zip(specs, fds, ods):
+            native.check(lib.pr_shadow_reset(devs[si].handle))
+            native.check(lib.pr_render(devs[si].handle, C.byref(fd.desc), C.byref(od)))
+        torch.cuda.synchronize()
+        ps.append(time.perf_counter() - t0)
+    for d in devs:
+        d.close()
+    n = len(specs)
+    return {"workload": "32 sphere scenes (1k-500k tris, log-uniform) x 8 views 1280x720, 16 casting point lights, "
+                        "1024^2 maps, AO", "n_views": n, "n_tris_total": int(sum(render.FlatScene(s).n_tris
+                                                                                    for s in scenes)),
+            "n_passes": st["n_passes"], "batched_views_per_s": n / bt, "plain_views_per_s": n / min(ps),
+            "batched_over_plain": min(ps) / bt, "plain": "one synchronous pr_render per view",
+            "plain_async_views_per_s": n / min(pt), "batched_over_plain_async": min(pt) / bt,
+            "plain_async": "pr_render_async per view, one context and stream per scene",
+            "batched_ms": bt * 1e3, "batched_device_ms": st["ms_total"], "plain_ms": min(ps) * 1e3, "kernel_launches_per_batch": st["n_kernel_launches"],
+            "graph_reused": st["graph_reused"], "device_gb": st["device_bytes"] / 1e9, "tuned": tune}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -260,6 +344,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-shading measurement")
     ap.add_argument("--adam", type=int, default=0, help="also run this many Adam steps over 16 views")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-views measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -398,6 +483,8 @@ def main():
                 "clocks": clk}
         if not args.no_diff:
             line["diff"] = measure_diff(dev, args.steps, args.adam)
+        if not args.no_batch:
+            line["batched"] = measure_batch()
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line), flush=True)

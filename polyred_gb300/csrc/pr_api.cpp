@@ -958,6 +958,15 @@ int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params
     return PR_OK;
 }
 
+// Test hook (not part of the public header): the shade kernel's float32 Pow
+// beside the float64 algorithm on n device-resident argument pairs.
+int pr_debug_pow_probe(const float* x, const float* y, float* fast, float* ref, int n) {
+    int e = prk::launch_pow_probe(x, y, fast, ref, n, nullptr);
+    if (e) return fail(PR_ERR_CUDA, "pow probe launch: %s", cudaGetErrorString((cudaError_t)e));
+    CUDA_TRY(cudaDeviceSynchronize());
+    return PR_OK;
+}
+
 // Test hook (not part of the public header): the AO kernel's float32 Atan
 // and its certified Pow(T, 10000) colour scaling, each beside the float64
 // algorithm, on n device-resident inputs (col, o_fast, o_ref: 4 bytes each).

@@ -343,6 +343,88 @@ PR_DEV float atan_f32(float x) {
     return __double2float_rn(go_atan((double)x));
 }
 
+// float32(Go math.Pow(float64(x), float64(y))) (math/pow.go), as the
+// specular term of shader/blinn_cpu.go:86 needs it. For 0 < x < 1 and an
+// integer 2 <= y <= 4096, Go runs binary exponentiation on the frexp
+// mantissa of x; that runs here on float32 pairs (hi + lo, products by
+// fmaf, each within 2^-45 relative), with the binary exponent kept apart.
+// Squaring doubles a relative error, so X^(2^k) is within (2^k - 1) 2^-45
+// and the product within y 2^-45 of x^y; Go's float64 result is within
+// y 2^-53 of it. When the interval y 2^-44 around the pair lies strictly
+// inside one float32 rounding interval (normal or subnormal), the rounding
+// is decided; otherwise, and for other arguments, the float64 algorithm
+// runs. Go's early exit for |exponent| > 4096 only occurs for results far
+// below the float32 range, which round to 0 here as there.
+struct DF { float hi, lo; };
+PR_DEV DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const float h = __fadd_rn(p, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+PR_DEV float go_pow_f32(float x, float y) {
+    const bool yint = y >= 0.0f && y <= 4096.0f && __fsub_rn(__fadd_rz(y, 8388608.0f), 8388608.0f) == y;
+    if (yint && x > 0.0f && x < 1.0f && y >= 2.0f && x >= 0x1p-60f) {
+        uint32_t n = __float_as_uint(__fadd_rz(y, 8388608.0f)) - 0x4B000000u;
+        const float ny = y;
+        // frexp: x = m 2^xe, m in [0.5, 1)
+        const uint32_t xb = __float_as_uint(x);
+        int xe = (int)(xb >> 23) - 126;
+        DF X = {__uint_as_float((xb & 0x807fffffu) | 0x3f000000u), 0.0f};
+        DF a = {1.0f, 0.0f};
+        int ae = 0;
+        for (; n != 0; n >>= 1) {
+            if (n & 1u) {
+                a = df_mul(a, X);
+                ae += xe;
+                if (a.hi < 0.5f) {
+                    a.hi = __fmul_rn(a.hi, 2.0f);
+                    a.lo = __fmul_rn(a.lo, 2.0f);
+                    ae--;
+                }
+            }
+            if (n == 1u) break;
+            X = df_mul(X, X);
+            xe <<= 1;
+            if (X.hi < 0.5f) {
+                X.hi = __fmul_rn(X.hi, 2.0f);
+                X.lo = __fmul_rn(X.lo, 2.0f);
+                xe--;
+            }
+        }
+        // value (a.hi + a.lo) 2^ae with a.hi in [0.5, 1], |a.lo| <= ulp(a.hi) / 2
+        const float tol = __fmul_ru(__fmul_ru(a.hi, ny), 0x1p-44f);
+        if (ae >= -125) {
+            // normal: a.hi 2^ae is a float32; it is the rounding if the error interval stays inside
+            const uint32_t hb = __float_as_uint(a.hi);
+            const float hu = __uint_as_float(((hb >> 23) - 24u) << 23);                             // half ulp above
+            const float hd = (hb & 0x7fffffu) ? hu : __uint_as_float(((hb >> 23) - 25u) << 23);     // half gap below
+            if (__fadd_ru(a.lo, tol) < hu && __fsub_rd(a.lo, tol) > -hd)
+                return __uint_as_float((uint32_t)((int)(hb >> 23) + ae) << 23 | (hb & 0x7fffffu));
+        } else if (ae >= -149 - 24) {
+            // subnormal or zero: q = value / 2^-149 (< 2^23), rounded to an integer
+            const float sc = __uint_as_float((uint32_t)(ae + 149 + 127) << 23);
+            const float qh = __fmul_rn(a.hi, sc), ql = __fmul_rn(a.lo, sc), qt = __fmul_ru(tol, sc);
+            const float qi = __fsub_rn(__fadd_rn(qh, 8388608.0f), 8388608.0f);  // RN(qh), qh < 2^23
+            const float r = __fadd_rn(__fsub_rn(qh, qi), ql);                    // qh - qi exact
+            if (__fadd_ru(fabsf(r), qt) < 0.5f) return __uint_as_float(__float_as_uint(__fadd_rn(qi, 8388608.0f)) - 0x4B000000u);
+        } else {
+            if (ae < -149 - 26) return 0.0f;  // below 2^-151 (a.hi <= 1): rounds to +0
+        }
+    }
+    if (y == 0.0f || x == 1.0f) return 1.0f;
+    if (y == 1.0f) return x;
+    if (x == 0.0f && y > 0.0f && y < 8388608.0f) {
+        // Pow(+-0, y) = +-0 for an odd integer y > 0, else +0
+        const float t = __fadd_rz(y, 8388608.0f);
+        const bool odd = __fsub_rn(t, 8388608.0f) == y && (__float_as_uint(t) & 1u) != 0u;
+        return (odd && signbit(x)) ? x : 0.0f;
+    }
+    return __double2float_rn(go_pow((double)x, (double)y));
+}
+
 // The three colour channels of material/ao.go:34-37 after
 // total = math.Pow(T, 10000): uint8(float32(Pow(T, 10000)) * float32(ch)).
 // Pow runs in float32 with a certified error bound, and its float64 form only

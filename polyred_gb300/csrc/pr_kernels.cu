@@ -785,7 +785,6 @@ PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
                 float LdR = 0, LdG = 0, LdB = 0, LsR = 0, LsG = 0, LsB = 0;
                 const V4 nn = (mat->flags & PR_MAT_FLAT_SHADING) ? fn : n;
                 const V4 cam = {P.cam[0], P.cam[1], P.cam[2], 1.0f};
-                const double shin = (double)mat->shininess;
                 for (int li = 0; li < P.n_lights; li++) {
                     const LightK& L = P.lights[li];
                     V4 Lv;
@@ -801,7 +800,7 @@ PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
                     V4 Vv = unit4(sub4(cam, wp));
                     V4 Hv = unit4(add4(Lv, Vv));
                     float Ld = pclamp(dot4(nn, Lv), 0.0f, 1.0f);
-                    float Ls = __double2float_rn(go_pow((double)pclamp(dot4(nn, Hv), 0.0f, 1.0f), shin));
+                    float Ls = go_pow_f32(pclamp(dot4(nn, Hv), 0.0f, 1.0f), mat->shininess);
                     LdR = __fadd_rn(LdR, __fmul_rn(__fmul_rn(Ld, cr), I));
                     LdG = __fadd_rn(LdG, __fmul_rn(__fmul_rn(Ld, cg), I));
                     LdB = __fadd_rn(LdB, __fmul_rn(__fmul_rn(Ld, cb), I));
@@ -1287,6 +1286,13 @@ __global__ void __launch_bounds__(kAoThreads) ao_batch_kernel(const AoParams* vi
     }
 }
 
+__global__ void pow_probe_kernel(const float* x, const float* y, float* fast, float* ref, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    fast[i] = go_pow_f32(x[i], y[i]);
+    ref[i] = __double2float_rn(go_pow((double)x[i], (double)y[i]));
+}
+
 __global__ void ao_probe_kernel(const float* x, float* atan_fast, float* atan_ref, const float* T, const uchar4* col,
                                 uchar4* o_fast, uchar4* o_ref, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1412,6 +1418,11 @@ int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream) {
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream) {
     if (n == 0) return 0;
     decode_shadow_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(smap, out, n);
+    return check(cudaGetLastError());
+}
+int launch_pow_probe(const float* x, const float* y, float* fast, float* ref, int n, void* stream) {
+    if (n <= 0) return 0;
+    pow_probe_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x, y, fast, ref, n);
     return check(cudaGetLastError());
 }
 int launch_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const void* col, void* o_fast,

@@ -234,6 +234,7 @@ int launch_col_to_float(const uchar4* col, float4* out, size_t n, void* stream);
 int launch_fill_u32(uint32_t* p, uint32_t v, size_t n, void* stream);
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
+int launch_pow_probe(const float* x, const float* y, float* fast, float* ref, int n, void* stream);
 int launch_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const void* col, void* o_fast,
                     void* o_ref, int n, void* stream);
 int launch_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n,

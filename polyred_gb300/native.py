@@ -41,6 +41,8 @@ def load(build_if_missing=False):
     except OSError as e:
         raise NativeUnavailable(f"cannot load {LIB_PATH}: {e}") from e
     _abi.bind(lib)
+    lib.pr_debug_pow_probe.restype = C.c_int
+    lib.pr_debug_pow_probe.argtypes = [C.c_void_p] * 4 + [C.c_int]
     lib.pr_debug_ao_probe.restype = C.c_int
     lib.pr_debug_ao_probe.argtypes = [C.c_void_p] * 7 + [C.c_int]
     lib.pr_debug_fma_probe.restype = C.c_int

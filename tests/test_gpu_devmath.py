@@ -85,3 +85,28 @@ def test_ao_atan_and_pow_shortcuts(native_lib):
     assert np.array_equal(af.view(np.uint32), ar.view(np.uint32)), int((af != ar).sum())
     bad = np.flatnonzero((of != orf).any(1))
     assert len(bad) == 0, (len(bad), T[bad[:4]], col[bad[:4]], of[bad[:4]], orf[bad[:4]])
+
+
+def test_pow_float32_matches_float64(native_lib):
+    """The shade kernel's Pow (float32 pairs with a certified rounding)
+    against the float64 algorithm: shininess exponents, arguments across
+    (0, 1] including tiny ones (subnormal and zero results), zeros, ones,
+    and non-integer exponents (float64 path)."""
+    import torch
+    g = np.random.default_rng(13)
+    n = 1 << 20
+    x = np.concatenate([
+        g.uniform(0, 1, n // 4),
+        1 - np.exp(g.uniform(np.log(1e-8), np.log(0.5), n // 4)),
+        np.exp(g.uniform(np.log(1e-30), 0, n // 4)),
+        np.float32([0.0, -0.0, 1.0, 0.5, 0.25, 2.0 ** -60, 2.0 ** -59, 0.9999999]),
+    ]).astype(np.float32)
+    x = np.concatenate([x, g.uniform(0, 1, n - len(x))]).astype(np.float32)
+    ys = np.float32([1, 2, 3, 4, 5, 7, 8, 12, 16, 31, 32, 33, 50, 64, 100, 128, 255, 1000, 4096, 0, 12.5, 4097])
+    y = ys[g.integers(0, len(ys), n)].astype(np.float32)
+    tx, ty = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    f, r = torch.empty_like(tx), torch.empty_like(tx)
+    assert native_lib.pr_debug_pow_probe(tx.data_ptr(), ty.data_ptr(), f.data_ptr(), r.data_ptr(), n) == 0
+    f, r = f.cpu().numpy(), r.cpu().numpy()
+    bad = np.flatnonzero(f.view(np.uint32) != r.view(np.uint32))
+    assert len(bad) == 0, (len(bad), x[bad[:4]], y[bad[:4]], f[bad[:4]], r[bad[:4]])
