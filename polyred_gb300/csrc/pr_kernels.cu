@@ -785,19 +785,22 @@ PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
                 float LdR = 0, LdG = 0, LdB = 0, LsR = 0, LsG = 0, LsB = 0;
                 const V4 nn = (mat->flags & PR_MAT_FLAT_SHADING) ? fn : n;
                 const V4 cam = {P.cam[0], P.cam[1], P.cam[2], 1.0f};
+                const V4 Vv = unit4(sub4(cam, wp));  // the same for every light
                 for (int li = 0; li < P.n_lights; li++) {
                     const LightK& L = P.lights[li];
                     V4 Lv;
                     float I;
                     if (L.type == PR_LIGHT_POINT) {
-                        V4 Ldir = sub4(V4{L.pos[0], L.pos[1], L.pos[2], 1.0f}, wp);
-                        Lv = unit4(Ldir);
-                        I = __fdiv_rn(L.intensity, len4(Ldir));
+                        const V4 Ldir = sub4(V4{L.pos[0], L.pos[1], L.pos[2], 1.0f}, wp);
+                        // Ldir.Unit() and Ldir.Len() share one length
+                        const float ln = len4(Ldir);
+                        const float inv = __fdiv_rn(1.0f, ln);
+                        Lv = V4{__fmul_rn(Ldir.x, inv), __fmul_rn(Ldir.y, inv), __fmul_rn(Ldir.z, inv), __fmul_rn(Ldir.w, inv)};
+                        I = __fdiv_rn(L.intensity, ln);
                     } else {
                         Lv = V4{-L.dir[0], -L.dir[1], -L.dir[2], 0.0f};
                         I = L.intensity;
                     }
-                    V4 Vv = unit4(sub4(cam, wp));
                     V4 Hv = unit4(add4(Lv, Vv));
                     float Ld = pclamp(dot4(nn, Lv), 0.0f, 1.0f);
                     float Ls = go_pow_f32(pclamp(dot4(nn, Hv), 0.0f, 1.0f), mat->shininess);
@@ -822,14 +825,15 @@ PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
             if ((P.flags & PR_FRAME_SHADOWMAP) && (mat->flags & PR_MAT_RECEIVE_SHADOW)) {
                 int occl = 0;
                 const size_t plane = (size_t)P.SW * P.SH;
+                // ViewportToWorld of the pixel, the same for every light
+                const V4 ws = apply4(V4{small_u2f((uint32_t)x), small_u2f((uint32_t)y), z, 1.0f}, P.s2w);
                 for (int li = 0; li < P.n_lights; li++) {
                     const LightK& L = P.lights[li];
                     if (!L.cast) {
                         occl++;
                         continue;
                     }
-                    V4 sc = pos4(apply4(apply4(apply4(apply4(V4{small_u2f((uint32_t)x), small_u2f((uint32_t)y), z, 1.0f}, P.s2w), L.lview), L.lproj),
-                                        P.shadow_vp));
+                    V4 sc = pos4(apply4(apply4(apply4(ws, L.lview), L.lproj), P.shadow_vp));
                     long long lx = go_f2i(sc.x), ly = go_f2i(sc.y);
                     long long idx = (long long)((unsigned long long)lx + (unsigned long long)ly * (unsigned long long)(long long)P.SW);
                     if (idx > 0 && idx < (long long)plane) {
