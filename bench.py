@@ -268,6 +268,48 @@ def measure_diff(dev, steps, adam_steps=0):
     return out
 
 
+def measure_soup(steps=10, n_tris=10_000_000, width=3840, height=2160):
+    """The small-triangle stress workload: 10M soup triangles at 3840x2160
+    (log-normal areas around 1 px, 30% back-facing, one point light, no
+    shadows, gamma on), resident frames timed with CUDA events."""
+    import torch
+    from polyred_gb300 import _abi, native, procedural, render
+    s, cam = procedural.soup_scene(n_tris, width, height)
+    dev = render.Device(0)
+    lib = native.load()
+    flat = render.FlatScene(s)
+    desc = flat.desc()
+    native.check(lib.pr_scene_upload(dev.handle, C.byref(desc)))
+    opts = dict(width=width, height=height, camera=cam, scene=s, perspective=True, shadow_map=False, gamma=True,
+                background=(0, 0, 0, 0), shadow_size=None)
+    fd = render.FrameDesc(opts, {})
+    rgba = torch.empty((height, width, 4), dtype=torch.uint8, device="cuda")
+    od = _abi.pr_outputs()
+    od.size = C.sizeof(_abi.pr_outputs)
+    od.flags = _abi.PR_OUT_DEVICE_PTRS
+    od.rgba = rgba.data_ptr()
+    for _ in range(3):
+        native.check(lib.pr_render(dev.handle, C.byref(fd.desc), C.byref(od)))
+    stream = torch.cuda.ExternalStream(dev.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        native.check(lib.pr_render_async(dev.handle, C.byref(fd.desc), C.byref(od)))
+        native.check(lib.pr_sync(dev.handle))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    st = _abi.pr_stats()
+    st.size = C.sizeof(_abi.pr_stats)
+    native.check(lib.pr_frame_stats(dev.handle, C.byref(st)))
+    dev.close()
+    return {"workload": "triangle soup 10M at 3840x2160 (areas log-normal median 1 px, 30% back-facing)",
+            "n_tris": n_tris, "value": n_tris / (ms / 1e3) / 1e6, "unit": "Mtri/s", "ms_per_frame": ms,
+            "n_raster_tris": st.n_raster_tris, "ms_setup": st.ms_setup, "ms_raster": st.ms_raster,
+            "ms_shade": st.ms_shade}
+
+
 def measure_batch(reps=3):
     """The batched workload (32 sphere scenes of 1k-500k triangles, 8 ring
     views each at 1280x720, 16 casting point lights per scene with 1024^2
@@ -362,6 +404,7 @@ def main():
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-shading measurement")
     ap.add_argument("--adam", type=int, default=0, help="also run this many Adam steps over 16 views")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-views measurement")
+    ap.add_argument("--no-soup", action="store_true", help="skip the 10M-triangle 4K soup measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -492,6 +535,8 @@ def main():
                 "clocks": clk}
         if not args.no_diff:
             line["diff"] = measure_diff(dev, args.steps, args.adam)
+        if not args.no_soup:
+            line["soup_4k"] = measure_soup()
         if not args.no_batch:
             line["batched"] = measure_batch()
         if world == 1 and not args.no_cpu_baseline:

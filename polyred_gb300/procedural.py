@@ -241,3 +241,16 @@ def triangle_soup(n_tris, width, height, seed=0x5EED0003, back_fraction=0.30, fo
     col = g.integers(0, 256, (n_tris, 3, 4), dtype=np.uint8)
     col[..., 3] = 255
     return sc.Mesh(pos, nor, None, col, np.zeros(n_tris, np.int32))
+
+
+def soup_scene(n_tris, width, height, seed=0x5EED0003):
+    """The small-triangle stress workload: a triangle soup (triangle_soup)
+    with one Blinn-Phong material, one point light and ambient 0.1, seen by
+    the camera the soup was unprojected through; no shadows."""
+    mesh = triangle_soup(n_tris, width, height, seed=seed)
+    mat = sc.BlinnPhong(diffuse=sc.color_from_value(0.8, 0.3, 0.2, 1.0), specular=sc.color_from_value(0.5, 0.5, 0.5, 1.0),
+                        shininess=32)
+    s = sc.Scene(sc.Geometry(mesh, mat), sc.Point(position=(0, 5, 5)), sc.Ambient(intensity=0.1))
+    cam = sc.Perspective(position=(0, 0, 0), target=(0, 0, -1), up=(0, 1, 0), fov=60, aspect=width / height, near=0.1,
+                         far=120)
+    return s, cam

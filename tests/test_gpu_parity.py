@@ -257,3 +257,16 @@ def test_repeated_frames_are_deterministic(device):
     g2, _ = p.frame()
     assert_bitexact(g1, g2)
     assert_bitexact(g1, c1)
+
+
+def test_triangle_soup_full_size(device):
+    """The small-triangle stress workload at full size: 10M soup triangles
+    (log-normal areas around 1 px, 30% back-facing) at 3840x2160, bit-exact
+    with the oracle (threaded, identical to its single-thread order)."""
+    W, H = 3840, 2160
+    s, cam = procedural.soup_scene(10_000_000, W, H)
+    p = Pair(device, options(s, cam, W, H, gamma=True), outputs=("rgba", "tri_id", "depth", "nor", "mat_id"))
+    gpu, cpu = p.frame()
+    assert (cpu["tri_id"] != 0xFFFFFFFF).sum() > 0.5 * W * H
+    assert p.stats["n_raster_tris"] > 5_000_000
+    assert_bitexact(gpu, cpu)
