@@ -191,6 +191,12 @@ PR_DEV int sutherland_hodgman(const V4* in3, float w, float h, V4* out) {
     return n;
 }
 
+// Vec4.Apply kept out of line in the per-triangle setup kernels: a dozen
+// inlined copies of twelve emulated float64 FMAs each overflow the
+// instruction cache (no_instruction stalls dominated), one shared copy
+// does not.
+__device__ __noinline__ V4 apply4_outline(V4 v, const float* m) { return apply4(v, m); }
+
 // Build and store the records of one sub-triangle; returns its pixel area
 // (0 = nothing to raster) and writes its bbox words.
 PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, const SubVtx* v, const float* recipw,
@@ -228,7 +234,7 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
             A.uv[k * 2 + 1] = v[k].v;
             A.col[k] = v[k].col;
             // render/raster.go:467-469
-            m[k] = apply4(apply4(apply4(v[k].pos, P.viewport_inv), P.proj_inv), P.view_inv);
+            m[k] = apply4_outline(apply4_outline(apply4_outline(v[k].pos, P.viewport_inv), P.proj_inv), P.view_inv);
             A.m[k * 3 + 0] = m[k].x;
             A.m[k * 3 + 1] = m[k].y;
             A.m[k * 3 + 2] = m[k].z;
@@ -302,7 +308,7 @@ PR_DEV bool transform_main(const SetupParams& P, uint32_t t, SubVtx* v, float* r
     for (int k = 0; k < 3; k++) {
         const V4 cp = mulv(trans, p[k]);
         recipw[k] = P.perspective ? __fdiv_rn(-1.0f, cp.w) : 1.0f;
-        v[k].pos = pos4(apply4(cp, P.viewport));
+        v[k].pos = pos4(apply4_outline(cp, P.viewport));
     }
     // cullBackFace (render/cull.go:26-28)
     if (cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y), __fsub_rn(v[2].pos.x, v[0].pos.x),
@@ -314,7 +320,7 @@ PR_DEV bool transform_main(const SetupParams& P, uint32_t t, SubVtx* v, float* r
     const float* nm = P.obj_normal + o * 16;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        v[k].nor = apply4(ld4(P.nor[t * 3 + k]), nm);
+        v[k].nor = apply4_outline(ld4(P.nor[t * 3 + k]), nm);
         const float2 uv = P.uv[t * 3 + k];
         v[k].u = uv.x;
         v[k].v = uv.y;
@@ -430,7 +436,7 @@ PR_DEV void setup_shadow_one(const SetupParams& P, uint32_t t) {
             mulm(P.pv, P.obj_model + o * 16, trans);
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                v[k].pos = pos4(apply4(mulv(trans, p[k]), P.viewport));
+                v[k].pos = pos4(apply4_outline(mulv(trans, p[k]), P.viewport));
                 v[k].nor = {0, 0, 0, 0};
                 v[k].u = v[k].v = 0;
                 v[k].col = 0;
