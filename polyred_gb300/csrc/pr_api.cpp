@@ -89,6 +89,7 @@ struct Ctx {
     DevBuf<uchar4> col;
     DevBuf<int32_t> mat;
     DevBuf<uint32_t> obj_first;
+    DevBuf<uint8_t> tri_flags;  // Triangle.IsValid per input triangle
     DevBuf<float> obj_model, obj_normal;
     DevBuf<int32_t> obj_matbase;
     DevBuf<pr_material> dmats;
@@ -209,6 +210,7 @@ void fill_scene_ptrs(Ctx* c, prk::SetupParams& p) {
     p.obj_model = c->obj_model.p;
     p.obj_normal = c->obj_normal.p;
     p.obj_matbase = c->obj_matbase.p;
+    p.tri_flags = c->tri_flags.p;
     p.n_tris = c->n_tris;
     p.n_objects = (uint32_t)c->objects.size();
 }
@@ -630,6 +632,7 @@ int pr_destroy(void* ctx) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     c->pos.release(); c->nor.release(); c->uv.release(); c->col.release(); c->mat.release();
     c->obj_first.release(); c->obj_model.release(); c->obj_normal.release(); c->obj_matbase.release();
+    c->tri_flags.release();
     c->dmats.release(); c->rrec.release(); c->arec.release(); c->tasks.release(); c->first_rec.release();
     c->clip_list.release();
     c->keys.release(); c->nanseq.release(); c->beaten.release(); c->win.release(); c->depth_ao.release();
@@ -682,6 +685,8 @@ int pr_scene_upload(void* ctx, const pr_scene_desc* s) {
     if ((rc = upload(c->obj_first, first.data(), first.size(), false, st))) return rc;
     if ((rc = upload(c->obj_model, model.data(), model.size(), false, st))) return rc;
     if ((rc = upload(c->obj_normal, normal.data(), normal.size(), false, st))) return rc;
+    if ((rc = c->tri_flags.ensure(std::max<uint32_t>(n, 1)))) return rc;
+    KTRY(prk::launch_tri_flags(c->pos.p, n, c->tri_flags.p, st));
     if ((rc = upload(c->obj_matbase, mb.data(), mb.size(), false, st))) return rc;
     if ((rc = upload(c->dmats, c->materials.data(), c->materials.size(), false, st))) return rc;
     CUDA_TRY(cudaStreamSynchronize(st));  // host vectors above go out of scope

@@ -296,14 +296,67 @@ PR_DEV void emit_tasks_warp(const SetupParams& P, const uint32_t* ridx, const ui
 // Proj.MulM(View).MulM(Model).MulV, -1/W, Viewport Apply + Pos, back-face,
 // viewport AABB; then the per-vertex attributes of surviving triangles
 // (the normal matrix Apply does not influence the culls).
-PR_DEV bool transform_main(const SetupParams& P, uint32_t t, SubVtx* v, float* recipw, int* matid, bool* contained) {
+// The objects of one setup block's triangles (usually one) and their
+// Proj·View·Model, computed once per block in the order of Mat4.MulM.
+constexpr int kBlkObj = 8;
+struct ObjCache {
+    uint32_t o0, n;  // first object; n > kBlkObj: not cached
+    uint32_t first[kBlkObj + 1];
+    float trans[kBlkObj][16];
+};
+
+// Block-wide (every thread calls): triangles [t0, t0 + blockDim.x).
+PR_DEV void obj_cache_fill(const SetupParams& P, uint32_t t0, ObjCache& C) {
+    if (threadIdx.x == 0) {
+        const uint32_t t1 = min(t0 + blockDim.x, P.n_tris) - 1u;
+        const uint32_t o0 = find_object(P.obj_first, P.n_objects, t0);
+        C.o0 = o0;
+        C.n = find_object(P.obj_first, P.n_objects, t1) - o0 + 1u;
+    }
+    __syncthreads();
+    const uint32_t n = C.n, o0 = C.o0;
+    if (n <= (uint32_t)kBlkObj) {
+        for (uint32_t e = threadIdx.x; e < n * 16u; e += blockDim.x) {
+            const uint32_t k = e >> 4, i = (e >> 2) & 3u, j = e & 3u;
+            const float* m = P.pv + i * 4;
+            const float* q = P.obj_model + (size_t)(o0 + k) * 16;
+            C.trans[k][e & 15u] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], q[j]), __fmul_rn(m[1], q[4 + j])),
+                                                      __fmul_rn(m[2], q[8 + j])),
+                                           __fmul_rn(m[3], q[12 + j]));
+        }
+        for (uint32_t e = threadIdx.x; e <= n; e += blockDim.x) C.first[e] = P.obj_first[o0 + e];
+    }
+    __syncthreads();
+}
+
+// Object of triangle t and its Proj·View·Model (from the cache when it holds t's block).
+PR_DEV uint32_t object_trans(const SetupParams& P, const ObjCache* C, uint32_t t, float* trans) {
+    if (C && C->n <= (uint32_t)kBlkObj) {
+        uint32_t k = 0;
+        while (k + 1 < C->n && C->first[k + 1] <= t) k++;
+#pragma unroll
+        for (int e = 0; e < 16; e++) trans[e] = C->trans[k][e];
+        return C->o0 + k;
+    }
     const uint32_t o = find_object(P.obj_first, P.n_objects, t);
+    mulm(P.pv, P.obj_model + o * 16, trans);
+    return o;
+}
+
+// Triangle.IsValid of triangle t (from the flags the scene upload computed).
+PR_DEV bool tri_valid_of(const SetupParams& P, uint32_t t, const V4* p) {
+    if (P.tri_flags) return P.tri_flags[t] != 0;
+    return tri_is_valid(p[0], p[1], p[2]);
+}
+
+PR_DEV bool transform_main(const SetupParams& P, const ObjCache* C, uint32_t t, SubVtx* v, float* recipw, int* matid,
+                           bool* contained) {
     V4 p[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) p[k] = ld4(P.pos[t * 3 + k]);
-    if (!tri_is_valid(p[0], p[1], p[2])) return false;
+    if (!tri_valid_of(P, t, p)) return false;
     float trans[16];
-    mulm(P.pv, P.obj_model + o * 16, trans);
+    const uint32_t o = object_trans(P, C, t, trans);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const V4 cp = mulv(trans, p[k]);
@@ -334,12 +387,12 @@ PR_DEV bool transform_main(const SetupParams& P, uint32_t t, SubVtx* v, float* r
 
 // cpuForwardPass + draw for triangles fully inside the viewport
 // (render/raster.go:257-269, 380-436); clipped ones go to clip_kernel.
-PR_DEV void setup_main_one(const SetupParams& P, uint32_t t, uint32_t* clip_list) {
+PR_DEV void setup_main_one(const SetupParams& P, const ObjCache* C, uint32_t t, uint32_t* clip_list) {
     SubVtx v[3];
     float recipw[3];
     int matid = -1;
     bool contained = false;
-    const bool ok = t < P.n_tris && transform_main(P, t, v, recipw, &matid, &contained);
+    const bool ok = t < P.n_tris && transform_main(P, C, t, v, recipw, &matid, &contained);
     if (ok && P.tri_scr) {
         float4* s = reinterpret_cast<float4*>(P.tri_scr + 12 * (size_t)t);
         s[0] = make_float4(v[0].pos.x, v[0].pos.y, recipw[0], v[1].pos.x);
@@ -365,7 +418,9 @@ PR_DEV void setup_main_one(const SetupParams& P, uint32_t t, uint32_t* clip_list
     emit_tasks_warp(P, &ridx, &area, 1);
 }
 __global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P, uint32_t* clip_list) {
-    setup_main_one(P, blockIdx.x * blockDim.x + threadIdx.x, clip_list);
+    __shared__ ObjCache C;
+    obj_cache_fill(P, blockIdx.x * blockDim.x, C);
+    setup_main_one(P, &C, blockIdx.x * blockDim.x + threadIdx.x, clip_list);
 }
 
 // clipTriangle (render/clipping.go:70-157) for the listed triangles: fan
@@ -382,7 +437,7 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
     V4 clips[10];
     if (j < n) {
         t = clip_list[j];
-        transform_main(P, t, v, recipw, &matid, &contained);
+        transform_main(P, nullptr, t, v, recipw, &matid, &contained);
         V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
         nc = sutherland_hodgman(in3, (float)P.W, (float)P.H, clips);
         if (nc < 0) {
@@ -423,17 +478,16 @@ __global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ Setup
 }
 
 // passShadows / drawDepth for one input triangle (render/shadow.go:137-192)
-PR_DEV void setup_shadow_one(const SetupParams& P, uint32_t t) {
+PR_DEV void setup_shadow_one(const SetupParams& P, const ObjCache* C, uint32_t t) {
     bool ok = false;
     SubVtx v[3];
     if (t < P.n_tris) {
-        const uint32_t o = find_object(P.obj_first, P.n_objects, t);
         V4 p[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) p[k] = ld4(P.pos[t * 3 + k]);
-        if (tri_is_valid(p[0], p[1], p[2])) {
+        if (tri_valid_of(P, t, p)) {
             float trans[16];
-            mulm(P.pv, P.obj_model + o * 16, trans);
+            object_trans(P, C, t, trans);
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 v[k].pos = pos4(apply4_outline(mulv(trans, p[k]), P.viewport));
@@ -461,7 +515,9 @@ PR_DEV void setup_shadow_one(const SetupParams& P, uint32_t t) {
     emit_tasks_warp(P, &ridx, &area, ok ? 1 : 0);
 }
 __global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
-    setup_shadow_one(P, blockIdx.x * blockDim.x + threadIdx.x);
+    __shared__ ObjCache C;
+    obj_cache_fill(P, blockIdx.x * blockDim.x, C);
+    setup_shadow_one(P, &C, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- raster
@@ -1160,6 +1216,14 @@ __global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant
         ao_one(P, j, s_off, s_rlo, s_rhi);
 }
 
+// Triangle.IsValid (geometry/primitive/triangle.go:63-80) of every input
+// triangle, once per scene upload: it depends on model-space positions only.
+__global__ void tri_flags_kernel(const float4* pos, uint32_t n, uint8_t* flags) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    flags[t] = tri_is_valid(ld4(pos[3 * t]), ld4(pos[3 * t + 1]), ld4(pos[3 * t + 2])) ? 1 : 0;
+}
+
 // ---------------------------------------------------------------- batches
 
 // The job owning launch block (or item) b: the largest j with start[j] <= b.
@@ -1176,12 +1240,18 @@ PR_DEV int job_of(const uint32_t* start, int n_jobs, uint32_t b) {
 }
 
 __global__ void __launch_bounds__(128) setup_shadow_batch_kernel(const SetupParams* jobs, const uint32_t* blk, int n_jobs) {
+    __shared__ ObjCache C;
     const int j = job_of(blk, n_jobs, blockIdx.x);
-    setup_shadow_one(jobs[j], (blockIdx.x - blk[j]) * blockDim.x + threadIdx.x);
+    const uint32_t t0 = (blockIdx.x - blk[j]) * blockDim.x;
+    obj_cache_fill(jobs[j], t0, C);
+    setup_shadow_one(jobs[j], &C, t0 + threadIdx.x);
 }
 __global__ void __launch_bounds__(128) setup_main_batch_kernel(const SetupParams* jobs, const uint32_t* blk, int n_jobs) {
+    __shared__ ObjCache C;
     const int j = job_of(blk, n_jobs, blockIdx.x);
-    setup_main_one(jobs[j], (blockIdx.x - blk[j]) * blockDim.x + threadIdx.x, jobs[j].clip_list);
+    const uint32_t t0 = (blockIdx.x - blk[j]) * blockDim.x;
+    obj_cache_fill(jobs[j], t0, C);
+    setup_main_one(jobs[j], &C, t0 + threadIdx.x, jobs[j].clip_list);
 }
 __global__ void __launch_bounds__(128) clip_batch_kernel(const SetupParams* jobs, const uint32_t* blk, int n_jobs) {
     const int j = job_of(blk, n_jobs, blockIdx.x);
@@ -1366,6 +1436,11 @@ int launch_shade(const ShadeParams& p, void* stream) {
     dim3 blk(32, 8);
     dim3 grd((p.W + 31) / 32, (p.H + 7) / 8);
     shade_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_tri_flags(const float4* pos, uint32_t n, uint8_t* flags, void* stream) {
+    if (n == 0) return 0;
+    tri_flags_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(pos, n, flags);
     return check(cudaGetLastError());
 }
 int launch_setup_shadow_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream) {

@@ -90,6 +90,7 @@ struct SetupParams {
     float* tri_scr;              // differentiation only: [n_tris][12] screen x, y, recipw per vertex
     uint32_t task_shift = kTaskShift;  // log2 pixels per raster task (<= 16)
     uint32_t* clip_list;         // batched main setup: this view's clip list
+    const uint8_t* tri_flags;    // [n_tris] Triangle.IsValid, or null (computed inline)
 };
 
 enum RasterMode { kMain = 0, kMainFixup = 1, kShadow = 2, kShadowFixup = 3 };
@@ -232,6 +233,7 @@ int launch_shade_batch(const ShadeParams* views, const uint32_t* blk, int n_view
 int launch_ao_batch(const AoParams* views, int n_views, uint32_t* chunk_ctr, int n_blocks, void* stream);
 int launch_col_to_float(const uchar4* col, float4* out, size_t n, void* stream);
 int launch_fill_u32(uint32_t* p, uint32_t v, size_t n, void* stream);
+int launch_tri_flags(const float4* pos, uint32_t n, uint8_t* flags, void* stream);
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
 int launch_pow_probe(const float* x, const float* y, float* fast, float* ref, int n, void* stream);
