@@ -126,6 +126,11 @@ struct Ctx {
     DevBuf<double> d_acc;
     pr_stats stats{};
     cudaEvent_t ev[6] = {};
+    // shadow passes run on their own stream, with their own records and tasks
+    cudaStream_t stream_s = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    DevBuf<prk::RasterRec> rrec_s;
+    DevBuf<uint2> tasks_s;
     int n_sms = 1;
 };
 
@@ -190,11 +195,13 @@ int ensure_work(Ctx* c, uint32_t need_rec, uint32_t need_tasks) {
         uint32_t cap = std::max(need_rec, c->cap_rec * 2);
         if ((rc = c->rrec.ensure(cap))) return rc;
         if ((rc = c->arec.ensure(cap))) return rc;
+        if ((rc = c->rrec_s.ensure(cap))) return rc;
         c->cap_rec = cap;
     }
     if (need_tasks > c->cap_tasks) {
         uint32_t cap = std::max(need_tasks, c->cap_tasks * 2);
         if ((rc = c->tasks.ensure(cap))) return rc;
+        if ((rc = c->tasks_s.ensure(cap))) return rc;
         c->cap_tasks = cap;
     }
     return PR_OK;
@@ -243,7 +250,7 @@ void collect_stats(Ctx* c) {
     c->stats.n_raster_tasks = n_tasks;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->stats.ms_shadow = ms;
-    cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->stats.ms_setup = ms;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]); c->stats.ms_setup = ms;  // concurrent with the shadow passes
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->stats.ms_raster = ms;
     cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); c->stats.ms_shade = ms;
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); c->stats.ms_total = ms;
@@ -363,7 +370,11 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
     {
         CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(prk::Counters) * (prk::kMaxLights + 1), st));
         CUDA_TRY(cudaEventRecord(c->ev[0], st));
-        // ---- shadow passes (render/raster.go:176-184) ----
+        // ---- shadow passes (render/raster.go:176-184), on their own stream:
+        // only the deferred pass reads the maps ----
+        cudaStream_t ss = c->stream_s;
+        CUDA_TRY(cudaEventRecord(c->ev_fork, st));
+        CUDA_TRY(cudaStreamWaitEvent(ss, c->ev_fork, 0));
         if (shadows) {
             M4 svp = prh::viewport((float)SW, (float)SH);
             for (int l = 0; l < NL; l++) {
@@ -376,20 +387,20 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 M4 lpv = prh::mulm(loadm(f->lights[l].shadow_proj), loadm(f->lights[l].shadow_view));
                 std::memcpy(sp.pv, lpv.m, 64);
                 std::memcpy(sp.viewport, svp.m, 64);
-                sp.rrec = c->rrec.p;
+                sp.rrec = c->rrec_s.p;
                 sp.arec = nullptr;
                 sp.cap_rec = c->cap_rec;
-                sp.tasks = c->tasks.p;
+                sp.tasks = c->tasks_s.p;
                 sp.cap_tasks = c->cap_tasks;
-                sp.first_rec = c->first_rec.p;
+                sp.first_rec = nullptr;
                 sp.cnt = dcnt + 1 + l;
                 if (c->n_tris > c->cap_rec) return fail(PR_ERR_OVERFLOW, "record capacity below triangle count");
                 uint32_t* plane = c->smap.p + (size_t)SW * SH * l;
-                CUDA_TRY(cudaMemsetAsync(c->lastnan.p, 0, (size_t)SW * SH * 4, st));
-                KTRY(prk::launch_setup_shadow(sp, st));
+                CUDA_TRY(cudaMemsetAsync(c->lastnan.p, 0, (size_t)SW * SH * 4, ss));
+                KTRY(prk::launch_setup_shadow(sp, ss));
                 prk::RasterParams rp{};
-                rp.rrec = c->rrec.p;
-                rp.tasks = c->tasks.p;
+                rp.rrec = c->rrec_s.p;
+                rp.tasks = c->tasks_s.p;
                 rp.cnt = dcnt + 1 + l;
                 rp.cnt_w = dcnt + 1 + l;
                 rp.W = SW;
@@ -397,14 +408,15 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 rp.mode = prk::kShadow;
                 rp.smap = plane;
                 rp.lastnan = c->lastnan.p;
-                KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
-                KTRY(prk::launch_shadow_fixup_reset(SW, SH, c->lastnan.p, plane, dcnt + 1 + l, st));
+                KTRY(prk::launch_raster(rp, c->n_sms * 8, ss));
+                KTRY(prk::launch_shadow_fixup_reset(SW, SH, c->lastnan.p, plane, dcnt + 1 + l, ss));
                 rp.mode = prk::kShadowFixup;
-                KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
+                KTRY(prk::launch_raster(rp, c->n_sms * 8, ss));
                 launches += 4;
             }
         }
-        CUDA_TRY(cudaEventRecord(c->ev[1], st));
+        CUDA_TRY(cudaEventRecord(c->ev[1], ss));
+        CUDA_TRY(cudaEventRecord(c->ev_join, ss));
         // ---- forward pass (render/raster.go:226-273) ----
         prk::SetupParams mp{};
         fill_scene_ptrs(c, mp);
@@ -489,6 +501,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             if (out->vcol) { if ((rc = c->o_vcol.ensure(npx * 4))) return rc; sp.gvcol = (uchar4*)c->o_vcol.p; }
             if (out->mat_id) { if ((rc = c->o_mat.ensure(npx))) return rc; sp.gmat = c->o_mat.p; }
         }
+        CUDA_TRY(cudaStreamWaitEvent(st, c->ev_join, 0));  // the shadow maps are complete
         KTRY(prk::launch_shade(sp, st));
         launches += 1;
         CUDA_TRY(cudaEventRecord(c->ev[5], st));
@@ -607,6 +620,12 @@ int pr_create(int device, void** out_ctx) {
         return fail(PR_ERR_CUDA, "cudaStreamCreate failed");
     }
     for (auto& ev : c->ev) cudaEventCreate(&ev);
+    if (cudaStreamCreateWithFlags(&c->stream_s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        pr_destroy(c);
+        return fail(PR_ERR_CUDA, "stream/event creation failed");
+    }
     if ((rc = c->cnt.ensure(prk::kMaxLights + 1))) { pr_destroy(c); return rc; }
     if (cudaMallocHost((void**)&c->h_cnt, sizeof(prk::Counters) * (prk::kMaxLights + 1)) != cudaSuccess) {
         pr_destroy(c);
@@ -642,9 +661,16 @@ int pr_destroy(void* ctx) {
     c->o_nor.release(); c->o_fnor.release(); c->o_wpos.release(); c->o_uvd.release(); c->o_mat.release();
     c->tri_scr.release(); c->d_kd.release(); c->d_ks.release(); c->d_shin.release(); c->d_vcol.release();
     c->d_acc.release();
+    c->rrec_s.release(); c->tasks_s.release();
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
     for (auto& ev : c->ev)
         if (ev) cudaEventDestroy(ev);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->stream_s) {
+        cudaStreamSynchronize(c->stream_s);
+        cudaStreamDestroy(c->stream_s);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PR_OK;
