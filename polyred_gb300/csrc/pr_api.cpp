@@ -111,7 +111,7 @@ struct Ctx {
     int SW = 0, SH = 0, n_slights = 0;
     DevBuf<uint32_t> smap, lastnan;
     bool smap_valid = false;
-    DevBuf<prk::Counters> cnt;  // [kMaxLights + 1]
+    DevBuf<prk::Counters> cnt;  // [kNumCounters]
     prk::Counters* h_cnt = nullptr;  // pinned mirror
     // staging for host outputs
     DevBuf<uint8_t> o_rgba, o_vcol;
@@ -131,6 +131,10 @@ struct Ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     DevBuf<prk::RasterRec> rrec_s;
     DevBuf<uint2> tasks_s;
+    // clipped sub-triangles: clipped and rasterised on a third stream beside the main raster
+    cudaStream_t stream_c = nullptr;
+    cudaEvent_t ev_setup = nullptr, ev_clip = nullptr;
+    DevBuf<uint2> tasks_c;
     int n_sms = 1;
 };
 
@@ -202,6 +206,7 @@ int ensure_work(Ctx* c, uint32_t need_rec, uint32_t need_tasks) {
         uint32_t cap = std::max(need_tasks, c->cap_tasks * 2);
         if ((rc = c->tasks.ensure(cap))) return rc;
         if ((rc = c->tasks_s.ensure(cap))) return rc;
+        if ((rc = c->tasks_c.ensure(cap))) return rc;
         c->cap_tasks = cap;
     }
     return PR_OK;
@@ -246,7 +251,7 @@ void collect_stats(Ctx* c) {
     c->stats.n_clipped_tris = c->h_cnt[0].n_clipped;
     c->stats.n_nan_fragments = c->h_cnt[0].n_nan;
     uint32_t n_tasks = 0;
-    for (int k = 0; k <= prk::kMaxLights; k++) n_tasks += c->h_cnt[k].n_tasks;
+    for (int k = 0; k < prk::kNumCounters; k++) n_tasks += c->h_cnt[k].n_tasks;
     c->stats.n_raster_tasks = n_tasks;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->stats.ms_shadow = ms;
@@ -368,7 +373,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
     uint32_t launches = 0;
 
     {
-        CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(prk::Counters) * (prk::kMaxLights + 1), st));
+        CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(prk::Counters) * prk::kNumCounters, st));
         CUDA_TRY(cudaEventRecord(c->ev[0], st));
         // ---- shadow passes (render/raster.go:176-184), on their own stream:
         // only the deferred pass reads the maps ----
@@ -442,8 +447,19 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         CUDA_TRY(cudaMemsetAsync(c->keys.p, 0, npx * 8, st));
         CUDA_TRY(cudaMemsetAsync(c->nanseq.p, 0xff, npx * 4, st));
         CUDA_TRY(cudaMemsetAsync(c->beaten.p, 0, npx * 4, st));
-        KTRY(prk::launch_setup_main(mp, c->clip_list.p, st));
+        KTRY(prk::launch_setup_main_only(mp, c->clip_list.p, st));
         CUDA_TRY(cudaEventRecord(c->ev[2], st));
+        // clipped triangles: their own task list and stream; records and the
+        // NaN flag stay the main pass's (visibility is order-independent)
+        cudaStream_t sc = c->stream_c;
+        prk::Counters* dclip = dcnt + prk::kClipCnt;
+        CUDA_TRY(cudaEventRecord(c->ev_setup, st));
+        CUDA_TRY(cudaStreamWaitEvent(sc, c->ev_setup, 0));
+        prk::SetupParams cp = mp;
+        cp.cnt = dclip;
+        cp.cnt_rec = dcnt;
+        cp.tasks = c->tasks_c.p;
+        KTRY(prk::launch_clip(cp, c->clip_list.p, sc));
         prk::RasterParams rp{};
         rp.rrec = c->rrec.p;
         rp.tasks = c->tasks.p;
@@ -455,12 +471,20 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         rp.keys = c->keys.p;
         rp.nanseq = c->nanseq.p;
         rp.beaten = c->beaten.p;
+        prk::RasterParams rc_ = rp;
+        rc_.tasks = c->tasks_c.p;
+        rc_.cnt = dclip;
+        KTRY(prk::launch_raster(rc_, c->n_sms * 8, sc));
+        CUDA_TRY(cudaEventRecord(c->ev_clip, sc));
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
+        CUDA_TRY(cudaStreamWaitEvent(st, c->ev_clip, 0));
         rp.mode = prk::kMainFixup;
+        rc_.mode = prk::kMainFixup;
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
+        KTRY(prk::launch_raster(rc_, c->n_sms * 8, st));
         KTRY(prk::launch_resolve(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p, st));
         CUDA_TRY(cudaEventRecord(c->ev[3], st));
-        launches += 5;
+        launches += 7;
 
         // ---- deferred shading + gamma (render/raster.go:275-378) ----
         std::unique_ptr<prk::ShadeParams> sp_owner(new (std::nothrow) prk::ShadeParams());
@@ -523,7 +547,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             launches += 1;
         }
         CUDA_TRY(cudaEventRecord(c->ev[4], st));
-        CUDA_TRY(cudaMemcpyAsync(c->h_cnt, dcnt, sizeof(prk::Counters) * (prk::kMaxLights + 1), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(c->h_cnt, dcnt, sizeof(prk::Counters) * prk::kNumCounters, cudaMemcpyDeviceToHost, st));
         if (!sync) {
             c->stats.n_kernel_launches = launches;
             return PR_OK;
@@ -531,7 +555,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         CUDA_TRY(cudaStreamSynchronize(st));
         // capacity check
         uint32_t ov = 0, need_rec = 0, need_tasks = 0;
-        for (int k = 0; k <= prk::kMaxLights; k++) {
+        for (int k = 0; k < prk::kNumCounters; k++) {
             ov |= c->h_cnt[k].overflow;
             need_rec = std::max(need_rec, c->h_cnt[k].need_rec);
             need_tasks = std::max(need_tasks, c->h_cnt[k].need_tasks);
@@ -622,12 +646,15 @@ int pr_create(int device, void** out_ctx) {
     for (auto& ev : c->ev) cudaEventCreate(&ev);
     if (cudaStreamCreateWithFlags(&c->stream_s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream_c, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_setup, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_clip, cudaEventDisableTiming) != cudaSuccess) {
         pr_destroy(c);
         return fail(PR_ERR_CUDA, "stream/event creation failed");
     }
-    if ((rc = c->cnt.ensure(prk::kMaxLights + 1))) { pr_destroy(c); return rc; }
-    if (cudaMallocHost((void**)&c->h_cnt, sizeof(prk::Counters) * (prk::kMaxLights + 1)) != cudaSuccess) {
+    if ((rc = c->cnt.ensure(prk::kNumCounters))) { pr_destroy(c); return rc; }
+    if (cudaMallocHost((void**)&c->h_cnt, sizeof(prk::Counters) * prk::kNumCounters) != cudaSuccess) {
         pr_destroy(c);
         return fail(PR_ERR_OOM, "pinned counter allocation failed");
     }
@@ -661,7 +688,13 @@ int pr_destroy(void* ctx) {
     c->o_nor.release(); c->o_fnor.release(); c->o_wpos.release(); c->o_uvd.release(); c->o_mat.release();
     c->tri_scr.release(); c->d_kd.release(); c->d_ks.release(); c->d_shin.release(); c->d_vcol.release();
     c->d_acc.release();
-    c->rrec_s.release(); c->tasks_s.release();
+    c->rrec_s.release(); c->tasks_s.release(); c->tasks_c.release();
+    if (c->ev_setup) cudaEventDestroy(c->ev_setup);
+    if (c->ev_clip) cudaEventDestroy(c->ev_clip);
+    if (c->stream_c) {
+        cudaStreamSynchronize(c->stream_c);
+        cudaStreamDestroy(c->stream_c);
+    }
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
     for (auto& ev : c->ev)
         if (ev) cudaEventDestroy(ev);
@@ -740,7 +773,7 @@ int pr_render(void* ctx, const pr_frame_desc* frame, pr_outputs* out) {
         rc = render_impl(c, frame, out, true);
         if (rc == PR_ERR_OVERFLOW) {
             uint32_t need_rec = 0, need_tasks = 0;
-            for (int k = 0; k <= prk::kMaxLights; k++) {
+            for (int k = 0; k < prk::kNumCounters; k++) {
                 need_rec = std::max(need_rec, c->h_cnt[k].need_rec);
                 need_tasks = std::max(need_tasks, c->h_cnt[k].need_tasks);
             }
@@ -762,7 +795,7 @@ int pr_sync(void* ctx) {
     Ctx* c = (Ctx*)ctx;
     if (!c) return fail(PR_ERR_INVALID_ARG, "ctx is NULL");
     CUDA_TRY(cudaStreamSynchronize(c->stream));
-    for (int k = 0; k <= prk::kMaxLights; k++)
+    for (int k = 0; k < prk::kNumCounters; k++)
         if (c->h_cnt[k].overflow) return fail(PR_ERR_OVERFLOW, "internal capacity exceeded in an asynchronous frame");
     collect_stats(c);
     return PR_OK;
@@ -923,7 +956,7 @@ int pr_diff_forward(void* ctx, const pr_frame_desc* frame, const pr_diff_params*
         rc = render_impl(c, frame, &o, true, &dh);
         if (rc == PR_ERR_OVERFLOW) {
             uint32_t need_rec = 0, need_tasks = 0;
-            for (int k = 0; k <= prk::kMaxLights; k++) {
+            for (int k = 0; k < prk::kNumCounters; k++) {
                 need_rec = std::max(need_rec, c->h_cnt[k].need_rec);
                 need_tasks = std::max(need_tasks, c->h_cnt[k].need_tasks);
             }
@@ -1472,7 +1505,7 @@ int batch_run(Batch* b, uint32_t nv, const pr_batch_view* views) {
                 rc = render_impl(c, views[v].frame, views[v].out, true);
                 if (rc == PR_ERR_OVERFLOW) {
                     uint32_t nr = 0, nt = 0;
-                    for (int k = 0; k <= prk::kMaxLights; k++) {
+                    for (int k = 0; k < prk::kNumCounters; k++) {
                         nr = std::max(nr, c->h_cnt[k].need_rec);
                         nt = std::max(nt, c->h_cnt[k].need_tasks);
                     }

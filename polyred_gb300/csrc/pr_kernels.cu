@@ -448,7 +448,8 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
     __syncwarp();
     const uint32_t nsub = nc > 2 ? (uint32_t)(nc - 2) : 0u;
     uint32_t tot;
-    const uint32_t base = warp_reserve(&P.cnt->n_rec, nsub, &tot);
+    Counters* crec = P.cnt_rec ? P.cnt_rec : P.cnt;
+    const uint32_t base = warp_reserve(&crec->n_rec, nsub, &tot);
     uint32_t ridxs[8], areas[8];
     int nw = 0;
     if (nsub > 0) {
@@ -472,7 +473,7 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
     emit_tasks_warp(P, ridxs, areas, nw);
 }
 __global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ SetupParams P, const uint32_t* clip_list) {
-    const uint32_t n = P.cnt->n_clipped;
+    const uint32_t n = (P.cnt_rec ? P.cnt_rec : P.cnt)->n_clipped;
     if (blockIdx.x * blockDim.x >= n) return;  // whole block idle (uniform per warp too)
     clip_one(P, clip_list, blockIdx.x * blockDim.x + threadIdx.x, n);
 }
@@ -659,7 +660,7 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
     __shared__ int s_start[kRasterWarps][32];
     const Counters* c = P.cnt;
     if (P.mode == kMainFixup || P.mode == kShadowFixup) {
-        if (c->nan_flag == 0) return;
+        if (P.cnt_w->nan_flag == 0) return;  // flags of every list of the pass meet in cnt_w
     }
     const uint32_t n_tasks = c->n_tasks;
     if (c->overflow) return;
@@ -1398,6 +1399,17 @@ int check(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
 
 }  // namespace
 
+int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stream) {
+    if (p.n_tris == 0) return 0;
+    setup_main_kernel<<<(p.n_tris + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
+    return check(cudaGetLastError());
+}
+int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream) {
+    if (p.n_tris == 0) return 0;
+    // the list's length is known only on the device: a grid for the worst case, idle blocks exit at once
+    clip_kernel<<<(p.n_tris + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
+    return check(cudaGetLastError());
+}
 int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream) {
     if (p.n_tris == 0) return 0;
     unsigned nb = (p.n_tris + 127) / 128;

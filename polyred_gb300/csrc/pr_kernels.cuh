@@ -13,6 +13,10 @@
 namespace prk {
 
 constexpr int kMaxLights = 16;
+// Counters of a frame: [0] the main pass, [1 + l] shadow pass l, [kClipCnt]
+// the clipped sub-triangles' raster tasks.
+constexpr int kClipCnt = kMaxLights + 1;
+constexpr int kNumCounters = kMaxLights + 2;
 constexpr int kMaxAmbient = 16;
 constexpr uint32_t kTaskShift = 10;  // a raster task is a 2^kTaskShift-pixel chunk of a bbox (default)
 constexpr uint32_t kNone = 0xFFFFFFFFu;
@@ -91,6 +95,7 @@ struct SetupParams {
     uint32_t task_shift = kTaskShift;  // log2 pixels per raster task (<= 16)
     uint32_t* clip_list;         // batched main setup: this view's clip list
     const uint8_t* tri_flags;    // [n_tris] Triangle.IsValid, or null (computed inline)
+    Counters* cnt_rec;           // clip: the main pass's counters (records, clip list); null: cnt
 };
 
 enum RasterMode { kMain = 0, kMainFixup = 1, kShadow = 2, kShadowFixup = 3 };
@@ -196,7 +201,9 @@ struct DiffParamsK {
 
 // Launch wrappers implemented in pr_kernels.cu (host-callable).
 namespace prk {
-int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream);
+int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream);  // setup, then clip
+int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stream);
+int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream);
 int launch_setup_shadow(const SetupParams& p, void* stream);
 int launch_raster(const RasterParams& p, int n_blocks, void* stream);
 int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
