@@ -988,6 +988,14 @@ PR_DEV bool ao_tap_exact(int t, float pxf, float pyf, float dX, float dY, int W,
     return true;
 }
 
+// The elevation of fast-path tap t again (settling a pending tap reloads it
+// instead of carrying it).
+PR_DEV float ao_tap_elev(const int (*s_off)[kAoTable], int k, int t, const float* p0, const float* pA, int tstar, float z,
+                         bool tiny) {
+    const float* q = (tiny && t < tstar) ? pA : p0;
+    return __fsub_rn(__ldg(q + s_off[k][t - 2]), z);
+}
+
 // maxElevationAngle's march for taps 2 .. 101 in groups of four, from shared
 // tables of index offsets and of bounds on 1/dist (see ao_kernel): the exact
 // ratio RN(elev/dist) of a tap lies in [RD(elev rlo), RU(elev rhi)]. A tap
@@ -1002,8 +1010,9 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
                            float pxf, float pyf, float dX, float dY, float& best) {
     float lb = best;
     int pt = 0;
-    float pel = 0.0f, phi = 0.0f;
+    float phi = 0.0f;
     bool nan_seen = false;
+#pragma unroll 2
     for (int g = 0; g < n_groups; g++) {
         const int t0 = 4 * g + 2;
         const int4 o = *reinterpret_cast<const int4*>(&s_off[k][4 * g]);
@@ -1029,7 +1038,6 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
             // Branch-free: each candidate becomes the pending tap; a pending
             // tap it overlaps is recorded and settled after the group (rare).
             int st[4];
-            float sel[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 nan_seen |= isnan(el[u]);
@@ -1037,9 +1045,7 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
                 const float rlo = __fmul_rd(el[u], lo[u]);
                 const bool ov = take & (pt != 0) & !(rlo >= phi);
                 st[u] = ov ? pt : 0;
-                sel[u] = pel;
                 pt = take ? t0 + u : pt;
-                pel = take ? el[u] : pel;
                 phi = take ? hi[u] : phi;
                 lb = take ? fmaxf(lb, rlo) : lb;
             }
@@ -1047,12 +1053,14 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
             if ((st[0] | st[1] | st[2] | st[3]) != 0) {
 #pragma unroll
                 for (int u = 0; u < 4; u++)
-                    if (st[u]) best = fmaxf(best, ao_exact_ratio(st[u], sel[u], pxf, pyf, dX, dY));
+                    if (st[u]) best = fmaxf(best, ao_exact_ratio(st[u], ao_tap_elev(s_off, k, st[u], p0, pA, tstar, z,
+                                                                                     TINY),
+                                                               pxf, pyf, dX, dY));
                 lb = fmaxf(lb, best);
             }
         }
     }
-    if (pt != 0) best = fmaxf(best, ao_exact_ratio(pt, pel, pxf, pyf, dX, dY));
+    if (pt != 0) best = fmaxf(best, ao_exact_ratio(pt, ao_tap_elev(s_off, k, pt, p0, pA, tstar, z, TINY), pxf, pyf, dX, dY));
     return true;
 }
 
