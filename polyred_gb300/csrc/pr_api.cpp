@@ -413,9 +413,11 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 rp.mode = prk::kShadow;
                 rp.smap = plane;
                 rp.lastnan = c->lastnan.p;
+                rp.take = &dcnt[1 + l].take[0];
                 KTRY(prk::launch_raster(rp, c->n_sms * 8, ss));
                 KTRY(prk::launch_shadow_fixup_reset(SW, SH, c->lastnan.p, plane, dcnt + 1 + l, ss));
                 rp.mode = prk::kShadowFixup;
+                rp.take = &dcnt[1 + l].take[1];
                 KTRY(prk::launch_raster(rp, c->n_sms * 8, ss));
                 launches += 4;
             }
@@ -471,15 +473,19 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         rp.keys = c->keys.p;
         rp.nanseq = c->nanseq.p;
         rp.beaten = c->beaten.p;
+        rp.take = &dcnt[0].take[0];
         prk::RasterParams rc_ = rp;
         rc_.tasks = c->tasks_c.p;
         rc_.cnt = dclip;
+        rc_.take = &dclip->take[0];
         KTRY(prk::launch_raster(rc_, c->n_sms * 8, sc));
         CUDA_TRY(cudaEventRecord(c->ev_clip, sc));
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_clip, 0));
         rp.mode = prk::kMainFixup;
         rc_.mode = prk::kMainFixup;
+        rp.take = &dcnt[0].take[1];
+        rc_.take = &dclip->take[1];
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
         KTRY(prk::launch_raster(rc_, c->n_sms * 8, st));
         KTRY(prk::launch_resolve(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p, st));
@@ -1596,7 +1602,7 @@ int pr_batch_tune(void* batch, uint32_t n_views, const pr_batch_view* views, cha
     if (!b) return fail(PR_ERR_INVALID_ARG, "batch is NULL");
     if (n_views == 0 || !views) return fail(PR_ERR_INVALID_ARG, "no views");
     std::lock_guard<std::mutex> lk(b->mu);
-    const uint32_t shifts[] = {8, 9, 10, 11, 12};
+    const uint32_t shifts[] = {5, 6, 8, 10, 12};
     const int bps[] = {2, 4, 8};
     std::string rep = "{\"candidates\": [";
     double best = 1e30;

@@ -525,139 +525,186 @@ __global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant
 
 constexpr int kRasterWarps = 8;
 
-struct SmRec {
-    float x[3], y[3], z[3], sabc;
-    uint32_t x0, y0, bw, seq;
-    uint32_t qx0, qy0;  // bbox coordinates of the task's first pixel
-    uint32_t magic;     // ceil(2^32 / bw): floor(t / bw) = umulhi(t, magic) for t < 2^16
+// One record of a warp's task batch in shared memory, laid out for 16-byte
+// loads, with the per-triangle terms of the coverage test precomputed.
+struct __align__(16) SmRec {
+    float4 ab;  // A.x, A.y, B.x, B.y (screen vertices)
+    float4 e0;  // (B-A).x, (B-A).y, (C-A).x, (C-A).y
+    float4 e1;  // (C-B).x, (C-B).y, RN(1/Sabc) (0: no early reject), Sabc
+    float4 zs;  // A.z, B.z, C.z, seq (bits)
+    uint4 bb;   // bbox x0, bbox y0 + the task's first row, bbox width bw, ceil(2^32 / bw)
 };
+
+// A warp's raster scratch: its 32 records, the prefix of their pixel counts,
+// and a ring of pixels that passed the early reject. The exact test runs
+// only once 32 of them are queued, on all lanes, instead of on the lanes
+// whose pixel happened to survive.
+struct RasterWarpSm {
+    SmRec rec[32];
+    int start[32];    // first warp pixel of each task
+    uint32_t tq[32];  // the task's first bbox index minus start (mod 2^32)
+    uint32_t q[64];   // (slot << 27) | bbox index t (t < 2^17)
+};
+
+// bbox index t of a record's pixel -> (px, py). t < 2^17 and bw <= 2^14, so
+// t * bw < 2^32 and the multiply-high quotient is exact.
+PR_DEV void rec_pixel(const uint4& bb, uint32_t t, int* px, int* py) {
+    const uint32_t q = __umulhi(t, bb.w);
+    *px = (int)(bb.x + (t - q * bb.z));
+    *py = (int)(bb.y + q);
+}
+
+// Conservative early reject (pixel certainly outside): the single-rounding
+// estimate differs from the reference's double rounding by at most one ulp,
+// so a margin of 2^-20 relative decides only pixels that are certainly out.
+PR_DEV bool pixel_rejected(const SmRec& r, int px, int py) {
+    const float fx = __fadd_rn(small_u2f((uint32_t)px), 0.5f), fy = __fadd_rn(small_u2f((uint32_t)py), 0.5f);
+    const float4 ab = r.ab, e0 = r.e0, e1 = r.e1;
+    const float apx = __fsub_rn(fx, ab.x), apy = __fsub_rn(fy, ab.y);
+    const float bpx = __fsub_rn(fx, ab.z), bpy = __fsub_rn(fy, ab.w);
+    const float inv = e1.z;
+    const float w0 = __fmul_rn(__fmaf_rn(e1.x, bpy, -__fmul_rn(e1.y, bpx)), inv);
+    const float w1 = __fmul_rn(__fmaf_rn(apx, e0.w, -__fmul_rn(apy, e0.z)), inv);
+    const float w2 = __fmul_rn(__fmaf_rn(e0.x, apy, -__fmul_rn(e0.y, apx)), inv);
+    const float shrink = 0.99999904632568359375f;  // 1 - 2^-20
+    return __fmul_rn(w0, shrink) < -kEps || __fmul_rn(w1, shrink) < -kEps || __fmul_rn(w2, shrink) < -kEps;
+}
 
 // Coverage and depth of one pixel against one record (drawClipped's
 // Barycoord / inside / z lines, render/raster.go:487-496).
 PR_DEV bool pixel_depth(const SmRec& r, int px, int py, float* zout) {
-    float fx = __fadd_rn(small_u2f((uint32_t)px), 0.5f), fy = __fadd_rn(small_u2f((uint32_t)py), 0.5f);
-    float apx = __fsub_rn(fx, r.x[0]), apy = __fsub_rn(fy, r.y[0]);
-    float abx = __fsub_rn(r.x[1], r.x[0]), aby = __fsub_rn(r.y[1], r.y[0]);
-    float acx = __fsub_rn(r.x[2], r.x[0]), acy = __fsub_rn(r.y[2], r.y[0]);
-    float bcx = __fsub_rn(r.x[2], r.x[1]), bcy = __fsub_rn(r.y[2], r.y[1]);
-    float bpx = __fsub_rn(fx, r.x[1]), bpy = __fsub_rn(fy, r.y[1]);
-    float sabc = r.sabc;
-    float as = fabsf(sabc);
-    if (as >= 1e-30f && as <= 1e30f) {
-        // Conservative early reject: the single-rounding estimate differs from
-        // the reference's double rounding by at most one ulp, so a margin of
-        // 2^-20 relative decides only pixels that are certainly outside.
-        float inv = __frcp_rn(sabc);
-        float w0 = __fmul_rn(__fmaf_rn(bcx, bpy, -__fmul_rn(bcy, bpx)), inv);
-        float w1 = __fmul_rn(__fmaf_rn(apx, acy, -__fmul_rn(apy, acx)), inv);
-        float w2 = __fmul_rn(__fmaf_rn(abx, apy, -__fmul_rn(aby, apx)), inv);
-        const float shrink = 0.99999904632568359375f;  // 1 - 2^-20
-        if (__fmul_rn(w0, shrink) < -kEps || __fmul_rn(w1, shrink) < -kEps || __fmul_rn(w2, shrink) < -kEps)
-            return false;
-    }
-    float sabp = cross_z(abx, aby, apx, apy);
-    float sapc = cross_z(apx, apy, acx, acy);
-    float sbcp = cross_z(bcx, bcy, bpx, bpy);
-    float b0 = __fdiv_rn(sbcp, sabc), b1 = __fdiv_rn(sapc, sabc), b2 = __fdiv_rn(sabp, sabc);
+    const float fx = __fadd_rn(small_u2f((uint32_t)px), 0.5f), fy = __fadd_rn(small_u2f((uint32_t)py), 0.5f);
+    const float4 ab = r.ab, e0 = r.e0, e1 = r.e1;
+    const float apx = __fsub_rn(fx, ab.x), apy = __fsub_rn(fy, ab.y);
+    const float bpx = __fsub_rn(fx, ab.z), bpy = __fsub_rn(fy, ab.w);
+    const float sabc = e1.w;
+    const float sabp = cross_z(e0.x, e0.y, apx, apy);
+    const float sapc = cross_z(apx, apy, e0.z, e0.w);
+    const float sbcp = cross_z(e1.x, e1.y, bpx, bpy);
+    const float b0 = __fdiv_rn(sbcp, sabc), b1 = __fdiv_rn(sapc, sabc), b2 = __fdiv_rn(sabp, sabc);
     if (b0 < -kEps || b1 < -kEps || b2 < -kEps) return false;
-    *zout = __fadd_rn(__fadd_rn(__fmul_rn(b0, r.z[0]), __fmul_rn(b1, r.z[1])), __fmul_rn(b2, r.z[2]));
+    const float4 zs = r.zs;
+    *zout = __fadd_rn(__fadd_rn(__fmul_rn(b0, zs.x), __fmul_rn(b1, zs.y)), __fmul_rn(b2, zs.z));
     return true;
 }
 
-// Tasks [base, base + 32) of one pass, one per lane, pixels spread over the
-// warp by a prefix scan of their counts. s_rec / s_start: this warp's slots.
-PR_DEV void raster_warp(const RasterParams& P, uint32_t base, uint32_t n_tasks, SmRec* s_rec, int* s_start) {
-    const int lane = threadIdx.x & 31;
-    {
-        uint32_t ti = base + lane;
-        int cnt = 0;
-        if (ti < n_tasks) {
-            uint2 tk = P.tasks[ti];
-            const float4* rp = reinterpret_cast<const float4*>(P.rrec + tk.x);
-            float4 q0 = rp[0], q1 = rp[1], q2 = rp[2], q3 = rp[3];
-            SmRec& s = s_rec[lane];
-            s.x[0] = q0.x; s.y[0] = q0.y; s.z[0] = q0.z;
-            s.x[1] = q0.w; s.y[1] = q1.x; s.z[1] = q1.y;
-            s.x[2] = q1.z; s.y[2] = q1.w; s.z[2] = q2.x;
-            s.sabc = q2.y;
-            uint32_t bx = __float_as_uint(q2.z), by = __float_as_uint(q2.w);
-            s.seq = __float_as_uint(q3.x);
-            uint32_t x0 = bx & 0xffffu, x1 = bx >> 16, y0 = by & 0xffffu, y1 = by >> 16;
-            if (x0 <= x1 && y0 <= y1) {
-                uint32_t bw = x1 - x0 + 1, area = bw * (y1 - y0 + 1);
-                uint32_t k0 = tk.y << P.task_shift;
-                if (k0 < area) cnt = (int)min(area - k0, 1u << P.task_shift);
-                s.x0 = x0;
-                s.y0 = y0;
-                s.bw = bw;
-                s.qy0 = k0 / bw;  // one division per task
-                s.qx0 = k0 - s.qy0 * bw;
-                s.magic = 0xFFFFFFFFu / bw + 1u;
-            }
+// The exact test and the depth write of one queued pixel.
+PR_DEV void raster_pixel(const RasterParams& P, const RasterWarpSm& S, uint32_t ent) {
+    const SmRec& r = S.rec[ent >> 27];
+    int px, py;
+    rec_pixel(r.bb, ent & 0x7FFFFFFu, &px, &py);
+    float z;
+    if (!pixel_depth(r, px, py, &z)) return;
+    const uint32_t seq = __float_as_uint(r.zs.w);
+    const bool zn = isnan(z);
+    if (P.mode == kMain) {
+        size_t i = (size_t)(P.H - 1 - py) * P.W + px;
+        if (zn) {
+            atomicMin(&P.nanseq[i], seq);
+            atomicExch(&P.cnt_w->nan_flag, 1u);
+            atomicAdd(&P.cnt_w->n_nan, 1u);
+        } else {
+            unsigned long long key = ((unsigned long long)fkey(z) << 32) | (unsigned long long)(0xFFFFFFFFu - seq);
+            atomicMax(&P.keys[i], key);
         }
-        int incl = cnt;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            int v = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= d) incl += v;
+    } else if (P.mode == kMainFixup) {
+        size_t i = (size_t)(P.H - 1 - py) * P.W + px;
+        if (!zn) {
+            uint32_t ns = P.nanseq[i];
+            if (ns != kNone && seq < ns) P.beaten[i] = 1u;
         }
-        s_start[lane] = incl - cnt;
-        int total = __shfl_sync(0xffffffffu, incl, 31);
-        __syncwarp();
-        for (int g = lane; g < total; g += 32) {
-            int j = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (s_start[j + step] <= g) j += step;
-            const SmRec& r = s_rec[j];
-            // pixel qx0 + l of the task's first row, l < 2^task_shift <= 2^16:
-            // t < 2^17, where the multiply-high quotient is exact for
-            // bw <= 2^15 (t * bw < 2^32)
-            const uint32_t t = r.qx0 + (uint32_t)(g - s_start[j]);
-            const uint32_t q = __umulhi(t, r.magic);
-            int px = (int)(r.x0 + (t - q * r.bw));
-            int py = (int)(r.y0 + r.qy0 + q);
-            float z;
-            if (!pixel_depth(r, px, py, &z)) continue;
-            bool zn = isnan(z);
-            if (P.mode == kMain) {
-                size_t i = (size_t)(P.H - 1 - py) * P.W + px;
-                if (zn) {
-                    atomicMin(&P.nanseq[i], r.seq);
-                    atomicExch(&P.cnt_w->nan_flag, 1u);
-                    atomicAdd(&P.cnt_w->n_nan, 1u);
-                } else {
-                    unsigned long long key = ((unsigned long long)fkey(z) << 32) | (unsigned long long)(0xFFFFFFFFu - r.seq);
-                    atomicMax(&P.keys[i], key);
-                }
-            } else if (P.mode == kMainFixup) {
-                size_t i = (size_t)(P.H - 1 - py) * P.W + px;
-                if (!zn) {
-                    uint32_t ns = P.nanseq[i];
-                    if (ns != kNone && r.seq < ns) P.beaten[i] = 1u;
-                }
-            } else if (P.mode == kShadow) {
-                size_t i = (size_t)px + (size_t)py * P.W;
-                if (zn) {
-                    if (P.lastnan) atomicMax(&P.lastnan[i], r.seq + 1u);
-                    atomicExch(&P.cnt_w->nan_flag, 1u);
-                    atomicAdd(&P.cnt_w->n_nan, 1u);
-                } else {
-                    atomicMax(&P.smap[i], fkey(z));
-                }
-            } else {  // kShadowFixup
-                size_t i = (size_t)px + (size_t)py * P.W;
-                uint32_t ln = P.lastnan[i];
-                if (!zn && ln != 0u && r.seq + 1u > ln) atomicMax(&P.smap[i], fkey(z));
-            }
+    } else if (P.mode == kShadow) {
+        size_t i = (size_t)px + (size_t)py * P.W;
+        if (zn) {
+            if (P.lastnan) atomicMax(&P.lastnan[i], seq + 1u);
+            atomicExch(&P.cnt_w->nan_flag, 1u);
+            atomicAdd(&P.cnt_w->n_nan, 1u);
+        } else {
+            atomicMax(&P.smap[i], fkey(z));
         }
-        __syncwarp();
+    } else {  // kShadowFixup
+        size_t i = (size_t)px + (size_t)py * P.W;
+        uint32_t ln = P.lastnan[i];
+        if (!zn && ln != 0u && seq + 1u > ln) atomicMax(&P.smap[i], fkey(z));
     }
 }
 
+// Tasks [base, base + 32) of one pass, one per lane, pixels spread over the
+// warp by a prefix scan of their counts.
+PR_DEV void raster_warp(const RasterParams& P, uint32_t base, uint32_t n_tasks, RasterWarpSm& S) {
+    const int lane = threadIdx.x & 31;
+    uint32_t ti = base + lane;
+    int cnt = 0;
+    uint32_t qx0 = 0;
+    if (ti < n_tasks) {
+        uint2 tk = P.tasks[ti];
+        const float4* rp = reinterpret_cast<const float4*>(P.rrec + tk.x);
+        const float4 q0 = rp[0], q1 = rp[1], q2 = rp[2], q3 = rp[3];
+        // record: A.xyz, B.xyz, C.xyz, Sabc, packed bbox x and y ranges, seq
+        const float ax = q0.x, ay = q0.y, bx = q0.w, by = q1.x, cx = q1.z, cy = q1.w, sabc = q2.y;
+        const uint32_t bxr = __float_as_uint(q2.z), byr = __float_as_uint(q2.w);
+        const uint32_t x0 = bxr & 0xffffu, x1 = bxr >> 16, y0 = byr & 0xffffu, y1 = byr >> 16;
+        SmRec& s = S.rec[lane];
+        s.ab = make_float4(ax, ay, bx, by);
+        s.e0 = make_float4(__fsub_rn(bx, ax), __fsub_rn(by, ay), __fsub_rn(cx, ax), __fsub_rn(cy, ay));
+        const float as = fabsf(sabc);
+        const float inv = (as >= 1e-30f && as <= 1e30f) ? __frcp_rn(sabc) : 0.0f;
+        s.e1 = make_float4(__fsub_rn(cx, bx), __fsub_rn(cy, by), inv, sabc);
+        s.zs = make_float4(q0.z, q1.y, q2.x, q3.x);
+        if (x0 <= x1 && y0 <= y1) {
+            const uint32_t bw = x1 - x0 + 1, area = bw * (y1 - y0 + 1);
+            const uint32_t k0 = tk.y << P.task_shift;
+            if (k0 < area) cnt = (int)min(area - k0, 1u << P.task_shift);
+            const uint32_t qy0 = k0 / bw;  // one division per task
+            qx0 = k0 - qy0 * bw;
+            s.bb = make_uint4(x0, y0 + qy0, bw, 0xFFFFFFFFu / bw + 1u);
+        }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    S.start[lane] = incl - cnt;
+    S.tq[lane] = qx0 - (uint32_t)(incl - cnt);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t head = 0, tail = 0;  // warp-uniform ring positions
+    for (int g0 = 0; g0 < total; g0 += 32) {
+        const int g = g0 + lane;
+        bool keep = false;
+        uint32_t ent = 0;
+        if (g < total) {
+            int j = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (S.start[j + step] <= g) j += step;
+            const SmRec& r = S.rec[j];
+            const uint32_t t = S.tq[j] + (uint32_t)g;
+            int px, py;
+            rec_pixel(r.bb, t, &px, &py);
+            keep = !pixel_rejected(r, px, py);
+            ent = ((uint32_t)j << 27) | t;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) S.q[(tail + __popc(m & lt)) & 63u] = ent;
+        tail += __popc(m);
+        if (tail - head >= 32u) {
+            __syncwarp();
+            raster_pixel(P, S, S.q[(head + lane) & 63u]);
+            head += 32u;
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+    if ((uint32_t)lane < tail - head) raster_pixel(P, S, S.q[(head + lane) & 63u]);
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_constant__ RasterParams P) {
-    __shared__ SmRec s_rec[kRasterWarps][32];
-    __shared__ int s_start[kRasterWarps][32];
+    __shared__ RasterWarpSm s_w[kRasterWarps];
     const Counters* c = P.cnt;
     if (P.mode == kMainFixup || P.mode == kShadowFixup) {
         if (P.cnt_w->nan_flag == 0) return;  // flags of every list of the pass meet in cnt_w
@@ -665,8 +712,20 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
     const uint32_t n_tasks = c->n_tasks;
     if (c->overflow) return;
     const int warp = threadIdx.x >> 5;
+    if (P.take) {
+        // Dynamic: a task's cost is its bbox chunk, and consecutive tasks of
+        // one object tend to be alike, so a static stride leaves a tail.
+        for (;;) {
+            uint32_t base = 0;
+            if ((threadIdx.x & 31) == 0) base = atomicAdd(P.take, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n_tasks) break;
+            raster_warp(P, base, n_tasks, s_w[warp]);
+        }
+        return;
+    }
     const uint32_t gw = blockIdx.x * kRasterWarps + warp, nw = gridDim.x * kRasterWarps;
-    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) raster_warp(P, base, n_tasks, s_rec[warp], s_start[warp]);
+    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) raster_warp(P, base, n_tasks, s_w[warp]);
 }
 
 PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
@@ -1310,8 +1369,7 @@ __global__ void __launch_bounds__(1024) batch_scan_kernel(const RasterParams* jo
 // (pass, warp batch) item from the global queue.
 __global__ void __launch_bounds__(kRasterWarps * 32) raster_batch_kernel(const RasterParams* jobs, const uint32_t* items,
                                                                          int n_jobs, uint32_t* queue) {
-    __shared__ SmRec s_rec[kRasterWarps][32];
-    __shared__ int s_start[kRasterWarps][32];
+    __shared__ RasterWarpSm s_w[kRasterWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t total = items[n_jobs];
     for (;;) {
@@ -1321,7 +1379,7 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_batch_kernel(const R
         if (it >= total) break;
         const int j = job_of(items, n_jobs, it);
         const RasterParams& P = jobs[j];
-        raster_warp(P, (it - items[j]) * 32u, P.cnt->n_tasks, s_rec[warp], s_start[warp]);
+        raster_warp(P, (it - items[j]) * 32u, P.cnt->n_tasks, s_w[warp]);
     }
 }
 
@@ -1575,6 +1633,7 @@ constexpr uint32_t kNoAllocMaxTris = 65536;
 constexpr uint32_t kNoAllocMaxObjects = 256;
 constexpr uint32_t kNoAllocMaxTexels = 1u << 20;  // e.g. 1024 x 1024
 constexpr uint32_t kNoAllocMaxTasks = 4u * kNoAllocMaxTris;
+constexpr uint32_t kNoAllocTaskShift = 10;  // 1024-pixel tasks: the fixed task table covers large triangles
 
 constexpr size_t kNaCounters = 0;                                   // Counters
 constexpr size_t kNaObjFirst = 256;                                 // u32 [max_objects + 1]
@@ -1690,8 +1749,10 @@ extern "C" int pr_depth_map_noalloc(const pr_depth_map_desc* d) {
     sp.tasks = tasks;
     sp.cap_tasks = kNoAllocMaxTasks;
     sp.cnt = cnt;
+    sp.task_shift = kNoAllocTaskShift;
     int rc = launch_setup_shadow(sp, st);
     RasterParams rp{};
+    rp.task_shift = kNoAllocTaskShift;
     rp.rrec = rrec;
     rp.tasks = tasks;
     rp.cnt = cnt;
@@ -1701,9 +1762,11 @@ extern "C" int pr_depth_map_noalloc(const pr_depth_map_desc* d) {
     rp.mode = kShadow;
     rp.smap = keys;
     rp.lastnan = lastnan;
+    rp.take = &cnt->take[0];
     if (!rc) rc = launch_raster(rp, sm_count() * 8, st);
     if (!rc) rc = launch_shadow_fixup_reset(d->width, d->height, lastnan, keys, cnt, st);
     rp.mode = kShadowFixup;
+    rp.take = &cnt->take[1];
     if (!rc) rc = launch_raster(rp, sm_count() * 8, st);
     if (rc) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: kernel launch failed");
     Counters h{};

@@ -18,7 +18,7 @@ constexpr int kMaxLights = 16;
 constexpr int kClipCnt = kMaxLights + 1;
 constexpr int kNumCounters = kMaxLights + 2;
 constexpr int kMaxAmbient = 16;
-constexpr uint32_t kTaskShift = 10;  // a raster task is a 2^kTaskShift-pixel chunk of a bbox (default)
+constexpr uint32_t kTaskShift = 5;  // a raster task is a 2^kTaskShift-pixel chunk of a bbox (default)
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
 // Raster record: what the coverage/depth test of one (sub-)triangle needs.
@@ -57,7 +57,8 @@ struct Counters {
     uint32_t need_rec;    // records needed when overflow
     uint32_t need_tasks;  // tasks needed when overflow
     uint32_t n_ao;        // pixels listed for ambient occlusion
-    uint32_t pad[7];
+    uint32_t take[2];     // raster work-queue heads: the pass, its NaN fix-up pass
+    uint32_t pad[5];
 };
 
 struct LightK {
@@ -113,6 +114,8 @@ struct RasterParams {
     uint32_t* smap;            // shadow: orderable depth keys, index x + y*W
     uint32_t* lastnan;         // shadow: 1 + max seq of NaN-depth fragments, 0 if none
     uint32_t task_shift = kTaskShift;  // as the setup that wrote the tasks
+    uint32_t* take = nullptr;          // zeroed work-queue head (warps take 32 tasks at a time), or
+                                       // null: a static stride over the tasks
 };
 
 struct ShadeParams {
