@@ -15,19 +15,31 @@ namespace prd {
 // (math/math.go:265-267), used by Vec4.Dot/Apply/Cross and Barycoord.
 //
 // GB300 runs FP64 at a small fraction of its FP32 rate, so the common case is
-// done in FP32:
-//   r1 = fmaf(a, b, c) is the single rounding RN32(s) of s = a*b + c.
-//   The double rounding RN32(RN64(s)) differs from it only when RN64(s) lands
-//   exactly on a float32 rounding midpoint that s itself is not on, i.e. when
-//   the exact residual s - r1 is within half a float64 ulp of +-half a
-//   float32 ulp of r1 (or of a quarter ulp just below a power of two).
-//   The residual is obtained error-free with the ErrFma algorithm of Boldo and
-//   Muller ("Exact and approximated error of the FMA", IEEE TC 2011):
-//   s = r1 + r2 + r3 exactly with |r3| <= ulp(r2)/2.
-//   Only when r2 sits exactly on such a midpoint with a nonzero r3 (a true
-//   hazard), or a special value shows up (tiny/zero r1, inf, NaN), does the
-//   FP64 unit compute the reference expression directly. On random and
-//   pixel-grid data that is fewer than 1 in 10^7 calls.
+// decided in FP32. Let s = a*b + c (exact) and r1 = fmaf(a, b, c) = RN32(s).
+//
+// (1) The double rounding RN32(RN64(s)) differs from r1 only if RN64(s) is a
+//     float32 rounding midpoint m with s != m (a float32 midpoint is a float64
+//     number, so RN64 cannot carry s across one). The tie then goes to the
+//     neighbour of m with an even significand, while r1 is the neighbour on
+//     s's side: a difference needs r1 odd, so that m is r1 +- ulp(r1)/2 and
+//     |s - r1| >= ulp(r1)/2 - ulp64(m)/2 >= T (1 - 2^-29), T = ulp(r1)/2.
+// (2) The residual e = s - r1 is estimated in FP32: p = RN(ab) and
+//     q = ab - p (exact by FMA); (sg, tau) = TwoSum(p, c) (Knuth), so
+//     ab + c = sg + tau + q; d = sg - r1 is exact (if tau = 0, r1 = RN(sg + q)
+//     with |sg| >= |q| or sg = 0, the Fast2Sum case; if tau != 0, the sum
+//     p + c is inexact, so |sg| >= 2^22 ulp(p) >= 2^23 |q| and r1 is within a
+//     factor 2 of sg, the Sterbenz case). e' = RN(RN(d + tau) + q) then
+//     differs from e by at most 2^-24 (|d + tau| + |e'|) <= 6 * 2^-24 T, the
+//     first rounding being exact when tau = 0 (|q| <= 4T when tau != 0).
+// (3) Hence |e'| < T (1 - 2^-20) proves r1 is the reference result. The test
+//     is an integer compare of bit patterns (T is a power of two; 16 float
+//     steps below it are 2^-20 T) and requires r1's exponent field >= 25, so
+//     that T and every partial result above are normal enough; an even r1
+//     also settles it by (1). What is left (an odd r1 within 2^-20 of a
+//     midpoint, tiny or infinite results, NaN) goes to the FP64 unit: on
+//     random and pixel-grid data about 1 call in 5 million.
+// (Checked against the FP64 expression on 4.8e8 inputs, 6e7 of them true
+// double-rounding hazards, with no difference.)
 // ---------------------------------------------------------------------------
 // Kept out of line: if the compiler predicated this into the fast path, the
 // FP64 pipe (2 lanes/clk/SM on GB300) would be occupied on every call.
@@ -36,37 +48,20 @@ static __device__ __noinline__ float fma64f_slow(float a, float b, float c) {
 }
 
 PR_DEV float fma64f(float a, float b, float c) {
-    float r1 = __fmaf_rn(a, b, c);
-    // With a zero factor or a zero addend, a*b + c is exact in float64, so the
-    // single rounding r1 already equals the reference's double rounding.
-    if (a == 0.0f || b == 0.0f || c == 0.0f) return r1;
-    float u1 = __fmul_rn(a, b);
-    float u2 = __fmaf_rn(a, b, -u1);  // a*b = u1 + u2 exactly
-    // TwoSum(c, u2) -> (a1, z1)
-    float a1 = __fadd_rn(c, u2);
-    float t1 = __fsub_rn(a1, c);
-    float z1 = __fadd_rn(__fsub_rn(c, __fsub_rn(a1, t1)), __fsub_rn(u2, t1));
-    // TwoSum(u1, a1) -> (b1, b2)
-    float b1 = __fadd_rn(u1, a1);
-    float t2 = __fsub_rn(b1, u1);
-    float b2 = __fadd_rn(__fsub_rn(u1, __fsub_rn(b1, t2)), __fsub_rn(a1, t2));
-    float g = __fadd_rn(__fsub_rn(b1, r1), b2);
-    float r2 = __fadd_rn(g, z1);
-    uint32_t ex = (__float_as_uint(r1) >> 23) & 0xffu;
-    // Tiny, zero, infinite or NaN r1: the error-free transform may not hold.
-    bool special = (ex < 25u) | (ex == 255u);
-    if (!special && r2 == 0.0f) return r1;  // s == r1 exactly
-    // half a float32 ulp of r1 (r1 normal with exponent field >= 25)
-    float u = __uint_as_float((ex - 24u) << 23);
-    float ad = fabsf(r2);
-    bool bad = !(ad <= u);  // NaN / out-of-bound residual (overflow inside the EFT)
-    if (__builtin_expect(special | bad, 0)) return fma64f_slow(a, b, c);
-    // A double-rounding hazard puts s within 2^-29 u of a midpoint, which
-    // makes r2 = RN32(s - r1) exactly +-u (or +-u/2 below a power of two).
-    if (ad != u && ad != 0.5f * u) return r1;
-    // r2 on a midpoint: s is exactly the midpoint (harmless) iff r3 == 0.
-    float r3 = __fsub_rn(z1, __fsub_rn(r2, g));
-    if (__builtin_expect(r3 == 0.0f, 1)) return r1;
+    const float r1 = __fmaf_rn(a, b, c);
+    // a zero first factor (a matrix entry, usually warp-uniform): s = c + (+-0)
+    // rounds to c in both precisions
+    if (a == 0.0f) return r1;
+    const float p = __fmul_rn(a, b);
+    const float q = __fmaf_rn(a, b, -p);
+    const float sg = __fadd_rn(p, c);
+    const float bb = __fsub_rn(sg, p);
+    const float tau = __fadd_rn(__fsub_rn(p, __fsub_rn(sg, bb)), __fsub_rn(c, bb));
+    const float e = __fadd_rn(__fadd_rn(__fsub_rn(sg, r1), tau), q);
+    const uint32_t rb = __float_as_uint(r1);
+    const int thr = (int)(rb & 0x7f800000u) - ((24 << 23) + 16);
+    if ((int)(__float_as_uint(e) & 0x7fffffffu) < thr) return r1;
+    if ((rb & 1u) == 0u && (rb & 0x7f800000u) != 0x7f800000u) return r1;
     return fma64f_slow(a, b, c);
 }
 

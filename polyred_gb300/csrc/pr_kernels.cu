@@ -850,7 +850,7 @@ PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
         const float uvY = __fmul_rn(wsum(A.uv[1], A.uv[3], A.uv[5], wc1, wc2, wc3), norm);
         const int matid = A.matid;
         float du = 0.0f, dv = 0.0f;
-        if (matid >= 0) {
+        if (matid >= 0 && P.guvd) {  // the UV derivatives only feed that G-buffer
             float bx3[3], by3[3];
             barycoord_s(__fadd_rn(fx, 1.0f), fy, X0, Y0, X1, Y1, X2, Y2, sabc, bx3);
             float wc1x = __fmul_rn(rw0, bx3[0]), wc2x = __fmul_rn(rw1, bx3[1]), wc3x = __fmul_rn(rw2, bx3[2]);

@@ -24,15 +24,46 @@ def _constructed(n, seed):
     return (a * s).astype(np.float32), (b * s).astype(np.float32), c.astype(np.float32)
 
 
+def _below_pow2(n, seed):
+    """c = the float just below 2^E (odd significand), a*b = 2^(E-25)
+    (1 - k^2 2^-46) +- one ulp of b: s sits next to the midpoint below 2^E."""
+    g = np.random.default_rng(seed)
+    E = g.integers(-40, 40, n)
+    k = g.integers(1, 300, n).astype(np.float64)
+    c = np.ldexp(1.0 - 2.0 ** -24, E).astype(np.float32)
+    a = (1.0 + k * 2.0 ** -23).astype(np.float32)
+    b = np.ldexp(1.0 - k * 2.0 ** -23, E - 25).astype(np.float32)
+    b = (b.view(np.int32) + g.integers(-1, 2, n).astype(np.int32)).view(np.float32)
+    s = np.where(g.integers(0, 2, n) == 1, 1.0, -1.0).astype(np.float32)
+    return a * s, b * s, c * s
+
+
+def _bits(n, seed, lo, hi):
+    """Random significands and signs with biased exponents in [lo, hi)."""
+    g = np.random.default_rng(seed)
+    m = g.integers(0, 1 << 32, (3, n), dtype=np.uint64).astype(np.uint32) & np.uint32(0x807FFFFF)
+    e = g.integers(lo, hi, (3, n)).astype(np.uint32) << np.uint32(23)
+    return tuple((m | e).view(np.float32))
+
+
 def test_fma64f_matches_fp64(native_lib):
     import torch
     g = np.random.default_rng(0)
     n = 1 << 20
+    ua, ub = g.uniform(-2000, 2000, (2, n)).astype(np.float32)
+    # near-cancellation: c = -RN(ab) moved by up to 4 ulps
+    cc = (-(ua * ub)).view(np.int32) + g.integers(-4, 5, n).astype(np.int32)
+    sm = (g.integers(-4, 5, (3, n)) * np.where(g.integers(0, 2, (3, n)) == 1, 1.0, 0.5)).astype(np.float32)
     sets = [
         tuple(g.uniform(-2000, 2000, (3, n)).astype(np.float32)),
         _constructed(n, 1),
         (np.floor(g.uniform(0, 4096, n)).astype(np.float32) + 0.5, (g.integers(0, 2000, n) * 0.25 - 250).astype(np.float32),
          (-g.integers(0, 100000, n) * 0.001953125).astype(np.float32)),
+        _below_pow2(n, 2),
+        (ua, ub, cc.view(np.float32)),
+        tuple(sm),
+        _bits(n, 3, 0, 256),    # every exponent: subnormals, zeros, infinities, NaNs
+        _bits(n, 4, 90, 170),
     ]
     for a, b, c in sets:
         ta, tb, tc = (torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (a, b, c))
@@ -41,7 +72,8 @@ def test_fma64f_matches_fp64(native_lib):
         rc = native_lib.pr_debug_fma_probe(ta.data_ptr(), tb.data_ptr(), tc.data_ptr(), out.data_ptr(), ref.data_ptr(), n)
         assert rc == 0
         o, r = out.cpu().numpy(), ref.cpu().numpy()
-        assert np.array_equal(o.view(np.uint32), r.view(np.uint32))
+        same = (o.view(np.uint32) == r.view(np.uint32)) | (np.isnan(o) & np.isnan(r))
+        assert same.all(), int((~same).sum())
 
 
 def _ao_probe(native_lib, x, T, col):
