@@ -47,7 +47,10 @@ static __device__ __noinline__ float fma64f_slow(float a, float b, float c) {
     return __double2float_rn(__fma_rn((double)a, (double)b, (double)c));
 }
 
-PR_DEV float fma64f(float a, float b, float c) {
+// The certified FP32 result; sets *bad when (3) does not settle it. Callers
+// evaluate whole chains this way and redo the chain on the FP64 unit when any
+// step is unsettled, so the common path has no call and no per-step branch.
+PR_DEV float fma64f_try(float a, float b, float c, bool& bad) {
     const float r1 = __fmaf_rn(a, b, c);
     // a zero first factor (a matrix entry, usually warp-uniform): s = c + (+-0)
     // rounds to c in both precisions
@@ -60,9 +63,16 @@ PR_DEV float fma64f(float a, float b, float c) {
     const float e = __fadd_rn(__fadd_rn(__fsub_rn(sg, r1), tau), q);
     const uint32_t rb = __float_as_uint(r1);
     const int thr = (int)(rb & 0x7f800000u) - ((24 << 23) + 16);
-    if ((int)(__float_as_uint(e) & 0x7fffffffu) < thr) return r1;
-    if ((rb & 1u) == 0u && (rb & 0x7f800000u) != 0x7f800000u) return r1;
-    return fma64f_slow(a, b, c);
+    const bool ok = (int)(__float_as_uint(e) & 0x7fffffffu) < thr ||
+                    ((rb & 1u) == 0u && (rb & 0x7f800000u) != 0x7f800000u);
+    bad |= !ok;
+    return r1;
+}
+
+PR_DEV float fma64f(float a, float b, float c) {
+    bool bad = false;
+    const float r = fma64f_try(a, b, c, bad);
+    return __builtin_expect(bad, 0) ? fma64f_slow(a, b, c) : r;
 }
 
 // ---- Go conversions and polyred scalar helpers --------------------------
@@ -119,17 +129,29 @@ struct V4 { float x, y, z, w; };
 
 PR_DEV V4 sub4(V4 v, V4 u) { return {__fsub_rn(v.x, u.x), __fsub_rn(v.y, u.y), __fsub_rn(v.z, u.z), __fsub_rn(v.w, u.w)}; }
 PR_DEV V4 add4(V4 v, V4 u) { return {__fadd_rn(v.x, u.x), __fadd_rn(v.y, u.y), __fadd_rn(v.z, u.z), __fadd_rn(v.w, u.w)}; }
+// Vec4.Dot; the FP64 redo of a chain with an unsettled step is out of line.
+static __device__ __noinline__ float dot4_exact(V4 v, V4 u) {
+    return fma64f_slow(v.x, u.x, fma64f_slow(v.y, u.y, fma64f_slow(v.z, u.z, __fmul_rn(v.w, u.w))));
+}
 PR_DEV float dot4(V4 v, V4 u) {
-    return fma64f(v.x, u.x, fma64f(v.y, u.y, fma64f(v.z, u.z, __fmul_rn(v.w, u.w))));
+    bool bad = false;
+    const float r = fma64f_try(v.x, u.x, fma64f_try(v.y, u.y, fma64f_try(v.z, u.z, __fmul_rn(v.w, u.w), bad), bad), bad);
+    return __builtin_expect(bad, 0) ? dot4_exact(v, u) : r;
 }
 PR_DEV float len4(V4 v) { return __fsqrt_rn(dot4(v, v)); }  // sqrt in f64 then f32 == correctly rounded sqrtf
 PR_DEV V4 unit4(V4 v) {
     float n = __fdiv_rn(1.0f, len4(v));
     return {__fmul_rn(v.x, n), __fmul_rn(v.y, n), __fmul_rn(v.z, n), __fmul_rn(v.w, n)};
 }
+static __device__ __noinline__ V4 cross4_exact(V4 v, V4 u) {
+    return {fma64f_slow(v.y, u.z, -__fmul_rn(v.z, u.y)), fma64f_slow(v.z, u.x, -__fmul_rn(v.x, u.z)),
+            fma64f_slow(v.x, u.y, -__fmul_rn(v.y, u.x)), 0.0f};
+}
 PR_DEV V4 cross4(V4 v, V4 u) {
-    return {fma64f(v.y, u.z, -__fmul_rn(v.z, u.y)), fma64f(v.z, u.x, -__fmul_rn(v.x, u.z)),
-            fma64f(v.x, u.y, -__fmul_rn(v.y, u.x)), 0.0f};
+    bool bad = false;
+    const V4 r = {fma64f_try(v.y, u.z, -__fmul_rn(v.z, u.y), bad), fma64f_try(v.z, u.x, -__fmul_rn(v.x, u.z), bad),
+                  fma64f_try(v.x, u.y, -__fmul_rn(v.y, u.x), bad), 0.0f};
+    return __builtin_expect(bad, 0) ? cross4_exact(v, u) : r;
 }
 PR_DEV V4 pos4(V4 v) {
     if (v.w == 1.0f || v.w == 0.0f) return {v.x, v.y, v.z, 1.0f};
@@ -137,11 +159,19 @@ PR_DEV V4 pos4(V4 v) {
     return {__fmul_rn(v.x, iw), __fmul_rn(v.y, iw), __fmul_rn(v.z, iw), 1.0f};
 }
 // Vec4.Apply with a row-major matrix m[16]
+static __device__ __noinline__ V4 apply4_exact(V4 v, const float* m) {
+    return {fma64f_slow(m[0], v.x, fma64f_slow(m[1], v.y, fma64f_slow(m[2], v.z, __fmul_rn(m[3], v.w)))),
+            fma64f_slow(m[4], v.x, fma64f_slow(m[5], v.y, fma64f_slow(m[6], v.z, __fmul_rn(m[7], v.w)))),
+            fma64f_slow(m[8], v.x, fma64f_slow(m[9], v.y, fma64f_slow(m[10], v.z, __fmul_rn(m[11], v.w)))),
+            fma64f_slow(m[12], v.x, fma64f_slow(m[13], v.y, fma64f_slow(m[14], v.z, __fmul_rn(m[15], v.w))))};
+}
 PR_DEV V4 apply4(V4 v, const float* m) {
-    return {fma64f(m[0], v.x, fma64f(m[1], v.y, fma64f(m[2], v.z, __fmul_rn(m[3], v.w)))),
-            fma64f(m[4], v.x, fma64f(m[5], v.y, fma64f(m[6], v.z, __fmul_rn(m[7], v.w)))),
-            fma64f(m[8], v.x, fma64f(m[9], v.y, fma64f(m[10], v.z, __fmul_rn(m[11], v.w)))),
-            fma64f(m[12], v.x, fma64f(m[13], v.y, fma64f(m[14], v.z, __fmul_rn(m[15], v.w))))};
+    bool bad = false;
+    const V4 r = {fma64f_try(m[0], v.x, fma64f_try(m[1], v.y, fma64f_try(m[2], v.z, __fmul_rn(m[3], v.w), bad), bad), bad),
+                  fma64f_try(m[4], v.x, fma64f_try(m[5], v.y, fma64f_try(m[6], v.z, __fmul_rn(m[7], v.w), bad), bad), bad),
+                  fma64f_try(m[8], v.x, fma64f_try(m[9], v.y, fma64f_try(m[10], v.z, __fmul_rn(m[11], v.w), bad), bad), bad),
+                  fma64f_try(m[12], v.x, fma64f_try(m[13], v.y, fma64f_try(m[14], v.z, __fmul_rn(m[15], v.w), bad), bad), bad)};
+    return __builtin_expect(bad, 0) ? apply4_exact(v, m) : r;
 }
 // Mat4.MulV: plain float32 sums left to right
 PR_DEV V4 mulv(const float* m, V4 v) {

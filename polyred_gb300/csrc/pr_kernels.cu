@@ -1123,6 +1123,73 @@ PR_DEV bool ao_fast_groups(int n_groups, const int (*s_off)[kAoTable], const flo
     return true;
 }
 
+// The exact ratios of the taps of group g (taps 4g+2 .. 4g+5) whose upper
+// bound exceeds lb; returns their maximum (0 if none). Each lane loops over
+// its own such taps only.
+template <bool TINY>
+__device__ __noinline__ float ao_settle_group(const int (*s_off)[kAoTable], const float (*s_rhi)[kAoTable], int k, int g,
+                                              const float* p0, const float* pA, int tstar, float z, float pxf, float pyf,
+                                              float dX, float dY, float lb) {
+    const int t0 = 4 * g + 2;
+    float el[4];
+    unsigned m = 0;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        el[u] = ao_tap_elev(s_off, k, t0 + u, p0, pA, tstar, z, TINY);
+        if (__fmul_ru(el[u], s_rhi[k][4 * g + u]) > lb) m |= 1u << u;
+    }
+    float r = 0.0f;
+    while (m) {
+        const int u = __ffs(m) - 1;
+        m &= m - 1u;
+        const float e = u == 0 ? el[0] : (u == 1 ? el[1] : (u == 2 ? el[2] : el[3]));
+        r = fmaxf(r, ao_exact_ratio(t0 + u, e, pxf, pyf, dX, dY));
+    }
+    return r;
+}
+
+// The march of ao_fast_groups for frames without NaN depths, bookkept per
+// group of four taps: a group is a candidate when the largest upper bound of
+// its taps exceeds lb; it then raises lb by the largest lower bound of its
+// taps and becomes the pending group (bounded above by that largest upper
+// bound phi). A pending group is settled (its taps above lb evaluated
+// exactly) only when a later candidate's lower bound does not clear phi, and
+// at the end. Every tap above the final lb is thus evaluated exactly, and
+// best is the exact maximum.
+template <bool TINY>
+PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const float (*s_rlo)[kAoTable],
+                              const float (*s_rhi)[kAoTable], int k, const float* p0, const float* pA, int tstar,
+                              float z, float pxf, float pyf, float dX, float dY, float& best) {
+    float lb = best;
+    int pg = -1;
+    float phi = 0.0f;
+#pragma unroll 2
+    for (int g = 0; g < n_groups; g++) {
+        const int t0 = 4 * g + 2;
+        const int4 o = *reinterpret_cast<const int4*>(&s_off[k][4 * g]);
+        const float4 rh = *reinterpret_cast<const float4*>(&s_rhi[k][4 * g]);
+        const float* q0 = (TINY && t0 < tstar) ? pA : p0;
+        const float* q1 = (TINY && t0 + 1 < tstar) ? pA : p0;
+        const float* q2 = (TINY && t0 + 2 < tstar) ? pA : p0;
+        const float* q3 = (TINY && t0 + 3 < tstar) ? pA : p0;
+        const float e0 = __fsub_rn(__ldg(q0 + o.x), z), e1 = __fsub_rn(__ldg(q1 + o.y), z);
+        const float e2 = __fsub_rn(__ldg(q2 + o.z), z), e3 = __fsub_rn(__ldg(q3 + o.w), z);
+        const float gh = fmaxf(fmaxf(__fmul_ru(e0, rh.x), __fmul_ru(e1, rh.y)), fmaxf(__fmul_ru(e2, rh.z), __fmul_ru(e3, rh.w)));
+        if (gh > lb) {
+            const float4 rl = *reinterpret_cast<const float4*>(&s_rlo[k][4 * g]);
+            const float gl = fmaxf(fmaxf(__fmul_rd(e0, rl.x), __fmul_rd(e1, rl.y)), fmaxf(__fmul_rd(e2, rl.z), __fmul_rd(e3, rl.w)));
+            lb = fmaxf(lb, gl);
+            if (pg >= 0 && gl < phi) {
+                best = fmaxf(best, ao_settle_group<TINY>(s_off, s_rhi, k, pg, p0, pA, tstar, z, pxf, pyf, dX, dY, lb));
+                lb = fmaxf(lb, best);
+            }
+            pg = g;
+            phi = gh;
+        }
+    }
+    if (pg >= 0) best = fmaxf(best, ao_settle_group<TINY>(s_off, s_rhi, k, pg, p0, pA, tstar, z, pxf, pyf, dX, dY, lb));
+}
+
 // AmbientOcclusionShade (material/ao.go:20-73) for the pixels the shade
 // kernel listed, one thread per pixel. Per direction, maxangle is the Max
 // over taps of float32(Atan(elev/dist)); Atan and the rounding to float32 are
@@ -1184,6 +1251,8 @@ PR_DEV void ao_one(const AoParams& P, uint32_t j, const int (*s_off)[kAoTable], 
     const float* p0 = P.depth + i;
     const float z = *p0;
     const float pxf = small_u2f((uint32_t)x), pyf = small_u2f((uint32_t)y);
+    // no NaN-depth fragment reached this frame's depth buffer (the raster flags every one)
+    const bool nan_free = P.cnt->nan_flag == 0u;
     float total = 0.0f;
     bool nanpix = false;
     for (int k = 0; k < P.n_dirs; k++) {
@@ -1241,7 +1310,12 @@ PR_DEV void ao_one(const AoParams& P, uint32_t j, const int (*s_off)[kAoTable], 
                         lo = mid + 1;
                 }
                 const float* pA = p0 + (tiny == 1 ? 1 : -W);
-                ok = ao_fast_groups<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
+                if (nan_free)
+                    ao_fast_groups_nf<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
+                else
+                    ok = ao_fast_groups<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
+            } else if (nan_free) {
+                ao_fast_groups_nf<false>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
             } else {
                 ok = ao_fast_groups<false>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
             }
