@@ -9,7 +9,8 @@ sRGB gamma. Metric: Mtri/s = input triangles per second of frame time.
          device outputs), CUDA events on the library's stream
   e2e    the same through the public C ABI with host buffers: every step
          uploads the triangle soup from pinned host memory (pr_scene_upload)
-         and reads back RGBA8 + triangle IDs + depth (pr_render)
+         and reads back RGBA8 + triangle IDs + depth (pr_render) into
+         page-locked buffers from pr_host_alloc
   --impl reference  the CPU restatement of the reference renderer (oracle/),
          all host threads, single-worker draw order
 
@@ -472,26 +473,32 @@ def main():
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     phases = {"ms_shadow": [], "ms_setup": [], "ms_raster": [], "ms_shade": [], "ms_ao": [], "n_ao_pixels": []}
-    launches = 0
+    # frames back to back on the library's stream, as a frame loop issues them
     ev0.record(stream)
     for _ in range(args.steps):
         native.check(lib.pr_render_async(dev.handle, C.byref(fd.desc), C.byref(od)))
-        native.check(lib.pr_sync(dev.handle))
-        st = stats()
-        launches += st.n_kernel_launches
-        for k in phases:
-            phases[k].append(getattr(st, k))
     ev1.record(stream)
     barrier()
     clk = clocks.stop()
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, "cuda")
     value = job_throughput(N_TRIS, world, ms)
 
-    # per-phase device times (CUDA events inside the library, same stream)
+    # per-phase device times (CUDA events inside the library, same stream) and
+    # launch counts: three more frames, each synchronised so that its
+    # statistics can be read (not timed)
+    per_frame = 0
+    for _ in range(3):
+        native.check(lib.pr_render_async(dev.handle, C.byref(fd.desc), C.byref(od)))
+        native.check(lib.pr_sync(dev.handle))
+        st = stats()
+        per_frame = st.n_kernel_launches
+        for k in phases:
+            phases[k].append(getattr(st, k))
+    launches = per_frame * args.steps
     ph = {k: statistics.mean(v) for k, v in phases.items() if v}
 
-    # ---- end-to-end leg (public C ABI, host buffers) ----
-    out = render.Outputs(W, H, ("rgba", "tri_id", "depth"))
+    # ---- end-to-end leg (public C ABI, host buffers in page-locked memory) ----
+    out = render.Outputs(W, H, ("rgba", "tri_id", "depth"), pinned=True)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)

@@ -180,7 +180,7 @@ typedef struct pr_stats {
     uint32_t n_tris_in;
     uint32_t n_raster_tris;    /* after cull/clip, main view */
     uint32_t n_clipped_tris;   /* input triangles that went through clipTriangle */
-    uint32_t n_raster_tasks;   /* raster work items (pixel-box chunks of <= 1024 px), all passes */
+    uint32_t n_raster_tasks;   /* raster work items (pixel-box chunks of <= 32 px), all passes */
     uint32_t n_nan_fragments;  /* fragments with NaN depth (degenerate triangles) */
     uint32_t n_kernel_launches;
     uint32_t reserved;
@@ -227,6 +227,14 @@ int pr_frame_stats(void* ctx, pr_stats* out);
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that
  * time or order work around it. */
 int pr_stream(void* ctx, void** out_stream);
+
+/* Page-locked host memory (cudaHostAlloc) for scene arrays and frame
+ * outputs: copies from and to it run at the link's full rate instead of
+ * through the driver's staging buffers. bytes > 0; free with pr_host_free.
+ * (The reference keeps its frame buffers in ordinary Go memory,
+ * render/raster.go:99-118; a Go host passes these instead.) */
+int pr_host_alloc(size_t bytes, void** out_ptr);
+int pr_host_free(void* ptr);
 
 /* ---- host math helpers --------------------------------------------------
  * f32 arithmetic exactly as the reference's Go (amd64) evaluates it, so a

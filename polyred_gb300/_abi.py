@@ -174,6 +174,8 @@ ENTRY_POINTS = [
     ("pr_sync", C.c_int, [VP]),
     ("pr_frame_stats", C.c_int, [VP, C.POINTER(pr_stats)]),
     ("pr_stream", C.c_int, [VP, C.POINTER(VP)]),
+    ("pr_host_alloc", C.c_int, [C.c_size_t, C.POINTER(VP)]),
+    ("pr_host_free", C.c_int, [VP]),
     ("pr_view_matrix", C.c_int, [FP, FP, FP, FP]),
     ("pr_perspective_matrix", C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, FP]),
     ("pr_orthographic_matrix", C.c_int, [C.c_float] * 6 + [FP]),

@@ -822,6 +822,24 @@ int pr_stream(void* ctx, void** out_stream) {
     return PR_OK;
 }
 
+int pr_host_alloc(size_t bytes, void** out_ptr) {
+    if (!out_ptr || bytes == 0) return fail(PR_ERR_INVALID_ARG, "NULL out_ptr or zero bytes");
+    *out_ptr = nullptr;
+    cudaError_t e = cudaHostAlloc(out_ptr, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        *out_ptr = nullptr;
+        return fail(PR_ERR_CUDA, "cudaHostAlloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return PR_OK;
+}
+
+int pr_host_free(void* ptr) {
+    if (!ptr) return fail(PR_ERR_INVALID_ARG, "ptr is NULL");
+    cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) return fail(PR_ERR_CUDA, "cudaFreeHost: %s", cudaGetErrorString(e));
+    return PR_OK;
+}
+
 int pr_view_matrix(const float pos[3], const float target[3], const float up[3], float out[16]) {
     if (!pos || !target || !up || !out) return fail(PR_ERR_INVALID_ARG, "NULL argument");
     M4 m = prh::view_matrix(pos, target, up);

@@ -143,6 +143,8 @@ var (
 	prLastError    func() string
 	prViewMatrix   func(pos, target, up *float32, out *float32) int32
 	prShadowCamera func(lightPos, center, view, proj, outView, outProj *float32) int32
+	prHostAlloc    func(bytes uintptr, out *unsafe.Pointer) int32
+	prHostFree     func(p unsafe.Pointer) int32
 )
 
 // LibraryPath is where Open looks for the library unless POLYRED_CUDA_LIB
@@ -168,6 +170,8 @@ func load() error {
 		purego.RegisterLibFunc(&prLastError, lib, "pr_last_error")
 		purego.RegisterLibFunc(&prViewMatrix, lib, "pr_view_matrix")
 		purego.RegisterLibFunc(&prShadowCamera, lib, "pr_shadow_camera")
+		purego.RegisterLibFunc(&prHostAlloc, lib, "pr_host_alloc")
+		purego.RegisterLibFunc(&prHostFree, lib, "pr_host_free")
 	})
 	return loadErr
 }
@@ -272,4 +276,26 @@ func ShadowCamera(lightPos, center [3]float32, view, proj [16]float32) (v, p [16
 	}
 	err = check(prShadowCamera(&lightPos[0], &center[0], &view[0], &proj[0], &v[0], &p[0]))
 	return
+}
+
+// HostAlloc returns n bytes of page-locked host memory (pr_host_alloc) for
+// frame outputs and scene arrays: the device copies to and from it at the
+// link's full rate. The memory is outside the Go heap; free it with HostFree.
+func HostAlloc(n uintptr) (unsafe.Pointer, error) {
+	if err := load(); err != nil {
+		return nil, err
+	}
+	var p unsafe.Pointer
+	if err := check(prHostAlloc(n, &p)); err != nil {
+		return nil, err
+	}
+	return p, nil
+}
+
+// HostFree releases memory from HostAlloc.
+func HostFree(p unsafe.Pointer) error {
+	if err := load(); err != nil {
+		return err
+	}
+	return check(prHostFree(p))
 }

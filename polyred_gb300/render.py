@@ -238,25 +238,47 @@ class FrameDesc:
         self.desc = f
 
 
+def _free_host(lib, ptrs):
+    for p in ptrs:
+        lib.pr_host_free(p)
+
+
+def host_array(shape, dtype):
+    """A zeroed numpy array in page-locked memory from pr_host_alloc (freed
+    with the array's last reference)."""
+    lib = native.load()
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    ptr = C.c_void_p()
+    native.check(lib.pr_host_alloc(max(n, 1), C.byref(ptr)))
+    buf = (C.c_uint8 * max(n, 1)).from_address(ptr.value)
+    a = np.frombuffer(buf, np.uint8, n).view(dtype).reshape(shape)
+    a[...] = 0
+    weakref.finalize(buf, _free_host, lib, [ptr.value])
+    return a
+
+
 class Outputs:
-    """Host arrays a frame writes (pr_outputs)."""
+    """Host arrays a frame writes (pr_outputs); pinned=True places them in
+    page-locked memory (pr_host_alloc), which the device writes at full link
+    speed."""
 
     FIELDS = {"rgba": (4, np.uint8), "tri_id": (1, np.uint32), "depth": (1, F32), "nor": (4, F32),
               "face_nor": (4, F32), "world_pos": (4, F32), "uvd": (4, F32), "vcol": (4, np.uint8),
               "mat_id": (1, np.int32)}
 
-    def __init__(self, width, height, want=("rgba",), n_shadow=0, shadow_size=None):
+    def __init__(self, width, height, want=("rgba",), n_shadow=0, shadow_size=None, pinned=False):
         self.arrays = {}
         o = _abi.pr_outputs()
         o.size = C.sizeof(_abi.pr_outputs)
         o.flags = 0
+        alloc = host_array if pinned else np.zeros
         for name in want:
             if name == "shadow_maps":
                 sw, sh = shadow_size
-                a = np.zeros((max(n_shadow, 1), sh, sw), F32)
+                a = alloc((max(n_shadow, 1), sh, sw), F32)
             else:
                 k, dt = self.FIELDS[name]
-                a = np.zeros((height, width, k) if k > 1 else (height, width), dt)
+                a = alloc((height, width, k) if k > 1 else (height, width), dt)
             self.arrays[name] = a
             setattr(o, name, a.ctypes.data)
         self.desc = o

@@ -68,6 +68,8 @@ def test_null_arguments_are_errors(native_lib):
     assert native_lib.pr_scene_upload(None, None) == _abi.PR_ERR_INVALID_ARG
     assert native_lib.pr_view_matrix(None, None, None, None) == _abi.PR_ERR_INVALID_ARG
     assert b"NULL" in native_lib.pr_last_error()
+    assert native_lib.pr_host_alloc(16, None) == _abi.PR_ERR_INVALID_ARG
+    assert native_lib.pr_host_free(None) == _abi.PR_ERR_INVALID_ARG
 
 
 def test_singular_inverse(native_lib):

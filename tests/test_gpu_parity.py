@@ -270,3 +270,24 @@ def test_triangle_soup_full_size(device):
     assert (cpu["tri_id"] != 0xFFFFFFFF).sum() > 0.5 * W * H
     assert p.stats["n_raster_tris"] > 5_000_000
     assert_bitexact(gpu, cpu)
+
+
+def test_pinned_outputs_match_pageable(device):
+    """Outputs in page-locked memory (pr_host_alloc) receive the same frame."""
+    import ctypes as C
+    from polyred_gb300 import native, render
+    lib = native.load()
+    s, cam = procedural.small_scene(320, 200)
+    o = options(s, cam, 320, 200)
+    flat = render.FlatScene(s)
+    d = flat.desc()
+    native.check(lib.pr_scene_upload(device.handle, C.byref(d)))
+    fd = render.FrameDesc(o, {})
+    names = ("rgba", "tri_id", "depth", "nor", "world_pos")
+    a = render.Outputs(320, 200, names)
+    b = render.Outputs(320, 200, names, pinned=True)
+    for out in (a, b):
+        native.check(lib.pr_render(device.handle, C.byref(fd.desc), C.byref(out.desc)))
+    for n in names:
+        assert np.array_equal(a.arrays[n].view(np.uint8), b.arrays[n].view(np.uint8)), n
+    assert (b.arrays["tri_id"] != 0xFFFFFFFF).sum() > 1000
