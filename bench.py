@@ -8,9 +8,11 @@ sRGB gamma. Metric: Mtri/s = input triangles per second of frame time.
   value  frames rendered with the scene resident in HBM (pr_render_async into
          device outputs), CUDA events on the library's stream
   e2e    the same through the public C ABI with host buffers: every step
-         uploads the triangle soup from pinned host memory (pr_scene_upload)
-         and reads back RGBA8 + triangle IDs + depth (pr_render) into
-         page-locked buffers from pr_host_alloc
+         uploads the triangle soup from pinned host memory and reads back
+         RGBA8 + triangle IDs + depth into page-locked buffers from
+         pr_host_alloc (pr_frame_submit: the next step's upload overlaps the
+         current frame), timed from before the first upload to after the
+         last readback
   --impl reference  the CPU restatement of the reference renderer (oracle/),
          all host threads, single-worker draw order
 
@@ -503,8 +505,9 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        native.check(lib.pr_scene_upload(dev.handle, C.byref(desc)))
-        native.check(lib.pr_render(dev.handle, C.byref(fd.desc), C.byref(out.desc)))
+        # upload + frame + readback; the next step's upload overlaps this frame
+        native.check(lib.pr_frame_submit(dev.handle, C.byref(desc), C.byref(fd.desc), C.byref(out.desc)))
+    native.check(lib.pr_sync(dev.handle))
     e1.record(stream)
     barrier()
     ems = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, "cuda")

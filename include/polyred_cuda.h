@@ -221,6 +221,21 @@ int pr_render(void* ctx, const pr_frame_desc* frame, pr_outputs* out);
 int pr_render_async(void* ctx, const pr_frame_desc* frame, pr_outputs* out);
 int pr_sync(void* ctx);
 
+/* pr_scene_upload + pr_render in one call that does not wait: the scene is
+ * copied on a stream of its own into the context's second set of scene
+ * buffers while the previous frame is still computing, the frame is queued
+ * behind it, and host outputs are copied back on a third stream while the
+ * next frame computes. The scene's arrays and host outputs must stay valid
+ * and unchanged until pr_sync (page-locked memory from pr_host_alloc moves
+ * at the link's full rate); outputs may also be device pointers
+ * (PR_OUT_DEVICE_PTRS). Like pr_scene_upload it starts the shadow maps from
+ * zero; shadow_maps output is not available. Capacities are not grown here:
+ * size them with one synchronous pr_render of a similar scene first;
+ * pr_sync reports a frame that overflowed. The reference walks the scene
+ * anew in every Render() (render/raster.go:241-271), so a frame loop that
+ * changes its scene every frame maps to this call. */
+int pr_frame_submit(void* ctx, const pr_scene_desc* scene, const pr_frame_desc* frame, pr_outputs* out);
+
 /* Counters of the last frame rendered on this context. */
 int pr_frame_stats(void* ctx, pr_stats* out);
 

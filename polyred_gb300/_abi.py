@@ -172,6 +172,7 @@ ENTRY_POINTS = [
     ("pr_render", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_outputs)]),
     ("pr_render_async", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_outputs)]),
     ("pr_sync", C.c_int, [VP]),
+    ("pr_frame_submit", C.c_int, [VP, C.POINTER(pr_scene_desc), C.POINTER(pr_frame_desc), C.POINTER(pr_outputs)]),
     ("pr_frame_stats", C.c_int, [VP, C.POINTER(pr_stats)]),
     ("pr_stream", C.c_int, [VP, C.POINTER(VP)]),
     ("pr_host_alloc", C.c_int, [C.c_size_t, C.POINTER(VP)]),

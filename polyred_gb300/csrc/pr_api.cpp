@@ -75,13 +75,34 @@ struct DevBuf {
     }
 };
 
-struct Ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::mutex mu;
-    // scene
+// Page-locked host memory that grows on demand.
+struct HostBuf {
+    uint8_t* p = nullptr;
+    size_t n = 0;
+    int ensure(size_t want) {
+        if (want <= n && p) return PR_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (cudaHostAlloc((void**)&p, std::max<size_t>(want, 1), cudaHostAllocDefault) != cudaSuccess) {
+            p = nullptr;
+            return fail(PR_ERR_OOM, "cudaHostAlloc(%zu bytes) failed", want);
+        }
+        n = std::max<size_t>(want, 1);
+        return PR_OK;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+// One device copy of a scene: the triangle arrays, the per-object tables,
+// the material table and the Triangle.IsValid flags. A context holds two, so
+// that pr_frame_submit can fill one while the frame in flight reads the other.
+struct SceneBufs {
     uint32_t n_tris = 0;
-    bool has_scene = false;
     std::vector<pr_object> objects;
     std::vector<pr_material> materials;
     DevBuf<float4> pos, nor;
@@ -93,6 +114,29 @@ struct Ctx {
     DevBuf<float> obj_model, obj_normal;
     DevBuf<int32_t> obj_matbase;
     DevBuf<pr_material> dmats;
+    HostBuf tables;                        // page-locked staging of the small tables (submitted uploads)
+    cudaEvent_t ev_uploaded = nullptr;     // the upload into these buffers has landed
+    cudaEvent_t ev_released = nullptr;     // the last frame that read them is past shading
+    void release() {
+        pos.release(); nor.release(); uv.release(); col.release(); mat.release();
+        obj_first.release(); tri_flags.release(); obj_model.release(); obj_normal.release();
+        obj_matbase.release(); dmats.release(); tables.release();
+        if (ev_uploaded) cudaEventDestroy(ev_uploaded);
+        if (ev_released) cudaEventDestroy(ev_released);
+        ev_uploaded = ev_released = nullptr;
+    }
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    // scene: sb is the one frames read; pr_frame_submit fills sb_back, then swaps
+    bool has_scene = false;
+    SceneBufs sb, sb_back;
+    // submitted frames: scene uploads and host-output copies on their own streams
+    cudaStream_t stream_u = nullptr, stream_d = nullptr;
+    cudaEvent_t ev_frame = nullptr, ev_d2h = nullptr;
     // raster work space
     DevBuf<prk::RasterRec> rrec;
     DevBuf<prk::AttrRec> arec;
@@ -179,6 +223,69 @@ int upload(DevBuf<T>& b, const void* src, size_t n, bool dev_src, cudaStream_t s
     return PR_OK;
 }
 
+// Copy a scene into b on stream st: the triangle arrays, the per-object
+// Model and Normal = Model.Inv().T() (render/raster.go:242-243), the
+// material table, and the Triangle.IsValid flags. staged: the small host
+// tables go through b's page-locked staging, so nothing waits for the copy;
+// otherwise the caller synchronises st before they go out of scope.
+int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool staged) {
+    int rc;
+    const bool dev = (s->flags & PR_SCENE_DEVICE_PTRS) != 0;
+    const uint32_t n = s->n_tris, no = s->n_objects, nm = s->n_materials;
+    std::vector<uint32_t> first(no + 1);
+    std::vector<float> model((size_t)no * 16), normal((size_t)no * 16);
+    std::vector<int32_t> mb(no);
+    for (uint32_t o = 0; o < no; o++) {
+        first[o] = s->objects[o].first_tri;
+        M4 m = loadm(s->objects[o].model), mi;
+        if (!prh::inv(m, &mi)) return fail(PR_ERR_SINGULAR, "object %u: model matrix is singular", o);
+        M4 nm4 = prh::transpose(mi);
+        std::memcpy(&model[(size_t)o * 16], m.m, 64);
+        std::memcpy(&normal[(size_t)o * 16], nm4.m, 64);
+        mb[o] = s->objects[o].mat_base;
+    }
+    first[no] = n;
+    if ((rc = upload(b.pos, s->pos, (size_t)n * 3, dev, st))) return rc;
+    if ((rc = upload(b.nor, s->nor, (size_t)n * 3, dev, st))) return rc;
+    if ((rc = upload(b.uv, s->uv, (size_t)n * 3, dev, st))) return rc;
+    if ((rc = upload(b.col, s->col, (size_t)n * 3, dev, st))) return rc;
+    if ((rc = upload(b.mat, s->mat_id, (size_t)n, dev, st))) return rc;
+    const void* t_first = first.data();
+    const void* t_model = model.data();
+    const void* t_normal = normal.data();
+    const void* t_mb = mb.data();
+    const void* t_mats = s->materials;
+    if (staged) {
+        auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
+        const size_t o_first = 0, o_model = al(o_first + first.size() * 4), o_normal = o_model + model.size() * 4,
+                     o_mb = o_normal + normal.size() * 4, o_mats = al(o_mb + mb.size() * 4),
+                     total = o_mats + (size_t)nm * sizeof(pr_material);
+        if ((rc = b.tables.ensure(total))) return rc;
+        uint8_t* h = b.tables.p;
+        std::memcpy(h + o_first, first.data(), first.size() * 4);
+        std::memcpy(h + o_model, model.data(), model.size() * 4);
+        std::memcpy(h + o_normal, normal.data(), normal.size() * 4);
+        std::memcpy(h + o_mb, mb.data(), mb.size() * 4);
+        if (nm) std::memcpy(h + o_mats, s->materials, (size_t)nm * sizeof(pr_material));
+        t_first = h + o_first;
+        t_model = h + o_model;
+        t_normal = h + o_normal;
+        t_mb = h + o_mb;
+        t_mats = h + o_mats;
+    }
+    if ((rc = upload(b.obj_first, t_first, first.size(), false, st))) return rc;
+    if ((rc = upload(b.obj_model, t_model, model.size(), false, st))) return rc;
+    if ((rc = upload(b.obj_normal, t_normal, normal.size(), false, st))) return rc;
+    if ((rc = upload(b.obj_matbase, t_mb, mb.size(), false, st))) return rc;
+    if ((rc = upload(b.dmats, t_mats, nm, false, st))) return rc;
+    if ((rc = b.tri_flags.ensure(std::max<uint32_t>(n, 1)))) return rc;
+    KTRY(prk::launch_tri_flags(b.pos.p, n, b.tri_flags.p, st));
+    b.objects.assign(s->objects, s->objects + no);
+    b.materials.assign(s->materials, s->materials + nm);
+    b.n_tris = n;
+    return PR_OK;
+}
+
 int ensure_frame(Ctx* c, int W, int H) {
     size_t n = (size_t)W * H;
     int rc;
@@ -213,18 +320,18 @@ int ensure_work(Ctx* c, uint32_t need_rec, uint32_t need_tasks) {
 }
 
 void fill_scene_ptrs(Ctx* c, prk::SetupParams& p) {
-    p.pos = c->pos.p;
-    p.nor = c->nor.p;
-    p.uv = c->uv.p;
-    p.col = c->col.p;
-    p.mat = c->mat.p;
-    p.obj_first = c->obj_first.p;
-    p.obj_model = c->obj_model.p;
-    p.obj_normal = c->obj_normal.p;
-    p.obj_matbase = c->obj_matbase.p;
-    p.tri_flags = c->tri_flags.p;
-    p.n_tris = c->n_tris;
-    p.n_objects = (uint32_t)c->objects.size();
+    p.pos = c->sb.pos.p;
+    p.nor = c->sb.nor.p;
+    p.uv = c->sb.uv.p;
+    p.col = c->sb.col.p;
+    p.mat = c->sb.mat.p;
+    p.obj_first = c->sb.obj_first.p;
+    p.obj_model = c->sb.obj_model.p;
+    p.obj_normal = c->sb.obj_normal.p;
+    p.obj_matbase = c->sb.obj_matbase.p;
+    p.tri_flags = c->sb.tri_flags.p;
+    p.n_tris = c->sb.n_tris;
+    p.n_objects = (uint32_t)c->sb.objects.size();
 }
 
 int validate_frame(const Ctx* c, const pr_frame_desc* f) {
@@ -269,8 +376,8 @@ void fill_shade_frame(const Ctx* c, const pr_frame_desc* f, const M4& s2w, int S
     sp.W = f->width;
     sp.H = f->height;
     sp.flags = f->flags;
-    sp.mats = c->dmats.p;
-    sp.n_mats = (uint32_t)c->materials.size();
+    sp.mats = c->sb.dmats.p;
+    sp.n_mats = (uint32_t)c->sb.materials.size();
     sp.n_lights = (int)f->n_lights;
     sp.n_ambient = (int)f->n_ambient;
     for (uint32_t l = 0; l < f->n_lights; l++) {
@@ -313,18 +420,33 @@ int frame_mats(const pr_frame_desc* f, FrameMats& m) {
     return PR_OK;
 }
 
+// The requested outputs from the staging buffers to the caller's host memory.
+int copy_host_outputs(Ctx* c, const pr_outputs* out, size_t npx, cudaStream_t st) {
+    if (out->rgba) CUDA_TRY(cudaMemcpyAsync(out->rgba, c->o_rgba.p, npx * 4, cudaMemcpyDeviceToHost, st));
+    if (out->tri_id) CUDA_TRY(cudaMemcpyAsync(out->tri_id, c->o_tri.p, npx * 4, cudaMemcpyDeviceToHost, st));
+    if (out->depth) CUDA_TRY(cudaMemcpyAsync(out->depth, c->o_depth.p, npx * 4, cudaMemcpyDeviceToHost, st));
+    if (out->nor) CUDA_TRY(cudaMemcpyAsync(out->nor, c->o_nor.p, npx * 16, cudaMemcpyDeviceToHost, st));
+    if (out->face_nor) CUDA_TRY(cudaMemcpyAsync(out->face_nor, c->o_fnor.p, npx * 16, cudaMemcpyDeviceToHost, st));
+    if (out->world_pos) CUDA_TRY(cudaMemcpyAsync(out->world_pos, c->o_wpos.p, npx * 16, cudaMemcpyDeviceToHost, st));
+    if (out->uvd) CUDA_TRY(cudaMemcpyAsync(out->uvd, c->o_uvd.p, npx * 16, cudaMemcpyDeviceToHost, st));
+    if (out->vcol) CUDA_TRY(cudaMemcpyAsync(out->vcol, c->o_vcol.p, npx * 4, cudaMemcpyDeviceToHost, st));
+    if (out->mat_id) CUDA_TRY(cudaMemcpyAsync(out->mat_id, c->o_mat.p, npx * 4, cudaMemcpyDeviceToHost, st));
+    return PR_OK;
+}
+
 // Extra outputs of a differentiable forward frame.
 struct DiffHooks {
     float4* dgb;  // [H][W][4] differentiation G-buffer
 };
 
-int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, const DiffHooks* dh = nullptr) {
+int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, const DiffHooks* dh = nullptr,
+                bool submit = false) {
     int rc = validate_frame(c, f);
     if (rc) return rc;
     if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
     if (out && out->size < sizeof(pr_outputs)) return fail(PR_ERR_INVALID_ARG, "outputs->size too small");
     bool out_dev = out && (out->flags & PR_OUT_DEVICE_PTRS);
-    if (!sync && out && !out_dev) return fail(PR_ERR_INVALID_ARG, "pr_render_async needs device output pointers");
+    if (!sync && !submit && out && !out_dev) return fail(PR_ERR_INVALID_ARG, "pr_render_async needs device output pointers");
     cudaStream_t st = c->stream;
     const int W = f->width, H = f->height;
     const int SW = f->shadow_width > 0 ? f->shadow_width : W;
@@ -344,10 +466,10 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
 
     if ((rc = set_device(c))) return rc;
     if ((rc = ensure_frame(c, W, H))) return rc;
-    uint32_t need_rec0 = c->n_tris + c->n_tris / 8 + 1024;
+    uint32_t need_rec0 = c->sb.n_tris + c->sb.n_tris / 8 + 1024;
     if ((rc = ensure_work(c, need_rec0, need_rec0))) return rc;
-    if ((rc = c->first_rec.ensure(std::max<uint32_t>(c->n_tris, 1)))) return rc;
-    if ((rc = c->clip_list.ensure(std::max<uint32_t>(c->n_tris, 1)))) return rc;
+    if ((rc = c->first_rec.ensure(std::max<uint32_t>(c->sb.n_tris, 1)))) return rc;
+    if ((rc = c->clip_list.ensure(std::max<uint32_t>(c->sb.n_tris, 1)))) return rc;
 
     // Shadow maps: allocated zeroed, reset when their geometry changes
     // (initShadowMaps, render/shadow.go:87), never cleared by a frame.
@@ -369,7 +491,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
     size_t npx = (size_t)W * H;
     c->stats = pr_stats{};
     c->stats.size = sizeof(pr_stats);
-    c->stats.n_tris_in = c->n_tris;
+    c->stats.n_tris_in = c->sb.n_tris;
     uint32_t launches = 0;
 
     {
@@ -399,7 +521,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 sp.cap_tasks = c->cap_tasks;
                 sp.first_rec = nullptr;
                 sp.cnt = dcnt + 1 + l;
-                if (c->n_tris > c->cap_rec) return fail(PR_ERR_OVERFLOW, "record capacity below triangle count");
+                if (c->sb.n_tris > c->cap_rec) return fail(PR_ERR_OVERFLOW, "record capacity below triangle count");
                 uint32_t* plane = c->smap.p + (size_t)SW * SH * l;
                 CUDA_TRY(cudaMemsetAsync(c->lastnan.p, 0, (size_t)SW * SH * 4, ss));
                 KTRY(prk::launch_setup_shadow(sp, ss));
@@ -443,7 +565,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         mp.first_rec = c->first_rec.p;
         mp.cnt = dcnt;
         if (dh) {
-            if ((rc = c->tri_scr.ensure((size_t)std::max<uint32_t>(c->n_tris, 1) * 12))) return rc;
+            if ((rc = c->tri_scr.ensure((size_t)std::max<uint32_t>(c->sb.n_tris, 1) * 12))) return rc;
             mp.tri_scr = c->tri_scr.p;
         }
         CUDA_TRY(cudaMemsetAsync(c->keys.p, 0, npx * 8, st));
@@ -532,8 +654,10 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             if (out->mat_id) { if ((rc = c->o_mat.ensure(npx))) return rc; sp.gmat = c->o_mat.p; }
         }
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_join, 0));  // the shadow maps are complete
+        CUDA_TRY(cudaStreamWaitEvent(st, c->ev_d2h, 0));   // a submitted frame's outputs left the staging
         KTRY(prk::launch_shade(sp, st));
         launches += 1;
+        CUDA_TRY(cudaEventRecord(c->sb.ev_released, st));  // the scene buffers are read no more
         CUDA_TRY(cudaEventRecord(c->ev[5], st));
         if (sp.rgba) {
             // AmbientOcclusionShade + gamma for the pixels the shade kernel listed
@@ -556,6 +680,13 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         CUDA_TRY(cudaMemcpyAsync(c->h_cnt, dcnt, sizeof(prk::Counters) * prk::kNumCounters, cudaMemcpyDeviceToHost, st));
         if (!sync) {
             c->stats.n_kernel_launches = launches;
+            if (submit && out && !out_dev) {
+                // host outputs leave on their own stream, beside the next frame
+                CUDA_TRY(cudaEventRecord(c->ev_frame, st));
+                CUDA_TRY(cudaStreamWaitEvent(c->stream_d, c->ev_frame, 0));
+                if ((rc = copy_host_outputs(c, out, npx, c->stream_d))) return rc;
+                CUDA_TRY(cudaEventRecord(c->ev_d2h, c->stream_d));
+            }
             return PR_OK;
         }
         CUDA_TRY(cudaStreamSynchronize(st));
@@ -576,17 +707,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
     collect_stats(c);
 
     // ---- host outputs ----
-    if (out && !out_dev) {
-        if (out->rgba) CUDA_TRY(cudaMemcpyAsync(out->rgba, c->o_rgba.p, npx * 4, cudaMemcpyDeviceToHost, st));
-        if (out->tri_id) CUDA_TRY(cudaMemcpyAsync(out->tri_id, c->o_tri.p, npx * 4, cudaMemcpyDeviceToHost, st));
-        if (out->depth) CUDA_TRY(cudaMemcpyAsync(out->depth, c->o_depth.p, npx * 4, cudaMemcpyDeviceToHost, st));
-        if (out->nor) CUDA_TRY(cudaMemcpyAsync(out->nor, c->o_nor.p, npx * 16, cudaMemcpyDeviceToHost, st));
-        if (out->face_nor) CUDA_TRY(cudaMemcpyAsync(out->face_nor, c->o_fnor.p, npx * 16, cudaMemcpyDeviceToHost, st));
-        if (out->world_pos) CUDA_TRY(cudaMemcpyAsync(out->world_pos, c->o_wpos.p, npx * 16, cudaMemcpyDeviceToHost, st));
-        if (out->uvd) CUDA_TRY(cudaMemcpyAsync(out->uvd, c->o_uvd.p, npx * 16, cudaMemcpyDeviceToHost, st));
-        if (out->vcol) CUDA_TRY(cudaMemcpyAsync(out->vcol, c->o_vcol.p, npx * 4, cudaMemcpyDeviceToHost, st));
-        if (out->mat_id) CUDA_TRY(cudaMemcpyAsync(out->mat_id, c->o_mat.p, npx * 4, cudaMemcpyDeviceToHost, st));
-    }
+    if (out && !out_dev && (rc = copy_host_outputs(c, out, npx, st))) return rc;
     if (out && out->shadow_maps) {
         size_t ns = (size_t)SW * SH * NL;
         if (!shadows || !c->smap_valid) {
@@ -655,7 +776,15 @@ int pr_create(int device, void** out_ctx) {
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream_c, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_setup, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_clip, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c->ev_clip, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream_u, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream_d, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_frame, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_d2h, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->sb.ev_uploaded, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->sb.ev_released, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->sb_back.ev_uploaded, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->sb_back.ev_released, cudaEventDisableTiming) != cudaSuccess) {
         pr_destroy(c);
         return fail(PR_ERR_CUDA, "stream/event creation failed");
     }
@@ -682,10 +811,15 @@ int pr_destroy(void* ctx) {
     if (!c) return fail(PR_ERR_INVALID_ARG, "ctx is NULL");
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    c->pos.release(); c->nor.release(); c->uv.release(); c->col.release(); c->mat.release();
-    c->obj_first.release(); c->obj_model.release(); c->obj_normal.release(); c->obj_matbase.release();
-    c->tri_flags.release();
-    c->dmats.release(); c->rrec.release(); c->arec.release(); c->tasks.release(); c->first_rec.release();
+    if (c->stream_u) cudaStreamSynchronize(c->stream_u);
+    if (c->stream_d) cudaStreamSynchronize(c->stream_d);
+    c->sb.release();
+    c->sb_back.release();
+    if (c->ev_frame) cudaEventDestroy(c->ev_frame);
+    if (c->ev_d2h) cudaEventDestroy(c->ev_d2h);
+    if (c->stream_u) cudaStreamDestroy(c->stream_u);
+    if (c->stream_d) cudaStreamDestroy(c->stream_d);
+    c->rrec.release(); c->arec.release(); c->tasks.release(); c->first_rec.release();
     c->clip_list.release();
     c->keys.release(); c->nanseq.release(); c->beaten.release(); c->win.release(); c->depth_ao.release();
     c->ao_list.release();
@@ -722,43 +856,35 @@ int pr_scene_upload(void* ctx, const pr_scene_desc* s) {
     int rc = validate_scene(s);
     if (rc) return rc;
     if ((rc = set_device(c))) return rc;
-    bool dev = (s->flags & PR_SCENE_DEVICE_PTRS) != 0;
-    cudaStream_t st = c->stream;
-    uint32_t n = s->n_tris;
-    if ((rc = upload(c->pos, s->pos, (size_t)n * 3, dev, st))) return rc;
-    if ((rc = upload(c->nor, s->nor, (size_t)n * 3, dev, st))) return rc;
-    if ((rc = upload(c->uv, s->uv, (size_t)n * 3, dev, st))) return rc;
-    if ((rc = upload(c->col, s->col, (size_t)n * 3, dev, st))) return rc;
-    if ((rc = upload(c->mat, s->mat_id, (size_t)n, dev, st))) return rc;
-    c->objects.assign(s->objects, s->objects + s->n_objects);
-    c->materials.assign(s->materials, s->materials + s->n_materials);
-    // Per-object Model and Normal = Model.Inv().T() (render/raster.go:242-243)
-    uint32_t no = s->n_objects;
-    std::vector<uint32_t> first(no + 1);
-    std::vector<float> model((size_t)no * 16), normal((size_t)no * 16);
-    std::vector<int32_t> mb(no);
-    for (uint32_t o = 0; o < no; o++) {
-        first[o] = s->objects[o].first_tri;
-        M4 m = loadm(s->objects[o].model), mi;
-        if (!prh::inv(m, &mi)) return fail(PR_ERR_SINGULAR, "object %u: model matrix is singular", o);
-        M4 nm = prh::transpose(mi);
-        std::memcpy(&model[(size_t)o * 16], m.m, 64);
-        std::memcpy(&normal[(size_t)o * 16], nm.m, 64);
-        mb[o] = s->objects[o].mat_base;
-    }
-    first[no] = n;
-    if ((rc = upload(c->obj_first, first.data(), first.size(), false, st))) return rc;
-    if ((rc = upload(c->obj_model, model.data(), model.size(), false, st))) return rc;
-    if ((rc = upload(c->obj_normal, normal.data(), normal.size(), false, st))) return rc;
-    if ((rc = c->tri_flags.ensure(std::max<uint32_t>(n, 1)))) return rc;
-    KTRY(prk::launch_tri_flags(c->pos.p, n, c->tri_flags.p, st));
-    if ((rc = upload(c->obj_matbase, mb.data(), mb.size(), false, st))) return rc;
-    if ((rc = upload(c->dmats, c->materials.data(), c->materials.size(), false, st))) return rc;
-    CUDA_TRY(cudaStreamSynchronize(st));  // host vectors above go out of scope
-    c->n_tris = n;
+    // submitted frames may still read the scene buffers
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream_u));
+    CUDA_TRY(cudaStreamSynchronize(c->stream_d));
+    if ((rc = scene_fill(c->sb, s, c->stream, false))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(c->stream));  // host tables go out of scope
     c->has_scene = true;
     c->smap_valid = false;
     return PR_OK;
+}
+
+int pr_frame_submit(void* ctx, const pr_scene_desc* scene, const pr_frame_desc* frame, pr_outputs* out) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(PR_ERR_INVALID_ARG, "ctx is NULL");
+    std::lock_guard<std::mutex> lk(c->mu);
+    int rc = validate_scene(scene);
+    if (rc) return rc;
+    if (out && out->shadow_maps) return fail(PR_ERR_UNSUPPORTED, "pr_frame_submit does not return shadow maps");
+    if ((rc = set_device(c))) return rc;
+    SceneBufs& b = c->sb_back;
+    CUDA_TRY(cudaEventSynchronize(b.ev_uploaded));                 // its staging is free again
+    CUDA_TRY(cudaStreamWaitEvent(c->stream_u, b.ev_released, 0));  // no frame reads it any more
+    if ((rc = scene_fill(b, scene, c->stream_u, true))) return rc;
+    CUDA_TRY(cudaEventRecord(b.ev_uploaded, c->stream_u));
+    std::swap(c->sb, c->sb_back);
+    c->has_scene = true;
+    c->smap_valid = false;  // as pr_scene_upload
+    CUDA_TRY(cudaStreamWaitEvent(c->stream, c->sb.ev_uploaded, 0));
+    return render_impl(c, frame, out, false, nullptr, true);
 }
 
 int pr_shadow_reset(void* ctx) {
@@ -801,6 +927,8 @@ int pr_sync(void* ctx) {
     Ctx* c = (Ctx*)ctx;
     if (!c) return fail(PR_ERR_INVALID_ARG, "ctx is NULL");
     CUDA_TRY(cudaStreamSynchronize(c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream_d));
+    CUDA_TRY(cudaStreamSynchronize(c->stream_u));
     for (int k = 0; k < prk::kNumCounters; k++)
         if (c->h_cnt[k].overflow) return fail(PR_ERR_OVERFLOW, "internal capacity exceeded in an asynchronous frame");
     collect_stats(c);
@@ -890,7 +1018,7 @@ namespace {
 // Device parameters of a differentiable call: the caller's or the scene's.
 int diff_setup(Ctx* c, const pr_frame_desc* f, const pr_diff_params* prm, prk::DiffParamsK& K) {
     int rc;
-    const uint32_t nm = (uint32_t)c->materials.size();
+    const uint32_t nm = (uint32_t)c->sb.materials.size();
     if (prm && prm->size < sizeof(pr_diff_params)) return fail(PR_ERR_INVALID_ARG, "params->size too small");
     if (prm && prm->n_materials != nm && (prm->kd || prm->ks || prm->shininess))
         return fail(PR_ERR_INVALID_ARG, "params->n_materials (%u) differs from the scene's (%u)", prm->n_materials, nm);
@@ -900,10 +1028,10 @@ int diff_setup(Ctx* c, const pr_frame_desc* f, const pr_diff_params* prm, prk::D
     std::vector<float> kd(3 * std::max<uint32_t>(nm, 1)), ks(kd.size()), sh(std::max<uint32_t>(nm, 1));
     for (uint32_t m = 0; m < nm; m++) {
         for (int k = 0; k < 3; k++) {
-            kd[3 * m + k] = (prm && prm->kd) ? prm->kd[3 * m + k] : c->materials[m].diffuse[k] / 255.0f;
-            ks[3 * m + k] = (prm && prm->ks) ? prm->ks[3 * m + k] : c->materials[m].specular[k] / 255.0f;
+            kd[3 * m + k] = (prm && prm->kd) ? prm->kd[3 * m + k] : c->sb.materials[m].diffuse[k] / 255.0f;
+            ks[3 * m + k] = (prm && prm->ks) ? prm->ks[3 * m + k] : c->sb.materials[m].specular[k] / 255.0f;
         }
-        sh[m] = (prm && prm->shininess) ? prm->shininess[m] : c->materials[m].shininess;
+        sh[m] = (prm && prm->shininess) ? prm->shininess[m] : c->sb.materials[m].shininess;
     }
     cudaStream_t st = c->stream;
     if ((rc = c->d_kd.ensure(kd.size())) || (rc = c->d_ks.ensure(ks.size())) || (rc = c->d_shin.ensure(sh.size())))
@@ -911,25 +1039,25 @@ int diff_setup(Ctx* c, const pr_frame_desc* f, const pr_diff_params* prm, prk::D
     CUDA_TRY(cudaMemcpyAsync(c->d_kd.p, kd.data(), kd.size() * 4, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(c->d_ks.p, ks.data(), ks.size() * 4, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(c->d_shin.p, sh.data(), sh.size() * 4, cudaMemcpyHostToDevice, st));
-    const size_t nv = (size_t)c->n_tris * 3;
+    const size_t nv = (size_t)c->sb.n_tris * 3;
     const float4* vcol = prm ? (const float4*)prm->vertex_color : nullptr;
     if (!vcol) {
         if ((rc = c->d_vcol.ensure(std::max<size_t>(nv, 1)))) return rc;
-        KTRY(prk::launch_col_to_float(c->col.p, c->d_vcol.p, nv, st));
+        KTRY(prk::launch_col_to_float(c->sb.col.p, c->d_vcol.p, nv, st));
         vcol = c->d_vcol.p;
     }
     K.W = f->width;
     K.H = f->height;
     K.vcol = vcol;
-    K.vnor = (prm && prm->vertex_normal) ? (const float4*)prm->vertex_normal : c->nor.p;
-    K.obj_first = c->obj_first.p;
-    K.n_objects = (uint32_t)c->objects.size();
-    K.obj_normal = c->obj_normal.p;
+    K.vnor = (prm && prm->vertex_normal) ? (const float4*)prm->vertex_normal : c->sb.nor.p;
+    K.obj_first = c->sb.obj_first.p;
+    K.n_objects = (uint32_t)c->sb.objects.size();
+    K.obj_normal = c->sb.obj_normal.p;
     K.n_mats = (int)nm;
     K.kd = c->d_kd.p;
     K.ks = c->d_ks.p;
     K.shin = c->d_shin.p;
-    K.mats = c->dmats.p;
+    K.mats = c->sb.dmats.p;
     K.n_lights = (int)f->n_lights;
     K.n_ambient = (int)f->n_ambient;
     for (uint32_t l = 0; l < f->n_lights; l++) {
@@ -1012,7 +1140,7 @@ int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params
     prk::DiffParamsK K{};
     if ((rc = diff_setup(c, frame, params, K))) return rc;
     cudaStream_t st = c->stream;
-    const size_t nv = (size_t)c->n_tris * 3;
+    const size_t nv = (size_t)c->sb.n_tris * 3;
     if (grads->vertex_color) CUDA_TRY(cudaMemsetAsync(grads->vertex_color, 0, nv * 16, st));
     if (grads->vertex_normal) CUDA_TRY(cudaMemsetAsync(grads->vertex_normal, 0, nv * 16, st));
     const int nm = K.n_mats, nl = K.n_lights, na = K.n_ambient;
@@ -1151,7 +1279,7 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
     for (uint32_t v = 0; v < nv; v++) {
         const Ctx* c = b->scenes[views[v].scene];
         const pr_frame_desc* f = views[v].frame;
-        const uint32_t n = c->n_tris;
+        const uint32_t n = c->sb.n_tris;
         const uint32_t r0 = n + n / 8 + 1024;
         const uint32_t cr = std::max(r0, b->cap_main_rec[v]), ct = std::max(r0, b->cap_main_tasks[v]);
         rec_m[v] = rec;
@@ -1175,7 +1303,7 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
         sm[v] = nsm;
         if (!shadows) continue;
         nsm += (size_t)SW * SH * std::max<uint32_t>(f->n_lights, 1);
-        const uint32_t n = c->n_tris;
+        const uint32_t n = c->sb.n_tris;
         const uint32_t ct = std::max(n + n / 8 + 1024, b->cap_shadow_tasks[v]);
         b->cap_shadow_tasks[v] = ct;
         for (uint32_t l = 0; l < f->n_lights; l++) {
@@ -1229,7 +1357,7 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
         std::memcpy(sp.viewport, svp.m, 64);
         sp.rrec = b->rrec.p + q.rec;
         sp.arec = nullptr;
-        sp.cap_rec = std::max<uint32_t>(c->n_tris, 1);
+        sp.cap_rec = std::max<uint32_t>(c->sb.n_tris, 1);
         sp.tasks = b->tasks.p + q.task;
         sp.cap_tasks = b->cap_shadow_tasks[q.v];
         sp.first_rec = nullptr;
@@ -1247,7 +1375,7 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
         rp.smap = b->smaps.p + sm[q.v] + (size_t)SW * SH * q.l;
         rp.lastnan = nullptr;  // NaN depth: the view is re-rendered alone
         rp.task_shift = b->task_shift;
-        p.blk.push_back(p.blk.back() + (c->n_tris + 127) / 128);
+        p.blk.push_back(p.blk.back() + (c->sb.n_tris + 127) / 128);
     }
     p.nb_s = p.blk.back();
     // main passes
@@ -1282,7 +1410,7 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
         mp.clip_list = b->clip_list.p + first[v];
         mp.cnt = dcnt + v;
         mp.task_shift = b->task_shift;
-        p.blk.push_back(p.blk.back() + (c->n_tris + 127) / 128);
+        p.blk.push_back(p.blk.back() + (c->sb.n_tris + 127) / 128);
         const size_t o = px[v];
         prk::RasterParams& rp = p.rj[v];
         rp.rrec = mp.rrec;
@@ -1656,7 +1784,7 @@ int pr_batch_tune(void* batch, uint32_t n_views, const pr_batch_view* views, cha
     size_t rec = 0, tasks = 0;
     for (uint32_t v = 0; v < n_views; v++) {
         const prk::Counters& k = b->h_cnt[v];
-        const uint32_t n = b->scenes[views[v].scene]->n_tris;
+        const uint32_t n = b->scenes[views[v].scene]->sb.n_tris;
         b->cap_main_rec[v] = std::max(k.n_rec + k.n_rec / 16 + 64, std::min(b->cap_main_rec[v], n + n / 8 + 1024));
         b->cap_main_tasks[v] = k.n_tasks + k.n_tasks / 16 + 64;
         rec += b->cap_main_rec[v];
