@@ -143,6 +143,8 @@ var (
 	prLastError    func() string
 	prViewMatrix   func(pos, target, up *float32, out *float32) int32
 	prShadowCamera func(lightPos, center, view, proj, outView, outProj *float32) int32
+	prFrameSubmit  func(ctx uintptr, s *SceneDesc, f *FrameDesc, o *Outputs) int32
+	prSync         func(ctx uintptr) int32
 	prHostAlloc    func(bytes uintptr, out *unsafe.Pointer) int32
 	prHostFree     func(p unsafe.Pointer) int32
 )
@@ -170,6 +172,8 @@ func load() error {
 		purego.RegisterLibFunc(&prLastError, lib, "pr_last_error")
 		purego.RegisterLibFunc(&prViewMatrix, lib, "pr_view_matrix")
 		purego.RegisterLibFunc(&prShadowCamera, lib, "pr_shadow_camera")
+		purego.RegisterLibFunc(&prFrameSubmit, lib, "pr_frame_submit")
+		purego.RegisterLibFunc(&prSync, lib, "pr_sync")
 		purego.RegisterLibFunc(&prHostAlloc, lib, "pr_host_alloc")
 		purego.RegisterLibFunc(&prHostFree, lib, "pr_host_free")
 	})
@@ -265,6 +269,33 @@ func (d *Device) Render(f *FrameDesc, o *Outputs) error {
 	runtime.KeepAlive(f)
 	runtime.KeepAlive(o)
 	return err
+}
+
+// Submit uploads the scene and queues one frame without waiting
+// (pr_frame_submit): the upload overlaps the frame before it, host outputs
+// come back while the next frame computes. The scene's arrays and the
+// outputs must stay valid and unchanged until Sync, so they should live
+// outside the Go heap (HostAlloc) or be pinned by the caller.
+func (d *Device) Submit(s *SceneDesc, f *FrameDesc, o *Outputs) error {
+	d.mu.Lock()
+	defer d.mu.Unlock()
+	if d.ctx == 0 {
+		return ErrClosed
+	}
+	s.Size = uint32(unsafe.Sizeof(*s))
+	f.Size = uint32(unsafe.Sizeof(*f))
+	o.Size = uint32(unsafe.Sizeof(*o))
+	return check(prFrameSubmit(d.ctx, s, f, o))
+}
+
+// Sync waits for every submitted frame and its outputs.
+func (d *Device) Sync() error {
+	d.mu.Lock()
+	defer d.mu.Unlock()
+	if d.ctx == 0 {
+		return ErrClosed
+	}
+	return check(prSync(d.ctx))
 }
 
 // ShadowCamera returns the light camera initShadowMaps fits around the main
