@@ -290,8 +290,13 @@ int ensure_frame(Ctx* c, int W, int H) {
     size_t n = (size_t)W * H;
     int rc;
     if ((rc = c->keys.ensure(n))) return rc;
+    // nanseq / beaten start all-kNone / all-0 and are put back so after any
+    // frame that used them, so a new allocation is set once
+    const size_t n0 = c->nanseq.n, b0 = c->beaten.n;
     if ((rc = c->nanseq.ensure(n))) return rc;
     if ((rc = c->beaten.ensure(n))) return rc;
+    if (c->nanseq.n != n0) CUDA_TRY(cudaMemsetAsync(c->nanseq.p, 0xff, c->nanseq.n * 4, c->stream));
+    if (c->beaten.n != b0) CUDA_TRY(cudaMemsetAsync(c->beaten.p, 0, c->beaten.n * 4, c->stream));
     if ((rc = c->win.ensure(n))) return rc;
     if ((rc = c->depth_ao.ensure(n))) return rc;
     if ((rc = c->ao_list.ensure(n))) return rc;
@@ -484,7 +489,10 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             c->n_slights = NL;
             c->smap_valid = true;
         }
+        const size_t l0 = c->lastnan.n;
         if ((rc = c->lastnan.ensure((size_t)SW * SH))) return rc;
+        // zero, and put back to zero after any pass that wrote it
+        if (c->lastnan.n != l0) CUDA_TRY(cudaMemsetAsync(c->lastnan.p, 0, c->lastnan.n * 4, st));
     }
 
     prk::Counters* dcnt = c->cnt.p;
@@ -523,7 +531,6 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 sp.cnt = dcnt + 1 + l;
                 if (c->sb.n_tris > c->cap_rec) return fail(PR_ERR_OVERFLOW, "record capacity below triangle count");
                 uint32_t* plane = c->smap.p + (size_t)SW * SH * l;
-                CUDA_TRY(cudaMemsetAsync(c->lastnan.p, 0, (size_t)SW * SH * 4, ss));
                 KTRY(prk::launch_setup_shadow(sp, ss));
                 prk::RasterParams rp{};
                 rp.rrec = c->rrec_s.p;
@@ -541,7 +548,8 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 rp.mode = prk::kShadowFixup;
                 rp.take = &dcnt[1 + l].take[1];
                 KTRY(prk::launch_raster(rp, c->n_sms * 8, ss));
-                launches += 4;
+                KTRY(prk::launch_nan_cleanup((size_t)SW * SH, c->lastnan.p, 0u, nullptr, 0u, dcnt + 1 + l, ss));
+                launches += 5;
             }
         }
         CUDA_TRY(cudaEventRecord(c->ev[1], ss));
@@ -569,8 +577,6 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             mp.tri_scr = c->tri_scr.p;
         }
         CUDA_TRY(cudaMemsetAsync(c->keys.p, 0, npx * 8, st));
-        CUDA_TRY(cudaMemsetAsync(c->nanseq.p, 0xff, npx * 4, st));
-        CUDA_TRY(cudaMemsetAsync(c->beaten.p, 0, npx * 4, st));
         KTRY(prk::launch_setup_main_only(mp, c->clip_list.p, st));
         CUDA_TRY(cudaEventRecord(c->ev[2], st));
         // clipped triangles: their own task list and stream; records and the
@@ -611,8 +617,9 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
         KTRY(prk::launch_raster(rc_, c->n_sms * 8, st));
         KTRY(prk::launch_resolve(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p, st));
+        KTRY(prk::launch_nan_cleanup(npx, c->nanseq.p, 0xFFFFFFFFu, c->beaten.p, 0u, dcnt, st));
         CUDA_TRY(cudaEventRecord(c->ev[3], st));
-        launches += 7;
+        launches += 8;
 
         // ---- deferred shading + gamma (render/raster.go:275-378) ----
         std::unique_ptr<prk::ShadeParams> sp_owner(new (std::nothrow) prk::ShadeParams());

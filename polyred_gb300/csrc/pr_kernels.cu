@@ -751,10 +751,23 @@ __global__ void resolve_kernel(int W, int H, const unsigned long long* keys, con
 
 // Shadow NaN fix-up: pixels that saw a NaN-depth fragment restart from NaN
 // (key 0) and take the maximum over the fragments drawn after the last one.
+// (A small persistent grid: with no NaN fragment, the usual case, every block
+// reads the flag and leaves.)
 __global__ void shadow_fixup_reset_kernel(size_t n, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt) {
     if (cnt->nan_flag == 0) return;
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && lastnan[i] != 0u) smap[i] = 0u;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (lastnan[i] != 0u) smap[i] = 0u;
+}
+
+// After a pass that saw a NaN-depth fragment, put its NaN bookkeeping back to
+// the state a pass starts from (a[] = va, b[] = vb); untouched otherwise, as
+// only NaN fragments write it.
+__global__ void nan_cleanup_kernel(size_t n, uint32_t* a, uint32_t va, uint32_t* b, uint32_t vb, const Counters* cnt) {
+    if (cnt->nan_flag == 0) return;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        a[i] = va;
+        if (b) b[i] = vb;
+    }
 }
 
 __global__ void decode_shadow_kernel(const uint32_t* smap, float* out, size_t n) {
@@ -1581,7 +1594,14 @@ int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t*
 int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,
                               void* stream) {
     size_t n = (size_t)W * H;
-    shadow_fixup_reset_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, lastnan, smap, cnt);
+    const unsigned nb = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 8);
+    shadow_fixup_reset_kernel<<<std::max(nb, 1u), 256, 0, (cudaStream_t)stream>>>(n, lastnan, smap, cnt);
+    return check(cudaGetLastError());
+}
+int launch_nan_cleanup(size_t n, uint32_t* a, uint32_t va, uint32_t* b, uint32_t vb, const Counters* cnt,
+                       void* stream) {
+    const unsigned nb = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 8);
+    nan_cleanup_kernel<<<std::max(nb, 1u), 256, 0, (cudaStream_t)stream>>>(n, a, va, b, vb, cnt);
     return check(cudaGetLastError());
 }
 int launch_shade(const ShadeParams& p, void* stream) {

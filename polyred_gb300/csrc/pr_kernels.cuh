@@ -213,6 +213,9 @@ int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t*
                    const Counters* cnt, uint32_t* win, float* depth_ao, void* stream);
 int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,
                               void* stream);
+// After a pass that saw a NaN fragment (cnt->nan_flag): a[0..n) = va and, if b, b[0..n) = vb.
+int launch_nan_cleanup(size_t n, uint32_t* a, uint32_t va, uint32_t* b, uint32_t vb, const Counters* cnt,
+                       void* stream);
 int launch_shade(const ShadeParams& p, void* stream);
 int launch_ao(const AoParams& p, void* stream);
 int launch_diff(const DiffParamsK& p, bool backward, void* stream);
