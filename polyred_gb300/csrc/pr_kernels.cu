@@ -816,8 +816,10 @@ PR_DEV void diff_gbuffer_pixel(const ShadeParams& P, size_t i, uint32_t seq, int
     D[3] = make_float4(fn.x, fn.y, fn.z, fn.w);
 }
 
-PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
-    if (x >= P.W || r >= P.H) return;
+// Returns true for a pixel that AO still has to finish (its pre-AO colour is
+// in rgba; the caller lists it).
+PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
+    if (x >= P.W || r >= P.H) return false;
     const int W = P.W, H = P.H;
     const int y = H - 1 - r;
     const size_t i = (size_t)r * W + x;
@@ -990,30 +992,43 @@ PR_DEV void shade_one(const ShadeParams& P, int x, int r) {
     }
     if (ao_pending) {
         P.rgba[i] = make_uchar4(c0, c1, c2, c3);  // pre-AO, pre-gamma colour
+        return true;
     }
-    {
-        // warp-aggregated append to the AO list
-        const unsigned act = __activemask();
-        const unsigned want = __ballot_sync(act, ao_pending);
-        if (want) {
-            const int lane = threadIdx.x & 31;
-            const int leader = __ffs(want) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(&P.cnt_w->n_ao, (uint32_t)__popc(want));
-            base = __shfl_sync(act, base, leader);
-            if (ao_pending) P.ao_list[base + __popc(want & ((1u << lane) - 1u))] = (uint32_t)i;
-        }
-    }
-    if (ao_pending) return;
     if (P.flags & PR_FRAME_GAMMA) {
         c0 = P.gamma[c0];
         c1 = P.gamma[c1];
         c2 = P.gamma[c2];
     }
     if (P.rgba) P.rgba[i] = make_uchar4(c0, c1, c2, c3);
+    return false;
+}
+
+// Block-wide append of the AO pixels of a 32 x 8 tile (every thread of the
+// 256-thread block calls): one atomic per tile, so the list runs tile by
+// tile and an AO block marches a compact patch whose taps overlap.
+PR_DEV void ao_append_tile(const ShadeParams& P, bool pending, uint32_t i) {
+    __shared__ uint32_t s_cnt[8];
+    __shared__ uint32_t s_base;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, pending);
+    if (lane == 0) s_cnt[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < 8; w++) tot += s_cnt[w];
+        s_base = tot ? atomicAdd(&P.cnt_w->n_ao, tot) : 0u;
+    }
+    __syncthreads();
+    if (pending) {
+        uint32_t o = s_base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        for (int w = 0; w < warp; w++) o += s_cnt[w];
+        P.ao_list[o] = i;
+    }
 }
 __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
-    shade_one(P, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool pending = shade_one(P, x, r);
+    if (P.ao_list) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
 }
 
 // ---------------------------------------------------------------- AO
@@ -1483,7 +1498,9 @@ __global__ void __launch_bounds__(256) shade_batch_kernel(const ShadeParams* vie
     const ShadeParams& P = views[v];
     const uint32_t b = blockIdx.x - blk[v], tiles_x = (uint32_t)(P.W + 31) / 32u;
     const uint32_t ty = b / tiles_x, tx = b - ty * tiles_x;
-    shade_one(P, (int)(tx * 32u + (threadIdx.x & 31u)), (int)(ty * 8u + (threadIdx.x >> 5)));
+    const int x = (int)(tx * 32u + (threadIdx.x & 31u)), r = (int)(ty * 8u + (threadIdx.x >> 5));
+    const bool pending = shade_one(P, x, r);
+    if (P.ao_list) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
 }
 
 // Persistent AO over every view's list, in chunks of one block taken from
