@@ -114,13 +114,14 @@ struct SceneBufs {
     DevBuf<float> obj_model, obj_normal;
     DevBuf<int32_t> obj_matbase;
     DevBuf<pr_material> dmats;
+    DevBuf<uint32_t> blk_obj;              // object of the first triangle of each 128-triangle block
     HostBuf tables;                        // page-locked staging of the small tables (submitted uploads)
     cudaEvent_t ev_uploaded = nullptr;     // the upload into these buffers has landed
     cudaEvent_t ev_released = nullptr;     // the last frame that read them is past shading
     void release() {
         pos.release(); nor.release(); uv.release(); col.release(); mat.release();
         obj_first.release(); tri_flags.release(); obj_model.release(); obj_normal.release();
-        obj_matbase.release(); dmats.release(); tables.release();
+        obj_matbase.release(); dmats.release(); blk_obj.release(); tables.release();
         if (ev_uploaded) cudaEventDestroy(ev_uploaded);
         if (ev_released) cudaEventDestroy(ev_released);
         ev_uploaded = ev_released = nullptr;
@@ -145,6 +146,7 @@ struct Ctx {
     uint32_t cap_rec = 0, cap_tasks = 0;
     // framebuffer
     int W = 0, H = 0;
+    DevBuf<float> obj_trans;  // [1 + lights][n_objects][16]: Proj·View·Model per pass and object
     DevBuf<unsigned long long> keys;
     DevBuf<uint32_t> nanseq, beaten, win;
     DevBuf<float> depth_ao;
@@ -245,6 +247,13 @@ int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool stage
         mb[o] = s->objects[o].mat_base;
     }
     first[no] = n;
+    // object of each 128-triangle block's first triangle (the last object starting at or before it)
+    const uint32_t nblk = (n + 127) / 128;
+    std::vector<uint32_t> blk(std::max<uint32_t>(nblk, 1), 0u);
+    for (uint32_t k = 0, o = 0; k < nblk; k++) {
+        while (o + 1 < no && first[o + 1] <= k * 128u) o++;
+        blk[k] = o;
+    }
     if ((rc = upload(b.pos, s->pos, (size_t)n * 3, dev, st))) return rc;
     if ((rc = upload(b.nor, s->nor, (size_t)n * 3, dev, st))) return rc;
     if ((rc = upload(b.uv, s->uv, (size_t)n * 3, dev, st))) return rc;
@@ -255,11 +264,12 @@ int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool stage
     const void* t_normal = normal.data();
     const void* t_mb = mb.data();
     const void* t_mats = s->materials;
+    const void* t_blk = blk.data();
     if (staged) {
         auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
         const size_t o_first = 0, o_model = al(o_first + first.size() * 4), o_normal = o_model + model.size() * 4,
                      o_mb = o_normal + normal.size() * 4, o_mats = al(o_mb + mb.size() * 4),
-                     total = o_mats + (size_t)nm * sizeof(pr_material);
+                     o_blk = al(o_mats + (size_t)nm * sizeof(pr_material)), total = o_blk + blk.size() * 4;
         if ((rc = b.tables.ensure(total))) return rc;
         uint8_t* h = b.tables.p;
         std::memcpy(h + o_first, first.data(), first.size() * 4);
@@ -267,6 +277,8 @@ int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool stage
         std::memcpy(h + o_normal, normal.data(), normal.size() * 4);
         std::memcpy(h + o_mb, mb.data(), mb.size() * 4);
         if (nm) std::memcpy(h + o_mats, s->materials, (size_t)nm * sizeof(pr_material));
+        std::memcpy(h + o_blk, blk.data(), blk.size() * 4);
+        t_blk = h + o_blk;
         t_first = h + o_first;
         t_model = h + o_model;
         t_normal = h + o_normal;
@@ -278,6 +290,7 @@ int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool stage
     if ((rc = upload(b.obj_normal, t_normal, normal.size(), false, st))) return rc;
     if ((rc = upload(b.obj_matbase, t_mb, mb.size(), false, st))) return rc;
     if ((rc = upload(b.dmats, t_mats, nm, false, st))) return rc;
+    if ((rc = upload(b.blk_obj, t_blk, blk.size(), false, st))) return rc;
     if ((rc = b.tri_flags.ensure(std::max<uint32_t>(n, 1)))) return rc;
     KTRY(prk::launch_tri_flags(b.pos.p, n, b.tri_flags.p, st));
     b.objects.assign(s->objects, s->objects + no);
@@ -335,6 +348,7 @@ void fill_scene_ptrs(Ctx* c, prk::SetupParams& p) {
     p.obj_normal = c->sb.obj_normal.p;
     p.obj_matbase = c->sb.obj_matbase.p;
     p.tri_flags = c->sb.tri_flags.p;
+    p.blk_obj = c->sb.blk_obj.p;
     p.n_tris = c->sb.n_tris;
     p.n_objects = (uint32_t)c->sb.objects.size();
 }
@@ -505,6 +519,20 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
     {
         CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(prk::Counters) * prk::kNumCounters, st));
         CUDA_TRY(cudaEventRecord(c->ev[0], st));
+        // Proj·View·Model of every object for the main pass (0) and each light (1 + l)
+        const uint32_t n_obj = (uint32_t)c->sb.objects.size();
+        const int n_pass = shadows ? 1 + NL : 1;
+        {
+            prk::PassMats pm;
+            std::memcpy(pm.pv[0], pv.m, 64);
+            for (int l = 0; shadows && l < NL; l++) {
+                const M4 lpv = prh::mulm(loadm(f->lights[l].shadow_proj), loadm(f->lights[l].shadow_view));
+                std::memcpy(pm.pv[1 + l], lpv.m, 64);
+            }
+            if ((rc = c->obj_trans.ensure((size_t)n_pass * std::max<uint32_t>(n_obj, 1) * 16))) return rc;
+            KTRY(prk::launch_obj_trans(pm, n_pass, c->sb.obj_model.p, n_obj, c->obj_trans.p, st));
+            launches += 1;
+        }
         // ---- shadow passes (render/raster.go:176-184), on their own stream:
         // only the deferred pass reads the maps ----
         cudaStream_t ss = c->stream_s;
@@ -529,6 +557,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 sp.cap_tasks = c->cap_tasks;
                 sp.first_rec = nullptr;
                 sp.cnt = dcnt + 1 + l;
+                sp.obj_trans = c->obj_trans.p + (size_t)(1 + l) * n_obj * 16;
                 if (c->sb.n_tris > c->cap_rec) return fail(PR_ERR_OVERFLOW, "record capacity below triangle count");
                 uint32_t* plane = c->smap.p + (size_t)SW * SH * l;
                 KTRY(prk::launch_setup_shadow(sp, ss));
@@ -561,6 +590,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         mp.H = H;
         mp.perspective = (f->flags & PR_FRAME_PERSPECTIVE) ? 1 : 0;
         std::memcpy(mp.pv, pv.m, 64);
+        mp.obj_trans = c->obj_trans.p;
         std::memcpy(mp.viewport, vp.m, 64);
         std::memcpy(mp.viewport_inv, vp_inv.m, 64);
         std::memcpy(mp.proj_inv, proj_inv.m, 64);

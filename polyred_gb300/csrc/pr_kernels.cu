@@ -329,8 +329,24 @@ PR_DEV void obj_cache_fill(const SetupParams& P, uint32_t t0, ObjCache& C) {
     __syncthreads();
 }
 
-// Object of triangle t and its Proj·View·Model (from the cache when it holds t's block).
+// Object of triangle t and its Proj·View·Model: from the pass's table (the
+// block's first object, then the few objects that start inside the block),
+// else from the block cache when it holds t's block.
 PR_DEV uint32_t object_trans(const SetupParams& P, const ObjCache* C, uint32_t t, float* trans) {
+    if (P.obj_trans) {
+        uint32_t o = P.blk_obj[t >> 7];
+        while (o + 1 < P.n_objects && P.obj_first[o + 1] <= t) o++;
+        const float4* q = reinterpret_cast<const float4*>(P.obj_trans + (size_t)o * 16);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float4 r = __ldg(q + e);
+            trans[4 * e] = r.x;
+            trans[4 * e + 1] = r.y;
+            trans[4 * e + 2] = r.z;
+            trans[4 * e + 3] = r.w;
+        }
+        return o;
+    }
     if (C && C->n <= (uint32_t)kBlkObj) {
         uint32_t k = 0;
         while (k + 1 < C->n && C->first[k + 1] <= t) k++;
@@ -419,7 +435,7 @@ PR_DEV void setup_main_one(const SetupParams& P, const ObjCache* C, uint32_t t, 
 }
 __global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P, uint32_t* clip_list) {
     __shared__ ObjCache C;
-    obj_cache_fill(P, blockIdx.x * blockDim.x, C);
+    if (!P.obj_trans) obj_cache_fill(P, blockIdx.x * blockDim.x, C);  // uniform
     setup_main_one(P, &C, blockIdx.x * blockDim.x + threadIdx.x, clip_list);
 }
 
@@ -517,8 +533,23 @@ PR_DEV void setup_shadow_one(const SetupParams& P, const ObjCache* C, uint32_t t
 }
 __global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
     __shared__ ObjCache C;
-    obj_cache_fill(P, blockIdx.x * blockDim.x, C);
+    if (!P.obj_trans) obj_cache_fill(P, blockIdx.x * blockDim.x, C);  // uniform
     setup_shadow_one(P, &C, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Proj·View·Model per (pass, object), the product obj_cache_fill forms.
+__global__ void obj_trans_kernel(const __grid_constant__ PassMats pm, int n_pass, const float* obj_model,
+                                 uint32_t n_objects, float* out) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n_pass * n_objects * 16) return;
+    const size_t po = e >> 4;
+    const int pass = (int)(po / n_objects);
+    const size_t o = po - (size_t)pass * n_objects;
+    const uint32_t i = (uint32_t)(e >> 2) & 3u, j = (uint32_t)e & 3u;
+    const float* m = pm.pv[pass] + i * 4;
+    const float* q = obj_model + o * 16;
+    out[e] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], q[j]), __fmul_rn(m[1], q[4 + j])), __fmul_rn(m[2], q[8 + j])),
+                       __fmul_rn(m[3], q[12 + j]));
 }
 
 // ---------------------------------------------------------------- raster
@@ -1572,6 +1603,13 @@ int check(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
 int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stream) {
     if (p.n_tris == 0) return 0;
     setup_main_kernel<<<(p.n_tris + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
+    return check(cudaGetLastError());
+}
+int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uint32_t n_objects, float* out,
+                     void* stream) {
+    const size_t n = (size_t)n_pass * n_objects * 16;
+    if (n == 0) return 0;
+    obj_trans_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(pm, n_pass, obj_model, n_objects, out);
     return check(cudaGetLastError());
 }
 int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream) {

@@ -77,6 +77,8 @@ struct SetupParams {
     const int32_t* mat;
     const uint32_t* obj_first;   // [n_objects + 1]
     const float* obj_model;      // [n_objects][16]
+    const float* obj_trans;      // [n_objects][16] this pass's Proj·View·Model, or null: per-block cache
+    const uint32_t* blk_obj;     // [n_tris / 128] object of each 128-triangle block's first triangle
     const float* obj_normal;     // [n_objects][16] Model.Inv().T()
     const int32_t* obj_matbase;  // [n_objects]
     uint32_t n_tris, n_objects;
@@ -207,6 +209,14 @@ namespace prk {
 int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream);  // setup, then clip
 int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stream);
 int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream);
+// Proj·View·Model of every object for n_pass passes: out[pass][o][16] from
+// the passes' Proj·View (pv[pass]) in Mat4.MulM's order.
+constexpr int kMaxPasses = kMaxLights + 1;
+struct PassMats {
+    float pv[kMaxPasses][16];
+};
+int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uint32_t n_objects, float* out,
+                     void* stream);
 int launch_setup_shadow(const SetupParams& p, void* stream);
 int launch_raster(const RasterParams& p, int n_blocks, void* stream);
 int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
