@@ -490,8 +490,8 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
 }
 __global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ SetupParams P, const uint32_t* clip_list) {
     const uint32_t n = (P.cnt_rec ? P.cnt_rec : P.cnt)->n_clipped;
-    if (blockIdx.x * blockDim.x >= n) return;  // whole block idle (uniform per warp too)
-    clip_one(P, clip_list, blockIdx.x * blockDim.x + threadIdx.x, n);
+    // grid-stride over the list (uniform per block, so every warp calls clip_one whole)
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) clip_one(P, clip_list, b + threadIdx.x, n);
 }
 
 // passShadows / drawDepth for one input triangle (render/shadow.go:137-192)
@@ -1614,8 +1614,9 @@ int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uin
 }
 int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream) {
     if (p.n_tris == 0) return 0;
-    // the list's length is known only on the device: a grid for the worst case, idle blocks exit at once
-    clip_kernel<<<(p.n_tris + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
+    // the list's length is known only on the device: a few blocks per SM stride over it
+    const unsigned nb = std::min((p.n_tris + 127) / 128, (unsigned)sm_count() * 4u);
+    clip_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
     return check(cudaGetLastError());
 }
 int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream) {
