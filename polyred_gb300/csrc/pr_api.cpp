@@ -143,6 +143,7 @@ struct Ctx {
     DevBuf<prk::AttrRec> arec;
     DevBuf<uint2> tasks;
     DevBuf<uint32_t> first_rec, clip_list;
+    DevBuf<uint32_t> attr_state, vis_list;  // deferred attribute records: per-record state, visible list
     uint32_t cap_rec = 0, cap_tasks = 0;
     // framebuffer
     int W = 0, H = 0;
@@ -324,6 +325,8 @@ int ensure_work(Ctx* c, uint32_t need_rec, uint32_t need_tasks) {
         uint32_t cap = std::max(need_rec, c->cap_rec * 2);
         if ((rc = c->rrec.ensure(cap))) return rc;
         if ((rc = c->arec.ensure(cap))) return rc;
+        if ((rc = c->attr_state.ensure(cap))) return rc;
+        if ((rc = c->vis_list.ensure(cap))) return rc;
         if ((rc = c->rrec_s.ensure(cap))) return rc;
         c->cap_rec = cap;
     }
@@ -591,6 +594,8 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         mp.perspective = (f->flags & PR_FRAME_PERSPECTIVE) ? 1 : 0;
         std::memcpy(mp.pv, pv.m, 64);
         mp.obj_trans = c->obj_trans.p;
+        mp.attr_state = c->attr_state.p;
+        mp.defer_attr = 1;  // attribute records for winning records only (attr_kernel after resolve)
         std::memcpy(mp.viewport, vp.m, 64);
         std::memcpy(mp.viewport_inv, vp_inv.m, 64);
         std::memcpy(mp.proj_inv, proj_inv.m, 64);
@@ -616,6 +621,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         CUDA_TRY(cudaEventRecord(c->ev_setup, st));
         CUDA_TRY(cudaStreamWaitEvent(sc, c->ev_setup, 0));
         prk::SetupParams cp = mp;
+        cp.defer_attr = 0;  // clipped sub-triangles carry interpolated attributes: written at once
         cp.cnt = dclip;
         cp.cnt_rec = dcnt;
         cp.tasks = c->tasks_c.p;
@@ -646,10 +652,12 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         rc_.take = &dclip->take[1];
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
         KTRY(prk::launch_raster(rc_, c->n_sms * 8, st));
-        KTRY(prk::launch_resolve(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p, st));
+        KTRY(prk::launch_resolve_listing(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p,
+                                         c->first_rec.p, c->attr_state.p, c->vis_list.p, st));
+        KTRY(prk::launch_attr(mp, c->vis_list.p, st));
         KTRY(prk::launch_nan_cleanup(npx, c->nanseq.p, 0xFFFFFFFFu, c->beaten.p, 0u, dcnt, st));
         CUDA_TRY(cudaEventRecord(c->ev[3], st));
-        launches += 8;
+        launches += 9;
 
         // ---- deferred shading + gamma (render/raster.go:275-378) ----
         std::unique_ptr<prk::ShadeParams> sp_owner(new (std::nothrow) prk::ShadeParams());
@@ -856,7 +864,7 @@ int pr_destroy(void* ctx) {
     if (c->ev_d2h) cudaEventDestroy(c->ev_d2h);
     if (c->stream_u) cudaStreamDestroy(c->stream_u);
     if (c->stream_d) cudaStreamDestroy(c->stream_d);
-    c->rrec.release(); c->arec.release(); c->tasks.release(); c->first_rec.release();
+    c->rrec.release(); c->arec.release(); c->tasks.release(); c->first_rec.release(); c->attr_state.release(); c->vis_list.release();
     c->clip_list.release();
     c->keys.release(); c->nanseq.release(); c->beaten.release(); c->win.release(); c->depth_ao.release();
     c->ao_list.release();

@@ -199,6 +199,38 @@ __device__ __noinline__ V4 apply4_outline(V4 v, const float* m) { return apply4(
 
 // Build and store the records of one sub-triangle; returns its pixel area
 // (0 = nothing to raster) and writes its bbox words.
+// The attribute record of record ridx (drawClipped's per-vertex inputs).
+PR_DEV void write_attr(const SetupParams& P, uint32_t ridx, const SubVtx* v, const float* recipw, int matid) {
+    AttrRec A;
+    V4 m[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        A.recipw[k] = recipw[k];
+        A.nor[k * 3 + 0] = v[k].nor.x;
+        A.nor[k * 3 + 1] = v[k].nor.y;
+        A.nor[k * 3 + 2] = v[k].nor.z;
+        A.uv[k * 2 + 0] = v[k].u;
+        A.uv[k * 2 + 1] = v[k].v;
+        A.col[k] = v[k].col;
+        // render/raster.go:467-469
+        m[k] = apply4_outline(apply4_outline(apply4_outline(v[k].pos, P.viewport_inv), P.proj_inv), P.view_inv);
+        A.m[k * 3 + 0] = m[k].x;
+        A.m[k * 3 + 1] = m[k].y;
+        A.m[k * 3 + 2] = m[k].z;
+    }
+    V4 fn = unit4(cross4(sub4(m[1], m[0]), sub4(m[2], m[0])));  // render/raster.go:479
+    A.fn[0] = fn.x; A.fn[1] = fn.y; A.fn[2] = fn.z; A.fn[3] = fn.w;
+    A.matid = matid;
+    const float4* as = reinterpret_cast<const float4*>(&A);
+    float4* ad = reinterpret_cast<float4*>(P.arec + ridx);
+#pragma unroll
+    for (int k = 0; k < 9; k++) ad[k] = as[k];
+}
+
+// Build and store the records of one sub-triangle; returns its pixel area
+// (0 = nothing to raster) and writes its bbox words. With P.defer_attr the
+// attribute record is left to attr_kernel, which writes it only for records
+// that win a pixel.
 PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, const SubVtx* v, const float* recipw,
                           int matid) {
     RasterRec R;
@@ -207,6 +239,7 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
         R.v[3 * k + 0] = v[k].pos.x;
         R.v[3 * k + 1] = v[k].pos.y;
         R.v[3 * k + 2] = v[k].pos.z;
+        R.recipw[k] = recipw ? recipw[k] : 0.0f;
     }
     R.sabc = sabc_of(R.v[0], R.v[1], R.v[3], R.v[4], R.v[6], R.v[7]);
     R.seq = seq;
@@ -216,37 +249,12 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
         R.by = 0u;
         area = 0;
     }
-    R.pad[0] = R.pad[1] = R.pad[2] = 0;
     const float4* rs = reinterpret_cast<const float4*>(&R);
     float4* rd = reinterpret_cast<float4*>(P.rrec + ridx);
 #pragma unroll
     for (int k = 0; k < 4; k++) rd[k] = rs[k];
-    if (P.arec) {
-        AttrRec A;
-        V4 m[3];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            A.recipw[k] = recipw[k];
-            A.nor[k * 3 + 0] = v[k].nor.x;
-            A.nor[k * 3 + 1] = v[k].nor.y;
-            A.nor[k * 3 + 2] = v[k].nor.z;
-            A.uv[k * 2 + 0] = v[k].u;
-            A.uv[k * 2 + 1] = v[k].v;
-            A.col[k] = v[k].col;
-            // render/raster.go:467-469
-            m[k] = apply4_outline(apply4_outline(apply4_outline(v[k].pos, P.viewport_inv), P.proj_inv), P.view_inv);
-            A.m[k * 3 + 0] = m[k].x;
-            A.m[k * 3 + 1] = m[k].y;
-            A.m[k * 3 + 2] = m[k].z;
-        }
-        V4 fn = unit4(cross4(sub4(m[1], m[0]), sub4(m[2], m[0])));  // render/raster.go:479
-        A.fn[0] = fn.x; A.fn[1] = fn.y; A.fn[2] = fn.z; A.fn[3] = fn.w;
-        A.matid = matid;
-        const float4* as = reinterpret_cast<const float4*>(&A);
-        float4* ad = reinterpret_cast<float4*>(P.arec + ridx);
-#pragma unroll
-        for (int k = 0; k < 9; k++) ad[k] = as[k];
-    }
+    if (P.attr_state) P.attr_state[ridx] = P.defer_attr ? 1u : 0u;
+    if (P.arec && !P.defer_attr) write_attr(P, ridx, v, recipw, matid);
     return area;
 }
 
@@ -365,8 +373,10 @@ PR_DEV bool tri_valid_of(const SetupParams& P, uint32_t t, const V4* p) {
     return tri_is_valid(p[0], p[1], p[2]);
 }
 
-PR_DEV bool transform_main(const SetupParams& P, const ObjCache* C, uint32_t t, SubVtx* v, float* recipw, int* matid,
-                           bool* contained) {
+// The transform and the culls of transform_main (screen positions, -1/W,
+// the object); false when a cull drops the triangle.
+PR_DEV bool transform_main_geom(const SetupParams& P, const ObjCache* C, uint32_t t, SubVtx* v, float* recipw,
+                                uint32_t* obj, bool* contained) {
     V4 p[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) p[k] = ld4(P.pos[t * 3 + k]);
@@ -386,6 +396,13 @@ PR_DEV bool transform_main(const SetupParams& P, const ObjCache* C, uint32_t t, 
     const Box vp = {0.0f, 0.0f, -1.0f, (float)P.W, (float)P.H, 1.0f};
     if (!box_intersect(vp, box3(v[0].pos, v[1].pos, v[2].pos))) return false;
     *contained = box_contains(vp, v[0].pos) && box_contains(vp, v[1].pos) && box_contains(vp, v[2].pos);
+    *obj = o;
+    return true;
+}
+
+// The per-vertex attributes of surviving triangle t of object o (the normal
+// matrix Apply does not influence the culls).
+PR_DEV void vertex_attrs(const SetupParams& P, uint32_t t, uint32_t o, SubVtx* v, int* matid) {
     const float* nm = P.obj_normal + o * 16;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -398,6 +415,13 @@ PR_DEV bool transform_main(const SetupParams& P, const ObjCache* C, uint32_t t, 
     int m = P.mat[t];
     if (m >= 0) m += P.obj_matbase[o];
     *matid = m;
+}
+
+PR_DEV bool transform_main(const SetupParams& P, const ObjCache* C, uint32_t t, SubVtx* v, float* recipw, int* matid,
+                           bool* contained) {
+    uint32_t o;
+    if (!transform_main_geom(P, C, t, v, recipw, &o, contained)) return false;
+    vertex_attrs(P, t, o, v, matid);
     return true;
 }
 
@@ -408,7 +432,9 @@ PR_DEV void setup_main_one(const SetupParams& P, const ObjCache* C, uint32_t t, 
     float recipw[3];
     int matid = -1;
     bool contained = false;
-    const bool ok = t < P.n_tris && transform_main(P, C, t, v, recipw, &matid, &contained);
+    uint32_t obj = 0;
+    const bool ok = t < P.n_tris && transform_main_geom(P, C, t, v, recipw, &obj, &contained);
+    if (ok && !P.defer_attr) vertex_attrs(P, t, obj, v, &matid);
     if (ok && P.tri_scr) {
         float4* s = reinterpret_cast<float4*>(P.tri_scr + 12 * (size_t)t);
         s[0] = make_float4(v[0].pos.x, v[0].pos.y, recipw[0], v[1].pos.x);
@@ -778,6 +804,57 @@ PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint
 __global__ void resolve_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
                                const uint32_t* beaten, const Counters* cnt, uint32_t* win, float* depth_ao) {
     resolve_one(W, H, keys, nanseq, beaten, cnt, win, depth_ao, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// resolve_kernel that also lists the winners' deferred attribute records:
+// the first pixel to find its record pending (1 -> 2) appends it.
+__global__ void resolve_listing_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
+                                       const uint32_t* beaten, Counters* cnt, uint32_t* win, float* depth_ao,
+                                       const uint32_t* first_rec, uint32_t* attr_state, uint32_t* vis) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    resolve_one(W, H, keys, nanseq, beaten, cnt, win, depth_ao, i);
+    bool want = false;
+    uint32_t ridx = 0;
+    if (i < (size_t)W * H) {
+        const uint32_t w = win[i];
+        if (w != kNone) {
+            ridx = first_rec[w >> 3] + (w & 7u);
+            want = atomicCAS(&attr_state[ridx], 1u, 2u) == 1u;
+        }
+    }
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, want);
+    if (m) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&cnt->n_vis, (uint32_t)__popc(m));
+        base = __shfl_sync(act, base, leader);
+        if (want) vis[base + __popc(m & ((1u << lane) - 1u))] = ridx;
+    }
+}
+
+// The deferred attribute records of the listed records: everything comes
+// back from the raster record (screen positions, -1/W, the triangle in seq)
+// and the scene, by the same functions the setup uses, so the bits are
+// those an eager setup writes.
+__global__ void __launch_bounds__(128) attr_kernel(const __grid_constant__ SetupParams P, const uint32_t* vis) {
+    const uint32_t n = P.cnt->n_vis;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t ridx = vis[j];
+        const float4* rp = reinterpret_cast<const float4*>(P.rrec + ridx);
+        const float4 q0 = rp[0], q1 = rp[1], q2 = rp[2], q3 = rp[3];
+        const uint32_t t = __float_as_uint(q3.x) >> 3;
+        SubVtx v[3];
+        v[0].pos = V4{q0.x, q0.y, q0.z, 1.0f};
+        v[1].pos = V4{q0.w, q1.x, q1.y, 1.0f};
+        v[2].pos = V4{q1.z, q1.w, q2.x, 1.0f};
+        const float recipw[3] = {q3.y, q3.z, q3.w};
+        uint32_t o = P.blk_obj[t >> 7];
+        while (o + 1 < P.n_objects && P.obj_first[o + 1] <= t) o++;
+        int matid = -1;
+        vertex_attrs(P, t, o, v, &matid);
+        write_attr(P, ridx, v, recipw, matid);
+    }
 }
 
 // Shadow NaN fix-up: pixels that saw a NaN-depth fragment restart from NaN
@@ -1603,6 +1680,18 @@ int check(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
 int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stream) {
     if (p.n_tris == 0) return 0;
     setup_main_kernel<<<(p.n_tris + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
+    return check(cudaGetLastError());
+}
+int launch_resolve_listing(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
+                           Counters* cnt, uint32_t* win, float* depth_ao, const uint32_t* first_rec,
+                           uint32_t* attr_state, uint32_t* vis, void* stream) {
+    size_t n = (size_t)W * H;
+    resolve_listing_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        W, H, keys, nanseq, beaten, cnt, win, depth_ao, first_rec, attr_state, vis);
+    return check(cudaGetLastError());
+}
+int launch_attr(const SetupParams& p, const uint32_t* vis, void* stream) {
+    attr_kernel<<<(unsigned)sm_count() * 8u, 128, 0, (cudaStream_t)stream>>>(p, vis);
     return check(cudaGetLastError());
 }
 int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uint32_t n_objects, float* out,

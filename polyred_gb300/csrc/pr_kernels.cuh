@@ -30,7 +30,7 @@ struct alignas(16) RasterRec {
     uint32_t bx;    // x0 | x1 << 16 (pixel bbox clamped to the buffer)
     uint32_t by;    // y0 | y1 << 16
     uint32_t seq;   // draw order: tri*8 + clip sub-index (main view), tri (shadow)
-    uint32_t pad[3];
+    float recipw[3];  // main view: the parent triangle's -1/W (for attributes computed later)
 };
 static_assert(sizeof(RasterRec) == 64, "RasterRec is four float4");
 
@@ -58,7 +58,8 @@ struct Counters {
     uint32_t need_tasks;  // tasks needed when overflow
     uint32_t n_ao;        // pixels listed for ambient occlusion
     uint32_t take[2];     // raster work-queue heads: the pass, its NaN fix-up pass
-    uint32_t pad[5];
+    uint32_t n_vis;       // records listed for their attributes (resolve)
+    uint32_t pad[4];
 };
 
 struct LightK {
@@ -78,6 +79,8 @@ struct SetupParams {
     const uint32_t* obj_first;   // [n_objects + 1]
     const float* obj_model;      // [n_objects][16]
     const float* obj_trans;      // [n_objects][16] this pass's Proj·View·Model, or null: per-block cache
+    uint32_t* attr_state;        // per record: 1 = attributes deferred, 0 = written here; null: no bookkeeping
+    int defer_attr;              // 1: leave the attribute record to attr_kernel (visible records only)
     const uint32_t* blk_obj;     // [n_tris / 128] object of each 128-triangle block's first triangle
     const float* obj_normal;     // [n_objects][16] Model.Inv().T()
     const int32_t* obj_matbase;  // [n_objects]
@@ -217,6 +220,13 @@ struct PassMats {
 };
 int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uint32_t n_objects, float* out,
                      void* stream);
+// Resolve that also lists, once each, the winning records whose attributes
+// were deferred (attr_state 1 -> 2) in vis (count in cnt->n_vis).
+int launch_resolve_listing(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
+                           Counters* cnt, uint32_t* win, float* depth_ao, const uint32_t* first_rec,
+                           uint32_t* attr_state, uint32_t* vis, void* stream);
+// The attribute records of the records resolve listed (P: the main view's setup parameters).
+int launch_attr(const SetupParams& p, const uint32_t* vis, void* stream);
 int launch_setup_shadow(const SetupParams& p, void* stream);
 int launch_raster(const RasterParams& p, int n_blocks, void* stream);
 int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
