@@ -819,7 +819,8 @@ __global__ void resolve_listing_kernel(int W, int H, const unsigned long long* k
         const uint32_t w = win[i];
         if (w != kNone) {
             ridx = first_rec[w >> 3] + (w & 7u);
-            want = atomicCAS(&attr_state[ridx], 1u, 2u) == 1u;
+            // most pixels find their record listed already: a plain read first
+            want = attr_state[ridx] == 1u && atomicCAS(&attr_state[ridx], 1u, 2u) == 1u;
         }
     }
     const unsigned act = __activemask();
@@ -836,24 +837,56 @@ __global__ void resolve_listing_kernel(int W, int H, const unsigned long long* k
 // The deferred attribute records of the listed records: everything comes
 // back from the raster record (screen positions, -1/W, the triangle in seq)
 // and the scene, by the same functions the setup uses, so the bits are
-// those an eager setup writes.
+// those an eager setup writes. Three lanes per record, one per vertex (ten
+// records per warp), and the face normal from the three world positions
+// gathered by shuffles.
 __global__ void __launch_bounds__(128) attr_kernel(const __grid_constant__ SetupParams P, const uint32_t* vis) {
     const uint32_t n = P.cnt->n_vis;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t ridx = vis[j];
-        const float4* rp = reinterpret_cast<const float4*>(P.rrec + ridx);
-        const float4 q0 = rp[0], q1 = rp[1], q2 = rp[2], q3 = rp[3];
-        const uint32_t t = __float_as_uint(q3.x) >> 3;
-        SubVtx v[3];
-        v[0].pos = V4{q0.x, q0.y, q0.z, 1.0f};
-        v[1].pos = V4{q0.w, q1.x, q1.y, 1.0f};
-        v[2].pos = V4{q1.z, q1.w, q2.x, 1.0f};
-        const float recipw[3] = {q3.y, q3.z, q3.w};
-        uint32_t o = P.blk_obj[t >> 7];
-        while (o + 1 < P.n_objects && P.obj_first[o + 1] <= t) o++;
-        int matid = -1;
-        vertex_attrs(P, t, o, v, &matid);
-        write_attr(P, ridx, v, recipw, matid);
+    const int lane = threadIdx.x & 31, r = lane / 3, k = lane - 3 * r;
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = wid * 10u; base < n; base += nw * 10u) {
+        const uint32_t j = base + (uint32_t)r;
+        const bool act = lane < 30 && j < n;
+        V4 m = {0.0f, 0.0f, 0.0f, 0.0f};
+        uint32_t ridx = 0, t = 0, o = 0;
+        if (act) {
+            ridx = vis[j];
+            const float* R = reinterpret_cast<const float*>(P.rrec + ridx);
+            t = __float_as_uint(R[12]) >> 3;
+            o = P.blk_obj[t >> 7];
+            while (o + 1 < P.n_objects && P.obj_first[o + 1] <= t) o++;
+            const V4 pos = {R[3 * k], R[3 * k + 1], R[3 * k + 2], 1.0f};
+            const V4 nor = apply4_outline(ld4(P.nor[t * 3 + k]), P.obj_normal + o * 16);
+            const float2 uv = P.uv[t * 3 + k];
+            m = apply4_outline(apply4_outline(apply4_outline(pos, P.viewport_inv), P.proj_inv), P.view_inv);  // render/raster.go:467-469
+            float* A = reinterpret_cast<float*>(P.arec + ridx);
+            A[k] = R[13 + k];  // recipw
+            A[3 + 3 * k] = nor.x;
+            A[4 + 3 * k] = nor.y;
+            A[5 + 3 * k] = nor.z;
+            A[12 + 2 * k] = uv.x;
+            A[13 + 2 * k] = uv.y;
+            A[18 + k] = __uint_as_float(pack_col(P.col[t * 3 + k]));
+            A[21 + 3 * k] = m.x;
+            A[22 + 3 * k] = m.y;
+            A[23 + 3 * k] = m.z;
+        }
+        const float m1x = __shfl_down_sync(0xffffffffu, m.x, 1), m1y = __shfl_down_sync(0xffffffffu, m.y, 1),
+                    m1z = __shfl_down_sync(0xffffffffu, m.z, 1);
+        const float m2x = __shfl_down_sync(0xffffffffu, m.x, 2), m2y = __shfl_down_sync(0xffffffffu, m.y, 2),
+                    m2z = __shfl_down_sync(0xffffffffu, m.z, 2);
+        if (act && k == 0) {
+            const V4 m1 = {m1x, m1y, m1z, 0.0f}, m2 = {m2x, m2y, m2z, 0.0f};
+            const V4 fn = unit4(cross4(sub4(m1, m), sub4(m2, m)));  // render/raster.go:479
+            float* A = reinterpret_cast<float*>(P.arec + ridx);
+            A[30] = fn.x;
+            A[31] = fn.y;
+            A[32] = fn.z;
+            A[33] = fn.w;
+            int matid = P.mat[t];
+            if (matid >= 0) matid += P.obj_matbase[o];
+            A[34] = __int_as_float(matid);
+        }
     }
 }
 
