@@ -823,14 +823,23 @@ __global__ void resolve_listing_kernel(int W, int H, const unsigned long long* k
             want = attr_state[ridx] == 1u && atomicCAS(&attr_state[ridx], 1u, 2u) == 1u;
         }
     }
-    const unsigned act = __activemask();
-    const unsigned m = __ballot_sync(act, want);
-    if (m) {
-        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&cnt->n_vis, (uint32_t)__popc(m));
-        base = __shfl_sync(act, base, leader);
-        if (want) vis[base + __popc(m & ((1u << lane) - 1u))] = ridx;
+    // one atomic per block on the list's counter (256 threads, every one reaches here)
+    __shared__ uint32_t s_cnt[8];
+    __shared__ uint32_t s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (lane == 0) s_cnt[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < 8; w++) tot += s_cnt[w];
+        s_base = tot ? atomicAdd(&cnt->n_vis, tot) : 0u;
+    }
+    __syncthreads();
+    if (want) {
+        uint32_t o = s_base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        for (int w = 0; w < warp; w++) o += s_cnt[w];
+        vis[o] = ridx;
     }
 }
 
@@ -841,8 +850,9 @@ __global__ void resolve_listing_kernel(int W, int H, const unsigned long long* k
 // records per warp), and the face normal from the three world positions
 // gathered by shuffles.
 __global__ void __launch_bounds__(128) attr_kernel(const __grid_constant__ SetupParams P, const uint32_t* vis) {
+    __shared__ __align__(16) float s_rec[4][10][36];  // each warp's ten records, stored whole
     const uint32_t n = P.cnt->n_vis;
-    const int lane = threadIdx.x & 31, r = lane / 3, k = lane - 3 * r;
+    const int lane = threadIdx.x & 31, r = lane / 3, k = lane - 3 * r, warp = threadIdx.x >> 5;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t base = wid * 10u; base < n; base += nw * 10u) {
         const uint32_t j = base + (uint32_t)r;
@@ -859,7 +869,7 @@ __global__ void __launch_bounds__(128) attr_kernel(const __grid_constant__ Setup
             const V4 nor = apply4_outline(ld4(P.nor[t * 3 + k]), P.obj_normal + o * 16);
             const float2 uv = P.uv[t * 3 + k];
             m = apply4_outline(apply4_outline(apply4_outline(pos, P.viewport_inv), P.proj_inv), P.view_inv);  // render/raster.go:467-469
-            float* A = reinterpret_cast<float*>(P.arec + ridx);
+            float* A = s_rec[warp][r];
             A[k] = R[13 + k];  // recipw
             A[3 + 3 * k] = nor.x;
             A[4 + 3 * k] = nor.y;
@@ -878,7 +888,7 @@ __global__ void __launch_bounds__(128) attr_kernel(const __grid_constant__ Setup
         if (act && k == 0) {
             const V4 m1 = {m1x, m1y, m1z, 0.0f}, m2 = {m2x, m2y, m2z, 0.0f};
             const V4 fn = unit4(cross4(sub4(m1, m), sub4(m2, m)));  // render/raster.go:479
-            float* A = reinterpret_cast<float*>(P.arec + ridx);
+            float* A = s_rec[warp][r];
             A[30] = fn.x;
             A[31] = fn.y;
             A[32] = fn.z;
@@ -886,7 +896,16 @@ __global__ void __launch_bounds__(128) attr_kernel(const __grid_constant__ Setup
             int matid = P.mat[t];
             if (matid >= 0) matid += P.obj_matbase[o];
             A[34] = __int_as_float(matid);
+            A[35] = 0.0f;
         }
+        __syncwarp();
+        // the warp's records out as whole 16-byte words: 9 per record
+        const uint32_t nr = min(10u, n - base);
+        for (uint32_t e = (uint32_t)lane; e < nr * 9u; e += 32u) {
+            const uint32_t rr = e / 9u, w4 = e - rr * 9u;
+            reinterpret_cast<float4*>(P.arec + vis[base + rr])[w4] = reinterpret_cast<const float4*>(s_rec[warp][rr])[w4];
+        }
+        __syncwarp();
     }
 }
 
