@@ -772,12 +772,14 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
     if (P.take) {
         // Dynamic: a task's cost is its bbox chunk, and consecutive tasks of
         // one object tend to be alike, so a static stride leaves a tail.
+        // four 32-task batches per atomic: one counter serves every warp of the pass
         for (;;) {
             uint32_t base = 0;
-            if ((threadIdx.x & 31) == 0) base = atomicAdd(P.take, 32u);
+            if ((threadIdx.x & 31) == 0) base = atomicAdd(P.take, 128u);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= n_tasks) break;
-            raster_warp(P, base, n_tasks, s_w[warp]);
+            const uint32_t end = min(base + 128u, n_tasks);
+            for (uint32_t b = base; b < end; b += 32u) raster_warp(P, b, n_tasks, s_w[warp]);
         }
         return;
     }
