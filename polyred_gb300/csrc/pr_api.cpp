@@ -422,6 +422,11 @@ void fill_shade_frame(const Ctx* c, const pr_frame_desc* f, const M4& s2w, int S
     std::memcpy(sp.s2w, s2w.m, 64);
     M4 svp = prh::viewport((float)SW, (float)SH);
     std::memcpy(sp.shadow_vp, svp.m, 64);
+    auto unit_bottom = [](const float* m) { return m[12] == 0.0f && m[13] == 0.0f && m[14] == 0.0f && m[15] == 1.0f; };
+    for (uint32_t l = 0; l < f->n_lights; l++) {
+        prk::LightK& K = sp.lights[l];
+        K.sfast = unit_bottom(K.lview) && unit_bottom(K.lproj) && unit_bottom(svp.m) ? 1 : 0;
+    }
     sp.SW = SW;
     sp.SH = SH;
     prh::gamma_table(sp.gamma);

@@ -978,6 +978,88 @@ PR_DEV void diff_gbuffer_pixel(const ShadeParams& P, size_t i, uint32_t seq, int
     D[3] = make_float4(fn.x, fn.y, fn.z, fn.w);
 }
 
+// The shadow test of one light (render/raster.go:339-352, render/shadow.go:230-283):
+// ws (ViewportToWorld of the pixel) through the light's view, projection and
+// the map viewport, then the map depth 0.03 in front of the pixel's.
+__device__ __noinline__ bool shadow_hit_exact(const ShadeParams& P, const LightK& L, V4 ws, size_t plane, int li) {
+    const V4 sc = pos4(apply4(apply4(apply4(ws, L.lview), L.lproj), P.shadow_vp));
+    const long long lx = go_f2i(sc.x), ly = go_f2i(sc.y);
+    const long long idx =
+        (long long)((unsigned long long)lx + (unsigned long long)ly * (unsigned long long)(long long)P.SW);
+    if (idx > 0 && idx < (long long)plane) {
+        const float sz = fkey_decode(P.smaps[plane * li + (size_t)idx]);
+        return sc.z < __fsub_rn(sz, 0.03f);
+    }
+    return false;
+}
+
+// Vec4.Apply evaluated with single-rounding FMAs, and a bound on its distance
+// from the reference's Apply (FMAs through float64) of the exact input, given
+// a bound e on the input's distance (e.w = 0: the bottom row (0, 0, 0, 1)
+// passes w through unchanged in both). Per row, both evaluations lie within
+// g sum_j |m_ij||input_j| of their exact values (g = gamma_4 = 4u'/(1-4u'),
+// u' = 2^-24 (1 + 2^-28) covering the double rounding), so
+// |fast - reference| <= sum_j |m_ij| (e_j (1 + g) + 2g |x_j|), all in upward
+// rounding (1 + g <= 1.0000005, 2g <= 4.8e-7).
+PR_DEV V4 apply4_bounded(V4 x, V4 e, const float* m, V4* eo) {
+    const V4 y = {__fmaf_rn(m[0], x.x, __fmaf_rn(m[1], x.y, __fmaf_rn(m[2], x.z, __fmul_rn(m[3], x.w)))),
+                  __fmaf_rn(m[4], x.x, __fmaf_rn(m[5], x.y, __fmaf_rn(m[6], x.z, __fmul_rn(m[7], x.w)))),
+                  __fmaf_rn(m[8], x.x, __fmaf_rn(m[9], x.y, __fmaf_rn(m[10], x.z, __fmul_rn(m[11], x.w)))),
+                  __fmaf_rn(m[12], x.x, __fmaf_rn(m[13], x.y, __fmaf_rn(m[14], x.z, __fmul_rn(m[15], x.w))))};
+    const float c1 = 1.0000005f, c2 = 4.8e-7f;
+    const float w0 = __fmaf_ru(e.x, c1, __fmul_ru(c2, fabsf(x.x))), w1 = __fmaf_ru(e.y, c1, __fmul_ru(c2, fabsf(x.y)));
+    const float w2 = __fmaf_ru(e.z, c1, __fmul_ru(c2, fabsf(x.z))), w3 = __fmul_ru(c2, fabsf(x.w));
+    *eo = V4{__fmaf_ru(fabsf(m[0]), w0, __fmaf_ru(fabsf(m[1]), w1, __fmaf_ru(fabsf(m[2]), w2, __fmul_ru(fabsf(m[3]), w3)))),
+             __fmaf_ru(fabsf(m[4]), w0, __fmaf_ru(fabsf(m[5]), w1, __fmaf_ru(fabsf(m[6]), w2, __fmul_ru(fabsf(m[7]), w3)))),
+             __fmaf_ru(fabsf(m[8]), w0, __fmaf_ru(fabsf(m[9]), w1, __fmaf_ru(fabsf(m[10]), w2, __fmul_ru(fabsf(m[11]), w3)))),
+             0.0f};
+    return y;
+}
+
+// shadow_hit_exact from the single-rounding transform, when its bound
+// decides every outcome (both truncated map coordinates and the depth
+// compare); false: undecided, the caller runs the exact test. The division
+// by w uses the same iw = RN(1/w) in both, so it scales the bound by |iw|
+// and adds two roundings (2u |sc| < 2.4e-7 |sc|); 1e-30 covers underflow.
+PR_DEV bool shadow_hit_fast(const ShadeParams& P, const LightK& L, V4 ws, size_t plane, int li, bool* hit) {
+    V4 e = {0.0f, 0.0f, 0.0f, 0.0f};
+    V4 v = apply4_bounded(ws, e, L.lview, &e);
+    v = apply4_bounded(v, e, L.lproj, &e);
+    v = apply4_bounded(v, e, P.shadow_vp, &e);
+    float sx = v.x, sy = v.y, sz = v.z, ia = 1.0f;
+    if (!(v.w == 1.0f || v.w == 0.0f)) {  // pos4
+        const float iw = __fdiv_rn(1.0f, v.w);
+        sx = __fmul_rn(v.x, iw);
+        sy = __fmul_rn(v.y, iw);
+        sz = __fmul_rn(v.z, iw);
+        ia = __fmul_ru(fabsf(iw), 1.0000002f);
+    }
+    const float dx = __fadd_ru(__fmaf_ru(ia, e.x, __fmul_ru(2.4e-7f, fabsf(sx))), 1e-30f);
+    const float dy = __fadd_ru(__fmaf_ru(ia, e.y, __fmul_ru(2.4e-7f, fabsf(sy))), 1e-30f);
+    const float dz = __fadd_ru(__fmaf_ru(ia, e.z, __fmul_ru(2.4e-7f, fabsf(sz))), 1e-30f);
+    const float xl = __fsub_rd(sx, dx), xh = __fadd_ru(sx, dx);
+    const float yl = __fsub_rd(sy, dy), yh = __fadd_ru(sy, dy);
+    if (!(fabsf(xl) < 8388608.0f && fabsf(xh) < 8388608.0f && fabsf(yl) < 8388608.0f && fabsf(yh) < 8388608.0f))
+        return false;
+    const int lx = trunc_small(xl), ly = trunc_small(yl);
+    if (lx != trunc_small(xh) || ly != trunc_small(yh)) return false;
+    const long long idx = (long long)lx + (long long)ly * (long long)P.SW;
+    if (!(idx > 0 && idx < (long long)plane)) {
+        *hit = false;
+        return true;
+    }
+    const float thr = __fsub_rn(fkey_decode(P.smaps[plane * li + (size_t)idx]), 0.03f);
+    if (__fadd_ru(sz, dz) < thr) {
+        *hit = true;
+        return true;
+    }
+    if (__fsub_rd(sz, dz) >= thr) {
+        *hit = false;
+        return true;
+    }
+    return false;
+}
+
 // Returns true for a pixel that AO still has to finish (its pre-AO colour is
 // in rgba; the caller lists it).
 PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
@@ -1132,13 +1214,9 @@ PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
                         occl++;
                         continue;
                     }
-                    V4 sc = pos4(apply4(apply4(apply4(ws, L.lview), L.lproj), P.shadow_vp));
-                    long long lx = go_f2i(sc.x), ly = go_f2i(sc.y);
-                    long long idx = (long long)((unsigned long long)lx + (unsigned long long)ly * (unsigned long long)(long long)P.SW);
-                    if (idx > 0 && idx < (long long)plane) {
-                        float sz = fkey_decode(P.smaps[plane * li + (size_t)idx]);
-                        if (sc.z < __fsub_rn(sz, 0.03f)) occl++;
-                    }
+                    bool hit = false;
+                    if (!(L.sfast && shadow_hit_fast(P, L, ws, plane, li, &hit))) hit = shadow_hit_exact(P, L, ws, plane, li);
+                    occl += hit ? 1 : 0;
                 }
                 float w = pow_half(occl);
                 shadow_w = w;

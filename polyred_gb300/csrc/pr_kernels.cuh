@@ -67,6 +67,8 @@ struct LightK {
     float pos[3], dir[3], intensity;
     float color[3];
     float lview[16], lproj[16];
+    int32_t sfast;    // 1: the bottom rows of lview, lproj and the map viewport are exactly (0, 0, 0, 1)
+    int32_t pad_[3];
 };
 
 // Per-view setup parameters (passed by value).
