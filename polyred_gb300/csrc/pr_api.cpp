@@ -340,6 +340,14 @@ int ensure_work(Ctx* c, uint32_t need_rec, uint32_t need_tasks) {
     return PR_OK;
 }
 
+// ViewportMatrix's pattern (pr_hostmath viewport): zeros and ones where
+// apply_viewport relies on them.
+int viewport_std(const float* m) {
+    for (int e : {1, 2, 4, 6, 8, 9, 11, 12, 13, 14})
+        if (m[e] != 0.0f) return 0;
+    return (m[10] == 1.0f && m[15] == 1.0f) ? 1 : 0;
+}
+
 void fill_scene_ptrs(Ctx* c, prk::SetupParams& p) {
     p.pos = c->sb.pos.p;
     p.nor = c->sb.nor.p;
@@ -558,6 +566,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 M4 lpv = prh::mulm(loadm(f->lights[l].shadow_proj), loadm(f->lights[l].shadow_view));
                 std::memcpy(sp.pv, lpv.m, 64);
                 std::memcpy(sp.viewport, svp.m, 64);
+                sp.vp_std = viewport_std(sp.viewport);
                 sp.rrec = c->rrec_s.p;
                 sp.arec = nullptr;
                 sp.cap_rec = c->cap_rec;
@@ -602,6 +611,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         mp.attr_state = c->attr_state.p;
         mp.defer_attr = 1;  // attribute records for winning records only (attr_kernel after resolve)
         std::memcpy(mp.viewport, vp.m, 64);
+        mp.vp_std = viewport_std(mp.viewport);
         std::memcpy(mp.viewport_inv, vp_inv.m, 64);
         std::memcpy(mp.proj_inv, proj_inv.m, 64);
         std::memcpy(mp.view_inv, view_inv.m, 64);
@@ -1405,6 +1415,7 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
         std::memcpy(sp.pv, lpv.m, 64);
         M4 svp = prh::viewport((float)SW, (float)SH);
         std::memcpy(sp.viewport, svp.m, 64);
+        sp.vp_std = viewport_std(sp.viewport);
         sp.rrec = b->rrec.p + q.rec;
         sp.arec = nullptr;
         sp.cap_rec = std::max<uint32_t>(c->sb.n_tris, 1);
@@ -1448,6 +1459,7 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
         mp.perspective = (f->flags & PR_FRAME_PERSPECTIVE) ? 1 : 0;
         std::memcpy(mp.pv, m.pv.m, 64);
         std::memcpy(mp.viewport, m.vp.m, 64);
+        mp.vp_std = viewport_std(mp.viewport);
         std::memcpy(mp.viewport_inv, m.vp_inv.m, 64);
         std::memcpy(mp.proj_inv, m.proj_inv.m, 64);
         std::memcpy(mp.view_inv, m.view_inv.m, 64);

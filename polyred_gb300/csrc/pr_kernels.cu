@@ -258,6 +258,24 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
     return area;
 }
 
+// Vec4.Apply(ViewportMatrix) for a matrix of ViewportMatrix's pattern
+// [sx 0 0 tx; 0 sy 0 ty; 0 0 1 0; 0 0 0 1] (P.vp_std). A zero first factor,
+// or a factor 1 with a +-0 addend, rounds exactly in float64 and float32
+// alike, so only the sx and sy terms need the float64-FMA emulation; the
+// matrix's own entries stay in every term (signs of zero included).
+__device__ __noinline__ V4 apply_viewport_exact(V4 v, const float* m) { return apply4(v, m); }
+PR_DEV V4 apply_viewport(V4 v, const float* m) {
+    bool bad = false;
+    const V4 r = {fma64f_try(m[0], v.x, __fmaf_rn(m[1], v.y, __fmaf_rn(m[2], v.z, __fmul_rn(m[3], v.w))), bad),
+                  __fmaf_rn(m[4], v.x, fma64f_try(m[5], v.y, __fmaf_rn(m[6], v.z, __fmul_rn(m[7], v.w)), bad)),
+                  __fmaf_rn(m[8], v.x, __fmaf_rn(m[9], v.y, __fmaf_rn(m[10], v.z, __fmul_rn(m[11], v.w)))),
+                  __fmaf_rn(m[12], v.x, __fmaf_rn(m[13], v.y, __fmaf_rn(m[14], v.z, __fmul_rn(m[15], v.w))))};
+    return __builtin_expect(bad, 0) ? apply_viewport_exact(v, m) : r;
+}
+PR_DEV V4 viewport_apply(const SetupParams& P, V4 v) {
+    return P.vp_std ? apply_viewport(v, P.viewport) : apply4_outline(v, P.viewport);
+}
+
 // ---- warp-aggregated reservations (all 32 lanes must call them) ----------
 
 PR_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -387,7 +405,7 @@ PR_DEV bool transform_main_geom(const SetupParams& P, const ObjCache* C, uint32_
     for (int k = 0; k < 3; k++) {
         const V4 cp = mulv(trans, p[k]);
         recipw[k] = P.perspective ? __fdiv_rn(-1.0f, cp.w) : 1.0f;
-        v[k].pos = pos4(apply4_outline(cp, P.viewport));
+        v[k].pos = pos4(viewport_apply(P, cp));
     }
     // cullBackFace (render/cull.go:26-28)
     if (cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y), __fsub_rn(v[2].pos.x, v[0].pos.x),
@@ -533,7 +551,7 @@ PR_DEV void setup_shadow_one(const SetupParams& P, const ObjCache* C, uint32_t t
             object_trans(P, C, t, trans);
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                v[k].pos = pos4(apply4_outline(mulv(trans, p[k]), P.viewport));
+                v[k].pos = pos4(viewport_apply(P, mulv(trans, p[k])));
                 v[k].nor = {0, 0, 0, 0};
                 v[k].u = v[k].v = 0;
                 v[k].col = 0;

@@ -91,6 +91,7 @@ struct SetupParams {
     int perspective;
     float pv[16];                // Proj.MulM(View)
     float viewport[16];
+    int vp_std;                  // 1: viewport has ViewportMatrix's zero/one pattern (apply_viewport)
     float viewport_inv[16], proj_inv[16], view_inv[16];
     RasterRec* rrec;
     AttrRec* arec;
