@@ -821,12 +821,8 @@ PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint
     win[i] = w;
     depth_ao[i] = d;
 }
-__global__ void resolve_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
-                               const uint32_t* beaten, const Counters* cnt, uint32_t* win, float* depth_ao) {
-    resolve_one(W, H, keys, nanseq, beaten, cnt, win, depth_ao, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
-}
 
-// resolve_kernel that also lists the winners' deferred attribute records:
+// Resolve (resolve_one) that also lists the winners' deferred attribute records:
 // the first pixel to find its record pending (1 -> 2) appends it.
 __global__ void resolve_listing_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
                                        const uint32_t* beaten, Counters* cnt, uint32_t* win, float* depth_ao,
@@ -1858,17 +1854,6 @@ int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream) {
     clip_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
     return check(cudaGetLastError());
 }
-int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream) {
-    if (p.n_tris == 0) return 0;
-    unsigned nb = (p.n_tris + 127) / 128;
-    setup_main_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return check(e);
-    // The clip list length is known only on the device: size the grid for
-    // the worst case; idle blocks exit at once.
-    clip_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
-    return check(cudaGetLastError());
-}
 int launch_setup_shadow(const SetupParams& p, void* stream) {
     if (p.n_tris == 0) return 0;
     unsigned nb = (p.n_tris + 127) / 128;
@@ -1877,13 +1862,6 @@ int launch_setup_shadow(const SetupParams& p, void* stream) {
 }
 int launch_raster(const RasterParams& p, int n_blocks, void* stream) {
     raster_kernel<<<n_blocks, kRasterWarps * 32, 0, (cudaStream_t)stream>>>(p);
-    return check(cudaGetLastError());
-}
-int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
-                   const Counters* cnt, uint32_t* win, float* depth_ao, void* stream) {
-    size_t n = (size_t)W * H;
-    resolve_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(W, H, keys, nanseq, beaten, cnt, win,
-                                                                                   depth_ao);
     return check(cudaGetLastError());
 }
 int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,

@@ -212,7 +212,6 @@ struct DiffParamsK {
 
 // Launch wrappers implemented in pr_kernels.cu (host-callable).
 namespace prk {
-int launch_setup_main(const SetupParams& p, uint32_t* clip_list, void* stream);  // setup, then clip
 int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stream);
 int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream);
 // Proj·View·Model of every object for n_pass passes: out[pass][o][16] from
@@ -232,8 +231,6 @@ int launch_resolve_listing(int W, int H, const unsigned long long* keys, const u
 int launch_attr(const SetupParams& p, const uint32_t* vis, void* stream);
 int launch_setup_shadow(const SetupParams& p, void* stream);
 int launch_raster(const RasterParams& p, int n_blocks, void* stream);
-int launch_resolve(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
-                   const Counters* cnt, uint32_t* win, float* depth_ao, void* stream);
 int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* smap, const Counters* cnt,
                               void* stream);
 // After a pass that saw a NaN fragment (cnt->nan_flag): a[0..n) = va and, if b, b[0..n) = vb.
