@@ -70,6 +70,8 @@ def test_null_arguments_are_errors(native_lib):
     assert b"NULL" in native_lib.pr_last_error()
     assert native_lib.pr_host_alloc(16, None) == _abi.PR_ERR_INVALID_ARG
     assert native_lib.pr_host_free(None) == _abi.PR_ERR_INVALID_ARG
+    assert native_lib.pr_frame_submit(None, None, None, None) == _abi.PR_ERR_INVALID_ARG
+    assert native_lib.pr_sync(None) == _abi.PR_ERR_INVALID_ARG
 
 
 def test_singular_inverse(native_lib):
