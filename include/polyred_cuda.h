@@ -54,6 +54,8 @@ extern "C" {
 #define PR_ERR_NO_DEVICE     -9
 #define PR_ERR_SINGULAR     -10  /* Mat4.Inv of a zero determinant; the
                                     reference panics (math/mat4.go:261-263) */
+#define PR_ERR_FATAL        -11  /* input the reference rejects with a panic
+                                    rather than an error (pr_obj_parse) */
 
 /* ---- flags ------------------------------------------------------------ */
 /* material.Standard flags (material/material.go:23-29) */
@@ -423,6 +425,76 @@ int pr_diff_forward(void* ctx, const pr_frame_desc* frame, const pr_diff_params*
  * grad_radiance: DEVICE [H][W][4] (alpha ignored). Returns when done. */
 int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params* params, const float* gbuf,
                      const float* grad_radiance, pr_diff_grads* grads);
+
+/* ---- OBJ / MTL parsing ------------------------------------------------
+ * Replaces model/obj/obj.go: obj.Load's line parsers (File.parse,
+ * parseObjLine, parseMtlLine, obj.go:139-611) as one pass over a text
+ * buffer; the host keeps the file handling of obj.Load (obj.go:78-137: which
+ * .mtl to read, the fallback to <name>.mtl, default materials when the .mtl
+ * fails) and model.Load's mesh assembly (model/load.go:40-152). Host only:
+ * no CUDA call, no device needed.
+ *
+ * A handle holds one obj.File's state. Feed it the .obj text, then the .mtl
+ * text, in the reference's order: the current material carries over from
+ * the .obj into the .mtl as it does in the reference. Numbers parse as Go's
+ * strconv.ParseFloat(s, 32) / ParseInt(s, 10, 32) / ParseUint(s, 10, 32).
+ *
+ * pr_obj_parse returns PR_ERR_INVALID_ARG where obj.go returns an error
+ * (message in pr_last_error(): "<what> in line:<n>" or strconv's text), and
+ * PR_ERR_FATAL where the reference panics (an .mtl property before any
+ * material, a colour outside [0, 1]). Lines before the failing one stay
+ * parsed. */
+#define PR_OBJ_TEXT_OBJ  0
+#define PR_OBJ_TEXT_MTL  1
+#define PR_OBJ_NO_INDEX  4294967295LL  /* obj.go's invINDEX: corner without vt / vn */
+
+typedef struct pr_obj_material {  /* obj.Material (obj.go:57-68) */
+    int32_t name;          /* offset of the name in pr_obj_info.strings */
+    int32_t map_kd;        /* offset of map_Kd's file name; -1: none */
+    int32_t illum;
+    float   opacity;       /* d */
+    float   refraction;    /* Ni */
+    float   shininess;     /* Ns */
+    uint8_t ambient[4];    /* Ka, Kd, Ks, Ke through color.FromValue; alpha 255 */
+    uint8_t diffuse[4];
+    uint8_t specular[4];
+    uint8_t emissive[4];
+} pr_obj_material;
+
+typedef struct pr_obj_info {     /* views into the handle, valid until its next parse or destroy */
+    uint32_t size;               /* sizeof(pr_obj_info), set by the caller */
+    uint32_t reserved;
+    const float* vertices;  int64_t n_vertices;   /* [n][3], 'v' with w divided in */
+    const float* normals;   int64_t n_normals;    /* [n][3] */
+    const float* uvs;       int64_t n_uvs;        /* [n][2] */
+    int64_t n_faces;
+    int64_t n_corners;
+    const int64_t* face_start;      /* [n_faces + 1]: corners of face i are [face_start[i], face_start[i+1]) */
+    const int64_t* corner_v;        /* [n_corners] 0-based; relative indices resolved (may be out of range) */
+    const int64_t* corner_vt;       /* [n_corners]; PR_OBJ_NO_INDEX when absent */
+    const int64_t* corner_vn;       /* [n_corners]; PR_OBJ_NO_INDEX when absent */
+    const int32_t* face_object;     /* [n_faces] object of each face */
+    const int32_t* face_material;   /* [n_faces] material index; -1: obj.go's "polyred_default" */
+    const uint8_t* face_smooth;     /* [n_faces] */
+    int64_t n_objects;               /* 'o' / 'g' lines and implicit "unnamed<line>" objects */
+    const int32_t* object_name;      /* [n_objects] string offsets */
+    const int64_t* object_mat_start; /* [n_objects + 1] ranges of object_mat */
+    const int32_t* object_mat;       /* Object.Materials as material indices */
+    int64_t n_materials;             /* in order of first mention */
+    const pr_obj_material* materials;
+    int64_t n_warnings;
+    const int32_t* warnings;         /* string offsets, File.Warnings */
+    const char* strings;  int64_t strings_len;   /* NUL-terminated entries */
+    int32_t matlib;                  /* last mtllib file name; -1: none */
+    int32_t current_material;        /* matCurrent; -1: none */
+    int64_t line;                    /* File.line after the last parse */
+} pr_obj_info;
+
+int pr_obj_create(void** out);
+int pr_obj_destroy(void* obj);
+/* kind: PR_OBJ_TEXT_OBJ or PR_OBJ_TEXT_MTL; text need not be NUL-terminated */
+int pr_obj_parse(void* obj, int kind, const char* text, size_t len);
+int pr_obj_get(void* obj, pr_obj_info* out);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,7 @@ PR_ERR_NO_SCENE = -7
 PR_ERR_UNSUPPORTED = -8
 PR_ERR_NO_DEVICE = -9
 PR_ERR_SINGULAR = -10
+PR_ERR_FATAL = -11
 
 PR_MAT_FLAT_SHADING = 1
 PR_MAT_AO = 2
@@ -35,6 +36,10 @@ PR_SCENE_DEVICE_PTRS = 1
 PR_OUT_DEVICE_PTRS = 1
 
 PR_TRI_NONE = 0xFFFFFFFF
+
+PR_OBJ_TEXT_OBJ = 0
+PR_OBJ_TEXT_MTL = 1
+PR_OBJ_NO_INDEX = 4294967295
 
 F16 = C.c_float * 16
 
@@ -161,6 +166,32 @@ class pr_batch_stats(C.Structure):
     ]
 
 
+class pr_obj_material(C.Structure):
+    _fields_ = [("name", C.c_int32), ("map_kd", C.c_int32), ("illum", C.c_int32), ("opacity", C.c_float),
+                ("refraction", C.c_float), ("shininess", C.c_float), ("ambient", C.c_uint8 * 4),
+                ("diffuse", C.c_uint8 * 4), ("specular", C.c_uint8 * 4), ("emissive", C.c_uint8 * 4)]
+
+
+class pr_obj_info(C.Structure):
+    _fields_ = [
+        ("size", C.c_uint32), ("reserved", C.c_uint32),
+        ("vertices", C.POINTER(C.c_float)), ("n_vertices", C.c_int64),
+        ("normals", C.POINTER(C.c_float)), ("n_normals", C.c_int64),
+        ("uvs", C.POINTER(C.c_float)), ("n_uvs", C.c_int64),
+        ("n_faces", C.c_int64), ("n_corners", C.c_int64),
+        ("face_start", C.POINTER(C.c_int64)), ("corner_v", C.POINTER(C.c_int64)),
+        ("corner_vt", C.POINTER(C.c_int64)), ("corner_vn", C.POINTER(C.c_int64)),
+        ("face_object", C.POINTER(C.c_int32)), ("face_material", C.POINTER(C.c_int32)),
+        ("face_smooth", C.POINTER(C.c_uint8)),
+        ("n_objects", C.c_int64), ("object_name", C.POINTER(C.c_int32)),
+        ("object_mat_start", C.POINTER(C.c_int64)), ("object_mat", C.POINTER(C.c_int32)),
+        ("n_materials", C.c_int64), ("materials", C.POINTER(pr_obj_material)),
+        ("n_warnings", C.c_int64), ("warnings", C.POINTER(C.c_int32)),
+        ("strings", C.c_void_p), ("strings_len", C.c_int64),
+        ("matlib", C.c_int32), ("current_material", C.c_int32), ("line", C.c_int64),
+    ]
+
+
 ENTRY_POINTS = [
     ("pr_abi_version", C.c_int, []),
     ("pr_error_string", C.c_char_p, [C.c_int]),
@@ -194,6 +225,10 @@ ENTRY_POINTS = [
                                   C.POINTER(pr_outputs)]),
     ("pr_diff_backward", C.c_int, [VP, C.POINTER(pr_frame_desc), C.POINTER(pr_diff_params), VP, VP,
                                    C.POINTER(pr_diff_grads)]),
+    ("pr_obj_create", C.c_int, [C.POINTER(VP)]),
+    ("pr_obj_destroy", C.c_int, [VP]),
+    ("pr_obj_parse", C.c_int, [VP, C.c_int, C.c_char_p, C.c_size_t]),
+    ("pr_obj_get", C.c_int, [VP, C.POINTER(pr_obj_info)]),
 ]
 
 

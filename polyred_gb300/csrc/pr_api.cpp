@@ -808,6 +808,7 @@ const char* pr_error_string(int status) {
         case PR_ERR_UNSUPPORTED: return "unsupported input";
         case PR_ERR_NO_DEVICE: return "no CUDA device";
         case PR_ERR_SINGULAR: return "singular matrix";
+        case PR_ERR_FATAL: return "input the reference rejects with a panic";
         default: return "unknown status";
     }
 }

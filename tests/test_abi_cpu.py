@@ -42,7 +42,8 @@ def test_struct_layouts_match_the_header(tmp_path):
     import subprocess
     structs = [_abi.pr_object, _abi.pr_material, _abi.pr_scene_desc, _abi.pr_light, _abi.pr_frame_desc,
                _abi.pr_outputs, _abi.pr_stats, _abi.pr_depth_map_desc, _abi.pr_diff_params,
-               _abi.pr_diff_grads, _abi.pr_batch_view, _abi.pr_batch_stats]
+               _abi.pr_diff_grads, _abi.pr_batch_view, _abi.pr_batch_stats, _abi.pr_obj_material,
+               _abi.pr_obj_info]
     lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){"]
     for st in structs:
         n = st.__name__
