@@ -313,6 +313,82 @@ def measure_soup(steps=10, n_tris=10_000_000, width=3840, height=2160):
             "ms_shade": st.ms_shade}
 
 
+def measure_obj(steps=20, n_tori=32, nu=128, nv=64, width=1920, height=1080):
+    """OBJ ingestion (model.Load): a 41 MB Wavefront OBJ of 32 tori (524,288
+    triangles from 262,144 quads, v/vt/vn, three .mtl materials, some
+    triangle+quad objects) in a temporary directory. Host phases, best of 3
+    wall-clock runs: native parse (file read included), mesh assembly, scene
+    flatten + upload. Then resident frames of the loaded scene at
+    width x height (one shadow-casting point light, 2048^2 map), CUDA
+    events. CPU baseline: the oracle's pure-Python restatement of obj.go on
+    the first 1 MB of the same text."""
+    import tempfile
+    import torch
+    from oracle import objparse
+    from polyred_gb300 import _abi, native, objload, procedural, render
+    obj, mtl, n_tris = procedural.obj_tori(n_tori, nu, nv)
+    tmp = tempfile.mkdtemp()
+    path = os.path.join(tmp, "tori.obj")
+    with open(path, "wb") as fh:
+        fh.write(obj)
+    with open(os.path.join(tmp, "tori.mtl"), "wb") as fh:
+        fh.write(mtl)
+    dev = render.Device(0)
+    lib = native.load()
+    t_parse = t_build = t_up = float("inf")
+    for _ in range(3):
+        t0 = time.perf_counter()
+        f = objload.parse_file(path)
+        t1 = time.perf_counter()
+        g = objload.build_group(f, path)
+        t2 = time.perf_counter()
+        s, cam = procedural.obj_tori_scene(g, width, height)
+        flat = render.FlatScene(s)
+        desc = flat.desc()
+        native.check(lib.pr_scene_upload(dev.handle, C.byref(desc)))
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        t_parse, t_build, t_up = min(t_parse, t1 - t0), min(t_build, t2 - t1), min(t_up, t3 - t2)
+    opts = dict(width=width, height=height, camera=cam, scene=s, perspective=True, shadow_map=True, gamma=True,
+                background=(0, 0, 0, 0), shadow_size=(2048, 2048), directional_shadows=False)
+    fd = render.FrameDesc(opts, shadow_cams(opts))
+    rgba = torch.empty((height, width, 4), dtype=torch.uint8, device="cuda")
+    od = _abi.pr_outputs()
+    od.size = C.sizeof(_abi.pr_outputs)
+    od.flags = _abi.PR_OUT_DEVICE_PTRS
+    od.rgba = rgba.data_ptr()
+    for _ in range(3):
+        native.check(lib.pr_render(dev.handle, C.byref(fd.desc), C.byref(od)))
+    stream = torch.cuda.ExternalStream(dev.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        native.check(lib.pr_render_async(dev.handle, C.byref(fd.desc), C.byref(od)))
+        native.check(lib.pr_sync(dev.handle))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    dev.close()
+    sample = obj[:1 << 20]
+    sample = sample[:sample.rindex(b"\n") + 1]
+    spath = os.path.join(tmp, "sample.obj")
+    with open(spath, "wb") as fh:
+        fh.write(sample.replace(b"mtllib tori.mtl\n", b""))
+    c0 = time.perf_counter()
+    objparse.load_file(spath)
+    c1 = time.perf_counter()
+    mb = len(obj) / 1e6
+    return {"workload": f"Wavefront OBJ, {n_tori} tori of {nu}x{nv} quads ({mb:.1f} MB, {n_tris} triangles), "
+                        f"{width}x{height}",
+            "file_mb": mb, "n_tris": n_tris, "parse_ms": t_parse * 1e3, "parse_mb_s": mb / t_parse,
+            "assemble_ms": t_build * 1e3, "flatten_upload_ms": t_up * 1e3,
+            "load_to_resident_ms": (t_parse + t_build + t_up) * 1e3,
+            "frame_ms": ms, "frame_mtri_s": n_tris / (ms / 1e3) / 1e6,
+            "cpu_baseline": {"value": len(sample) / 1e6 / (c1 - c0), "unit": "MB/s", "cores": 1, "kind": "port",
+                             "sample": "obj.go restated in pure Python, first 1 MB of the same OBJ text"}}
+
+
 def measure_batch(reps=3):
     """The batched workload (32 sphere scenes of 1k-500k triangles, 8 ring
     views each at 1280x720, 16 casting point lights per scene with 1024^2
@@ -408,6 +484,7 @@ def main():
     ap.add_argument("--adam", type=int, default=0, help="also run this many Adam steps over 16 views")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-views measurement")
     ap.add_argument("--no-soup", action="store_true", help="skip the 10M-triangle 4K soup measurement")
+    ap.add_argument("--no-obj", action="store_true", help="skip the OBJ ingestion measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -549,6 +626,11 @@ def main():
             line["soup_4k"] = measure_soup()
         if not args.no_batch:
             line["batched"] = measure_batch()
+        if not args.no_obj:
+            try:
+                line["obj_ingest"] = measure_obj()
+            except Exception as e:  # the headline line must still print
+                line["obj_ingest"] = {"error": f"{type(e).__name__}: {e}"}
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line), flush=True)

@@ -85,14 +85,25 @@ enum LineStatus { L_OK = 0, L_ERROR = 1, L_FATAL = 2 };
 
 // ---------------------------------------------------------------- fields
 
-bool ascii_space(unsigned char c) { return c == ' ' || (c >= '\t' && c <= '\r'); }
+// Byte classes: 1 = ASCII white space (\t \n \v \f \r ' '), 2 = a lead byte
+// of a non-ASCII white-space rune (C2, E1, E2, E3), 0 = anything else.
+struct ByteClass {
+    unsigned char c[256];
+    ByteClass() {
+        memset(c, 0, sizeof(c));
+        for (int b : {' ', '\t', '\n', '\v', '\f', '\r'}) c[b] = 1;
+        for (int b : {0xC2, 0xE1, 0xE2, 0xE3}) c[b] = 2;
+    }
+};
+const ByteClass kClass;
 
 // Width of the unicode.IsSpace rune starting at p (0 if none). Non-ASCII
 // white space is U+0085, U+00A0, U+1680, U+2000..U+200A, U+2028, U+2029,
 // U+202F, U+205F and U+3000; their lead bytes (C2, E1, E2, E3) never
 // continue another sequence, so they mark rune boundaries whatever precedes.
-size_t space_width(const unsigned char* p, const unsigned char* end) {
-    if (ascii_space(*p)) return 1;
+inline size_t space_width(const unsigned char* p, const unsigned char* end) {
+    unsigned char k = kClass.c[*p];
+    if (k != 2) return k;
     size_t left = (size_t)(end - p);
     if (p[0] == 0xC2 && left >= 2 && (p[1] == 0x85 || p[1] == 0xA0)) return 2;
     if (left >= 3) {
@@ -192,6 +203,56 @@ size_t common_prefix_ci(const char* s, size_t n, const char* word) {
     size_t i = 0;
     while (i < n && word[i] && lower(s[i]) == word[i]) i++;
     return i;
+}
+
+// Clinger's fast path (W. D. Clinger, "How to Read Floating Point Numbers
+// Accurately", PLDI 1990): when the decimal digits form an integer
+// M <= 2^24 and the power of ten k has |k| <= 10, both M and 10^|k| are
+// exact floats, so one IEEE multiply or divide rounds the exact value
+// correctly. `m` is a well-formed unsigned decimal without '_'. Returns
+// false when the text is outside the fast path.
+bool clinger_fast(const char* m, size_t n, float* out) {
+    static const float kPow10[11] = {1e0f, 1e1f, 1e2f, 1e3f, 1e4f, 1e5f, 1e6f, 1e7f, 1e8f, 1e9f, 1e10f};
+    uint64_t mant = 0;
+    int digits = 0, frac = 0;
+    bool dot = false;
+    size_t i = 0;
+    for (; i < n; i++) {
+        char c = m[i];
+        if (c == '.') {
+            dot = true;
+            continue;
+        }
+        if (!is_dec(c)) break;
+        if (mant == 0 && c == '0') {  // leading zeros carry no digits
+            if (dot) frac++;
+            continue;
+        }
+        if (++digits > 8) return false;
+        mant = mant * 10 + (uint64_t)(c - '0');
+        if (dot) frac++;
+    }
+    int exp = 0;
+    if (i < n) {  // 'e' / 'E' [sign] digits
+        i++;
+        bool eneg = false;
+        if (m[i] == '+' || m[i] == '-') eneg = m[i++] == '-';
+        for (; i < n; i++) {
+            exp = exp * 10 + (m[i] - '0');
+            if (exp > 100) return false;
+        }
+        if (eneg) exp = -exp;
+    }
+    if (mant > (1u << 24)) return false;
+    int k = exp - frac;
+    if (mant == 0) {
+        *out = 0.0f;
+        return true;
+    }
+    if (k < -10 || k > 10) return false;
+    float f = (float)mant;
+    *out = k < 0 ? f / kPow10[-k] : f * kPow10[k];
+    return true;
 }
 
 // strconv.ParseFloat(s, 32). Returns false with *msg set on error.
@@ -299,6 +360,10 @@ bool parse_f32(Span sp, float* out, std::string* msg) {
     }
     float v = 0;
     bool range = false;
+    if (!hex && !underscores && clinger_fast(m, mn, &v)) {
+        *out = neg ? -v : v;
+        return true;
+    }
     if (!hex) {
         auto r = std::from_chars(m, m + mn, v, std::chars_format::general);
         if (r.ec == std::errc::result_out_of_range || r.ptr != m + mn) {

@@ -279,6 +279,11 @@ def load(path, image_textures="error", skip_faceless=False):
         f = parse_file(path)
     except ObjError as e:
         raise ObjError(f"model: cannot load the given file {path}: {e}") from None
+    return build_group(f, path, image_textures, skip_faceless)
+
+
+def build_group(f, path="", image_textures="error", skip_faceless=False):
+    """loadObj's second half (model/load.go:47-152) on a parsed ObjFile."""
     mats = _materials(f, path, image_textures)
     default = default_material()
     names = f.material_names

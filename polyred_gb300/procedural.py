@@ -8,6 +8,9 @@
                   U[-10,10]^3, radii U[0.2,1.5], 4 materials, point +
                   directional light, AO and shadow maps
   triangle_soup   small random triangles with log-normal screen area
+  obj_tori        Wavefront OBJ / MTL text of a field of tori (quads with vt
+                  and vn, three materials, some triangle+quad objects, some
+                  negative indices) for the OBJ loading path
 
 Random numbers: splitmix64 seeds a xoshiro128** generator; floats are the top
 24 bits of a draw times 2^-24.
@@ -253,4 +256,80 @@ def soup_scene(n_tris, width, height, seed=0x5EED0003):
     s = sc.Scene(sc.Geometry(mesh, mat), sc.Point(position=(0, 5, 5)), sc.Ambient(intensity=0.1))
     cam = sc.Perspective(position=(0, 0, 0), target=(0, 0, -1), up=(0, 1, 0), fov=60, aspect=width / height, near=0.1,
                          far=120)
+    return s, cam
+
+
+# ---------------------------------------------------------------- OBJ text
+
+OBJ_TORI_MTL = (b"newmtl m0\nKa 1 1 1\nKd 0.8 0.3 0.2\nKs 0.5 0.5 0.5\nNs 32\nillum 2\n"
+                b"newmtl m1\nKd 0.2 0.6 0.9\nKs 0.3 0.3 0.3\nNs 64\nd 1\nillum 2\n"
+                b"newmtl m2\nKd 0.9 0.9 0.9\nKs 0.1 0.1 0.1\nNs 8\nillum 0\n")
+
+
+def _rows(tag, arr, fmt):
+    line = tag + " " + " ".join([fmt] * arr.shape[1])
+    return "\n".join(line % tuple(r) for r in arr.tolist())
+
+
+def obj_tori(n_tori=32, nu=128, nv=64, seed=0x0B17041, hybrid_every=3, relative_every=4):
+    """OBJ and MTL text of n_tori tori, each 'o torus<k>' with 'usemtl
+    m<k % 3>', nu x nv grid vertices (v, vt, vn) and nu x nv quad faces
+    wound outward. Every hybrid_every-th torus writes its first 16 quads as
+    two triangles each (triangles + quads: the reference's PolygonMesh,
+    MaterialID -1); every relative_every-th uses negative (relative)
+    indices. Centres U[-8,8] x U[-2,2] x U[-8,8], R U[0.8,1.6], r = R x
+    U[0.2,0.4], tilted about x by U[0, pi). Returns (obj_bytes, mtl_bytes,
+    n_tris)."""
+    rng = Xoshiro128(seed)
+    out = ["# tori field: %d tori of %d x %d quads" % (n_tori, nu, nv), "mtllib tori.mtl"]
+    iu, jv = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    u = (2.0 * np.pi * iu / nu).reshape(-1)
+    v = (2.0 * np.pi * jv / nv).reshape(-1)
+    a = (iu * nv + jv).reshape(-1)
+    b = (((iu + 1) % nu) * nv + jv).reshape(-1)
+    c = (((iu + 1) % nu) * nv + (jv + 1) % nv).reshape(-1)
+    d = (iu * nv + (jv + 1) % nv).reshape(-1)
+    quads = np.stack([a, d, c, b], axis=1)  # outward: (d - a) x (b - a) points away from the tube
+    uv = np.stack([iu.reshape(-1) / nu, jv.reshape(-1) / nv], axis=1)
+    count = 0
+    n_tris = 0
+    for k in range(n_tori):
+        cx, cy, cz = rng.uniform(-8, 8), rng.uniform(-2, 2), rng.uniform(-8, 8)
+        R = rng.uniform(0.8, 1.6)
+        r = R * rng.uniform(0.2, 0.4)
+        ang = rng.uniform(0.0, math.pi)
+        ca, sa = math.cos(ang), math.sin(ang)
+        x = (R + r * np.cos(v)) * np.cos(u)
+        y = r * np.sin(v)
+        z = (R + r * np.cos(v)) * np.sin(u)
+        nx, ny, nz = np.cos(v) * np.cos(u), np.sin(v), np.cos(v) * np.sin(u)
+        pos = np.stack([x + cx, y * ca - z * sa + cy, y * sa + z * ca + cz], axis=1)
+        nor = np.stack([nx, ny * ca - nz * sa, ny * sa + nz * ca], axis=1)
+        out += ["o torus%d" % k, "usemtl m%d" % (k % 3), _rows("v", pos, "%.6f"), _rows("vt", uv, "%.5f"),
+                _rows("vn", nor, "%.5f"), "s 1"]
+        first = count + 1
+        count += nu * nv
+        idx = quads + (first - count - 1 if k % relative_every == relative_every - 1 else first)
+        faces = idx.tolist()
+        lines = []
+        start = 0
+        if k % hybrid_every == hybrid_every - 1:
+            for q in faces[:16]:
+                lines.append("f %d/%d/%d %d/%d/%d %d/%d/%d" % (q[0], q[0], q[0], q[1], q[1], q[1], q[2], q[2], q[2]))
+                lines.append("f %d/%d/%d %d/%d/%d %d/%d/%d" % (q[0], q[0], q[0], q[2], q[2], q[2], q[3], q[3], q[3]))
+            start = 16
+        lines += ["f %d/%d/%d %d/%d/%d %d/%d/%d %d/%d/%d" % (q[0], q[0], q[0], q[1], q[1], q[1], q[2], q[2], q[2],
+                                                              q[3], q[3], q[3]) for q in faces[start:]]
+        out.append("\n".join(lines))
+        n_tris += 2 * nu * nv
+    return ("\n".join(out) + "\n").encode(), OBJ_TORI_MTL, n_tris
+
+
+def obj_tori_scene(group, width, height, shadows=True):
+    """The tori group with a shadow-casting point light, a directional light
+    and ambient 0.15, seen from (0, 9, 18) with a 45-degree perspective."""
+    s = sc.Scene(group, sc.Point(position=(6, 10, 8), intensity=1.0, cast_shadow=shadows),
+                 sc.Directional(direction=(-1, -2, -1), intensity=0.4), sc.Ambient(intensity=0.15))
+    cam = sc.Perspective(position=(0, 9, 18), target=(0, 0, 0), up=(0, 1, 0), fov=45.0, aspect=width / height,
+                         near=0.1, far=100.0)
     return s, cam

@@ -296,6 +296,10 @@ VALID_NUMBERS = [
     "0.30000001192092896", "9999999999999999999999999", "1_000", "1_0.5_0e1_0", "0x1p0", "0x1.8p1", "-0x.1p4",
     "0X1P-149", "0x1p-150", "0x1.000001p0", "0x1_0p0", "0x_1p0", "inf", "-inf", "+Inf", "INFINITY", "-Infinity",
     "nan", "NaN", "NAN", "00001.5000", "1e0000000000000000000010",
+    # both sides of the exact fast path: <= 8 digits and M <= 2^24, |k| <= 10
+    "16777216", "16777216e10", "1677721.6", "16777217e-10", "12345678e-10", "12345678e-11", "1.2345678e10",
+    "9.9999999e-11", "0.00000000012345678", "99999999", "1e10", "1e11", "1e-10", "1e-11", "0.0000001e-3",
+    "4.2949673e9", "-0.000000", "+00000000000000.00000000001",
 ]
 
 INVALID_NUMBERS = [
