@@ -50,7 +50,7 @@ extern "C" {
 #define PR_ERR_TIMEOUT       -5  /* a bounded device wait gave up */
 #define PR_ERR_UNIMPLEMENTED -6
 #define PR_ERR_NO_SCENE      -7
-#define PR_ERR_UNSUPPORTED   -8  /* e.g. MSAA != 1, a non-uniform texture */
+#define PR_ERR_UNSUPPORTED   -8  /* e.g. a non-uniform texture, MSAA in a batch */
 #define PR_ERR_NO_DEVICE     -9
 #define PR_ERR_SINGULAR     -10  /* Mat4.Inv of a zero determinant; the
                                     reference panics (math/mat4.go:261-263) */
@@ -141,9 +141,9 @@ typedef struct pr_light {
 } pr_light;
 
 typedef struct pr_frame_desc {
-    uint32_t size;
+    uint32_t size;           /* sizeof(pr_frame_desc); PR_FRAME_DESC_SIZE_V1 (no msaa field) is accepted */
     uint32_t flags;          /* PR_FRAME_* */
-    int32_t  width, height;  /* framebuffer size (MSAA 1) */
+    int32_t  width, height;  /* render.Size: the image Render() returns */
     float    view[16];       /* Camera.ViewMatrix() */
     float    proj[16];       /* Camera.ProjMatrix() */
     float    cam_pos[3];     /* Camera.Position() */
@@ -154,7 +154,20 @@ typedef struct pr_frame_desc {
     const float*    ambient; /* [n_ambient] light.Environment intensities, traversal order */
     int32_t  shadow_width;   /* 0 = framebuffer size (the reference's only mode) */
     int32_t  shadow_height;
+    /* render.MSAA(n) (render/options.go:66-68), 1..16; 0 counts as 1. The
+     * frame renders into a framebuffer of (n*width) x (n*height)
+     * (render/raster.go:147-151) whose viewport test and clipping use n times
+     * the framebuffer size, as the reference's draw and cullViewFrustum do
+     * (render/raster.go:414-441, render/cull.go:15-23); the shadow maps
+     * default to the framebuffer size. passAntialiasing's imageutil.Resize
+     * (internal/imageutil/resize.go:16-66) then scales the RGBA image to
+     * width x height. With n > 1 pr_outputs.rgba is [height][width][4] and
+     * every other output is [n*height][n*width] (the framebuffer). Not
+     * available in batches and the adjoint (PR_ERR_UNSUPPORTED). */
+    int32_t  msaa;
+    int32_t  reserved;
 } pr_frame_desc;
+#define PR_FRAME_DESC_SIZE_V1 192u  /* pr_frame_desc up to shadow_height */
 
 /* ---- outputs ------------------------------------------------------------
  * Every array is optional (NULL = not wanted). Rows are top-down: row r holds

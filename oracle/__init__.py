@@ -26,6 +26,8 @@ def load():
         build()
         from polyred_gb300 import _abi
         lib = C.CDLL(LIB)
+        lib.orc_resize.restype = C.c_int
+        lib.orc_resize.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         lib.orc_render.restype = C.c_int
         lib.orc_render.argtypes = [C.POINTER(_abi.pr_scene_desc), C.POINTER(_abi.pr_frame_desc),
                                    C.c_void_p, C.c_int, C.POINTER(_abi.pr_outputs), C.c_void_p]
@@ -172,3 +174,14 @@ def diff_backward64(inp, grad):
         setattr(o, k, res[v].ctypes.data)
     lib.orc_diff_backward64(C.byref(inp.s), g.ctypes.data, C.byref(o))
     return res
+
+
+def resize(img, width, height):
+    """imageutil.Resize of an (H, W, 4) uint8 image to (height, width, 4)."""
+    import numpy as np
+    img = np.ascontiguousarray(img, np.uint8)
+    out = np.zeros((height, width, 4), np.uint8)
+    rc = load().orc_resize(img.ctypes.data, img.shape[1], img.shape[0], width, height, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"orc_resize failed: {rc}")
+    return out

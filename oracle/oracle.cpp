@@ -105,6 +105,7 @@ struct Ctx {
     const pr_scene_desc* sc;
     const pr_frame_desc* fr;
     int W, H, SW, SH;
+    int M;  // render.MSAA: W, H are already M times the image
     bool perspect;
     FB* fb;
 };
@@ -292,14 +293,15 @@ void draw(Ctx& c, const MVP& mvp, const Vtx& in1, const Vtx& in2, const Vtx& in3
     // cullBackFace (render/cull.go:26-28)
     if (cross4(sub4(t2.pos, t1.pos), sub4(t3.pos, t1.pos)).z < 0) return;
     V3 ps[3] = {to3(t1.pos), to3(t2.pos), to3(t3.pos)};
-    AABB vp{{0, 0, -1}, {(float)c.W, (float)c.H, 1}};
+    // viewportAABB: Max = MSAA * the (already MSAA-sized) buffer
+    AABB vp{{0, 0, -1}, {(float)(c.M * c.W), (float)(c.M * c.H), 1}};
     if (!aabb_intersect(vp, new_aabb(ps, 3))) return;
     if (aabb_contains(vp, ps, 3)) {
         draw_clipped(c, mvp, t1, t2, t3, recipw, matid, tri);
         return;
     }
     if (clipped) *clipped = true;
-    std::vector<V4> clips = sutherland_hodgman({t1.pos, t2.pos, t3.pos}, (float)c.W, (float)c.H);
+    std::vector<V4> clips = sutherland_hodgman({t1.pos, t2.pos, t3.pos}, (float)(c.M * c.W), (float)(c.M * c.H));
     for (size_t i = 2; i < clips.size(); i++) {
         Vtx a = clip_vertex(clips[0], t1, t2, t3);
         Vtx b = clip_vertex(clips[i - 1], t1, t2, t3);
@@ -352,7 +354,7 @@ void draw_depth(const Ctx& c, float* depths, const MVP& mvp, const Vtx& v1, cons
     for (int k = 0; k < 3; k++) p[k] = pos4(apply4(mulv(mvp.trans, vs[k]->pos), mvp.viewport));
     if (cross4(sub4(p[1], p[0]), sub4(p[2], p[0])).z < 0) return;
     // cullViewFrustum (render/cull.go:15-23)
-    V3 vpc[3] = {{(float)c.SW, (float)c.SH, 1}, {0, 0, 0}, {0, 0, -1}};
+    V3 vpc[3] = {{(float)(c.SW * c.M), (float)(c.SH * c.M), 1}, {0, 0, 0}, {0, 0, -1}};
     AABB vp = new_aabb(vpc, 3);
     V3 ps[3] = {to3(p[0]), to3(p[1]), to3(p[2])};
     AABB ta = new_aabb(ps, 3);
@@ -572,6 +574,74 @@ void parallel_rows(int threads, int H, F&& fn) {
 
 // ---------------------------------------------------------------- C API
 
+// ---- passAntialiasing: imageutil.Resize (internal/imageutil/resize.go:16-181)
+
+float resize_linear(float in) {
+    in = std::fabs(in);
+    if (in <= 1) return 1 - in;
+    return 0;
+}
+
+// createWeights8 with the linear kernel: int16 taps (x256) and start indices
+void create_weights8(int dy, int filter_length, float scale, std::vector<int16_t>& coeffs, std::vector<int>& start,
+                     int& len) {
+    len = filter_length * (int)std::max(std::ceil(scale), 1.0f);
+    float factor = std::min(1.0f / scale, 1.0f);
+    coeffs.assign((size_t)dy * len, 0);
+    start.assign(dy, 0);
+    for (int y = 0; y < dy; y++) {
+        float interp = scale * ((float)y + 0.5f) - 0.5f;
+        start[y] = (int)interp - len / 2 + 1;
+        interp -= (float)start[y];
+        for (int i = 0; i < len; i++) {
+            float in = (interp - (float)i) * factor;
+            coeffs[(size_t)y * len + i] = (int16_t)(resize_linear(in) * 256);
+        }
+    }
+}
+
+// resizeRGBA: `in` has in_dx pixels per row; writes out (out_dx x out_dy),
+// out row y column x from in row x (the passes transpose).
+void resize_rgba(const uint8_t* in, int in_dx, uint8_t* out, int out_dx, int out_dy,
+                 const std::vector<int16_t>& coeffs, const std::vector<int>& start, int len) {
+    const int maxX = in_dx - 1;
+    for (int x = 0; x < out_dx; x++) {
+        const uint8_t* row = in + (size_t)x * in_dx * 4;
+        for (int y = 0; y < out_dy; y++) {
+            int32_t rgba[4] = {0, 0, 0, 0}, sum = 0;
+            for (int i = 0; i < len; i++) {
+                int32_t coeff = coeffs[(size_t)y * len + i];
+                if (coeff == 0) continue;
+                int xi = start[y] + i;
+                if ((unsigned)xi < (unsigned)maxX)
+                    xi *= 4;
+                else if (xi >= maxX)
+                    xi = 4 * maxX;
+                else
+                    xi = 0;
+                for (int k = 0; k < 4; k++) rgba[k] += coeff * (int32_t)row[xi + k];
+                sum += coeff;
+            }
+            for (int k = 0; k < 4; k++) {
+                int v = rgba[k] / sum;
+                out[((size_t)y * out_dx + x) * 4 + k] = (uint8_t)std::min(std::max(v, 0), 255);
+            }
+        }
+    }
+}
+
+void resize_image(const uint8_t* img, int dx, int dy, int width, int height, uint8_t* out) {
+    float scale_x = (float)dx / (float)width, scale_y = (float)dy / (float)height;
+    std::vector<int16_t> coeffs;
+    std::vector<int> start;
+    int len;
+    std::vector<uint8_t> temp((size_t)dy * width * 4);  // Dx = dy, Dy = width (transposed)
+    create_weights8(width, 2, scale_x, coeffs, start, len);
+    resize_rgba(img, dx, temp.data(), dy, width, coeffs, start, len);
+    create_weights8(height, 2, scale_y, coeffs, start, len);
+    resize_rgba(temp.data(), dy, out, width, height, coeffs, start, len);
+}
+
 extern "C" {
 
 void orc_ao_directions(float cosv[8], float sinv[8], int* n) {
@@ -688,14 +758,26 @@ int orc_shadow_camera(const float light_pos[3], const float center[3], const flo
     return PR_OK;
 }
 
+// imageutil.Resize of a dx x dy RGBA image (rows top-down) to w x h.
+int orc_resize(const uint8_t* img, int dx, int dy, int w, int h, uint8_t* out) {
+    if (!img || !out || dx <= 0 || dy <= 0 || w <= 0 || h <= 0) return PR_ERR_INVALID_ARG;
+    if (dx == w && dy == h) {
+        std::memcpy(out, img, (size_t)dx * dy * 4);
+        return PR_OK;
+    }
+    resize_image(img, dx, dy, w, h, out);
+    return PR_OK;
+}
+
 int orc_render(const pr_scene_desc* sc, const pr_frame_desc* fr, float* shadow_state, int threads,
                pr_outputs* out, orc_stats* st) {
     if (!sc || !fr || fr->width <= 0 || fr->height <= 0) return PR_ERR_INVALID_ARG;
     Ctx c;
     c.sc = sc;
     c.fr = fr;
-    c.W = fr->width;
-    c.H = fr->height;
+    c.M = (fr->size >= offsetof(pr_frame_desc, msaa) + sizeof(int32_t) && fr->msaa > 1) ? fr->msaa : 1;
+    c.W = fr->width * c.M;
+    c.H = fr->height * c.M;
     c.SW = fr->shadow_width > 0 ? fr->shadow_width : c.W;
     c.SH = fr->shadow_height > 0 ? fr->shadow_height : c.H;
     c.perspect = (fr->flags & PR_FRAME_PERSPECTIVE) != 0;
@@ -796,7 +878,12 @@ int orc_render(const pr_scene_desc* sc, const pr_frame_desc* fr, float* shadow_s
     if (shadow_state) std::memcpy(shadow_state, sdepth.data(), sdepth.size() * sizeof(float));
     if (out) {
         size_t n = (size_t)c.W * c.H;
-        if (out->rgba) std::memcpy(out->rgba, color.data(), n * 4);
+        if (out->rgba) {
+            if (c.M > 1)
+                resize_image(color.data(), c.W, c.H, fr->width, fr->height, out->rgba);
+            else
+                std::memcpy(out->rgba, color.data(), n * 4);
+        }
         for (size_t i = 0; i < n; i++) {
             const Frag& f = frags[i];
             if (out->tri_id) out->tri_id[i] = f.ok ? f.tri : PR_TRI_NONE;

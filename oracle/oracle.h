@@ -19,6 +19,9 @@ typedef struct orc_stats {
 // One Render() of the reference in single-worker order. shadow_state is the
 // persistent [n_lights][SH][SW] shadow-map storage (read, then updated), or
 // NULL for zeroed maps. threads > 1 splits rows (same result, see oracle.cpp).
+/* imageutil.Resize (internal/imageutil/resize.go:16-181) of a dx x dy RGBA
+ * image, rows top-down, to w x h */
+int orc_resize(const uint8_t* img, int dx, int dy, int w, int h, uint8_t* out);
 int orc_render(const pr_scene_desc* scene, const pr_frame_desc* frame, float* shadow_state, int threads,
                pr_outputs* out, orc_stats* stats);
 

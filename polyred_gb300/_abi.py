@@ -73,7 +73,10 @@ class pr_frame_desc(C.Structure):
                 ("view", F16), ("proj", F16), ("cam_pos", C.c_float * 3), ("background", C.c_uint8 * 4),
                 ("n_lights", C.c_uint32), ("n_ambient", C.c_uint32), ("lights", C.POINTER(pr_light)),
                 ("ambient", C.POINTER(C.c_float)), ("shadow_width", C.c_int32),
-                ("shadow_height", C.c_int32)]
+                ("shadow_height", C.c_int32), ("msaa", C.c_int32), ("reserved", C.c_int32)]
+
+
+PR_FRAME_DESC_SIZE_V1 = 192
 
 
 class pr_outputs(C.Structure):

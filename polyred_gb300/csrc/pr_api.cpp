@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -161,7 +162,7 @@ struct Ctx {
     DevBuf<prk::Counters> cnt;  // [kNumCounters]
     prk::Counters* h_cnt = nullptr;  // pinned mirror
     // staging for host outputs
-    DevBuf<uint8_t> o_rgba, o_vcol;
+    DevBuf<uint8_t> o_rgba, o_vcol, o_msaa;
     DevBuf<uint32_t> o_tri;
     DevBuf<float> o_depth, o_shadow;
     DevBuf<float4> o_nor, o_fnor, o_wpos, o_uvd;
@@ -364,11 +365,20 @@ void fill_scene_ptrs(Ctx* c, prk::SetupParams& p) {
     p.n_objects = (uint32_t)c->sb.objects.size();
 }
 
+// render.MSAA of a frame: 1 for descriptors without the field or with 0 / 1.
+int frame_msaa(const pr_frame_desc* f) {
+    return (f->size >= offsetof(pr_frame_desc, msaa) + sizeof(int32_t) && f->msaa > 1) ? f->msaa : 1;
+}
+
 int validate_frame(const Ctx* c, const pr_frame_desc* f) {
     if (!f) return fail(PR_ERR_INVALID_ARG, "frame is NULL");
-    if (f->size < sizeof(pr_frame_desc)) return fail(PR_ERR_INVALID_ARG, "frame->size %u < %zu", f->size, sizeof(pr_frame_desc));
-    if (f->width <= 0 || f->height <= 0 || f->width > 16384 || f->height > 16384)
-        return fail(PR_ERR_INVALID_ARG, "frame size %dx%d outside 1..16384", f->width, f->height);
+    if (f->size < PR_FRAME_DESC_SIZE_V1) return fail(PR_ERR_INVALID_ARG, "frame->size %u < %u", f->size, PR_FRAME_DESC_SIZE_V1);
+    if (f->size >= offsetof(pr_frame_desc, msaa) + sizeof(int32_t) && (f->msaa < 0 || f->msaa > 16))
+        return fail(PR_ERR_INVALID_ARG, "msaa %d outside 0..16", f->msaa);
+    const int64_t m = frame_msaa(f);
+    if (f->width <= 0 || f->height <= 0 || f->width * m > 16384 || f->height * m > 16384)
+        return fail(PR_ERR_INVALID_ARG, "framebuffer %lldx%lld (size %dx%d, msaa %lld) outside 1..16384",
+                    (long long)(f->width * m), (long long)(f->height * m), f->width, f->height, (long long)m);
     if (f->n_lights > (uint32_t)prk::kMaxLights) return fail(PR_ERR_UNSUPPORTED, "%u lights > %d", f->n_lights, prk::kMaxLights);
     if (f->n_ambient > (uint32_t)prk::kMaxAmbient)
         return fail(PR_ERR_UNSUPPORTED, "%u ambient lights > %d", f->n_ambient, prk::kMaxAmbient);
@@ -455,9 +465,10 @@ int frame_mats(const pr_frame_desc* f, FrameMats& m) {
     return PR_OK;
 }
 
-// The requested outputs from the staging buffers to the caller's host memory.
-int copy_host_outputs(Ctx* c, const pr_outputs* out, size_t npx, cudaStream_t st) {
-    if (out->rgba) CUDA_TRY(cudaMemcpyAsync(out->rgba, c->o_rgba.p, npx * 4, cudaMemcpyDeviceToHost, st));
+// The requested outputs from the staging buffers to the caller's host memory
+// (the image has npx_rgba pixels, the framebuffer fields npx).
+int copy_host_outputs(Ctx* c, const pr_outputs* out, size_t npx, size_t npx_rgba, cudaStream_t st) {
+    if (out->rgba) CUDA_TRY(cudaMemcpyAsync(out->rgba, c->o_rgba.p, npx_rgba * 4, cudaMemcpyDeviceToHost, st));
     if (out->tri_id) CUDA_TRY(cudaMemcpyAsync(out->tri_id, c->o_tri.p, npx * 4, cudaMemcpyDeviceToHost, st));
     if (out->depth) CUDA_TRY(cudaMemcpyAsync(out->depth, c->o_depth.p, npx * 4, cudaMemcpyDeviceToHost, st));
     if (out->nor) CUDA_TRY(cudaMemcpyAsync(out->nor, c->o_nor.p, npx * 16, cudaMemcpyDeviceToHost, st));
@@ -478,6 +489,20 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 bool submit = false) {
     int rc = validate_frame(c, f);
     if (rc) return rc;
+    // render.MSAA: every pass runs on the n-times framebuffer (the frame is
+    // rescaled here); passAntialiasing's resize to the image follows the
+    // deferred pass.
+    const int M = frame_msaa(f);
+    const size_t npx_img = (size_t)f->width * f->height;
+    const int W_img = f->width, H_img = f->height;
+    pr_frame_desc scaled;
+    if (M > 1) {
+        if (dh) return fail(PR_ERR_UNSUPPORTED, "MSAA is not available in the adjoint");
+        scaled = *f;
+        scaled.width *= M;
+        scaled.height *= M;
+        f = &scaled;
+    }
     if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
     if (out && out->size < sizeof(pr_outputs)) return fail(PR_ERR_INVALID_ARG, "outputs->size too small");
     bool out_dev = out && (out->flags & PR_OUT_DEVICE_PTRS);
@@ -562,6 +587,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 fill_scene_ptrs(c, sp);
                 sp.W = SW;
                 sp.H = SH;
+                sp.msaa = M;
                 sp.perspective = 0;
                 M4 lpv = prh::mulm(loadm(f->lights[l].shadow_proj), loadm(f->lights[l].shadow_view));
                 std::memcpy(sp.pv, lpv.m, 64);
@@ -605,6 +631,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         fill_scene_ptrs(c, mp);
         mp.W = W;
         mp.H = H;
+        mp.msaa = M;
         mp.perspective = (f->flags & PR_FRAME_PERSPECTIVE) ? 1 : 0;
         std::memcpy(mp.pv, pv.m, 64);
         mp.obj_trans = c->obj_trans.p;
@@ -713,6 +740,11 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             if (out->vcol) { if ((rc = c->o_vcol.ensure(npx * 4))) return rc; sp.gvcol = (uchar4*)c->o_vcol.p; }
             if (out->mat_id) { if ((rc = c->o_mat.ensure(npx))) return rc; sp.gmat = c->o_mat.p; }
         }
+        uchar4* rgba_img = sp.rgba;  // the image Render() returns
+        if (M > 1 && sp.rgba) {
+            if ((rc = c->o_msaa.ensure(npx * 4))) return rc;
+            sp.rgba = (uchar4*)c->o_msaa.p;  // the framebuffer's colours
+        }
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_join, 0));  // the shadow maps are complete
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_d2h, 0));   // a submitted frame's outputs left the staging
         KTRY(prk::launch_shade(sp, st));
@@ -735,6 +767,10 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             std::memcpy(ap.gamma, sp.gamma, 256);
             KTRY(prk::launch_ao(ap, st));
             launches += 1;
+            if (M > 1) {
+                KTRY(prk::launch_msaa_resize(sp.rgba, W, H, rgba_img, W_img, H_img, st));
+                launches += 1;
+            }
         }
         CUDA_TRY(cudaEventRecord(c->ev[4], st));
         CUDA_TRY(cudaMemcpyAsync(c->h_cnt, dcnt, sizeof(prk::Counters) * prk::kNumCounters, cudaMemcpyDeviceToHost, st));
@@ -744,7 +780,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
                 // host outputs leave on their own stream, beside the next frame
                 CUDA_TRY(cudaEventRecord(c->ev_frame, st));
                 CUDA_TRY(cudaStreamWaitEvent(c->stream_d, c->ev_frame, 0));
-                if ((rc = copy_host_outputs(c, out, npx, c->stream_d))) return rc;
+                if ((rc = copy_host_outputs(c, out, npx, npx_img, c->stream_d))) return rc;
                 CUDA_TRY(cudaEventRecord(c->ev_d2h, c->stream_d));
             }
             return PR_OK;
@@ -767,7 +803,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
     collect_stats(c);
 
     // ---- host outputs ----
-    if (out && !out_dev && (rc = copy_host_outputs(c, out, npx, st))) return rc;
+    if (out && !out_dev && (rc = copy_host_outputs(c, out, npx, npx_img, st))) return rc;
     if (out && out->shadow_maps) {
         size_t ns = (size_t)SW * SH * NL;
         if (!shadows || !c->smap_valid) {
@@ -885,7 +921,7 @@ int pr_destroy(void* ctx) {
     c->keys.release(); c->nanseq.release(); c->beaten.release(); c->win.release(); c->depth_ao.release();
     c->ao_list.release();
     c->smap.release(); c->lastnan.release(); c->cnt.release();
-    c->o_rgba.release(); c->o_vcol.release(); c->o_tri.release(); c->o_depth.release(); c->o_shadow.release();
+    c->o_rgba.release(); c->o_vcol.release(); c->o_msaa.release(); c->o_tri.release(); c->o_depth.release(); c->o_shadow.release();
     c->o_nor.release(); c->o_fnor.release(); c->o_wpos.release(); c->o_uvd.release(); c->o_mat.release();
     c->tri_scr.release(); c->d_kd.release(); c->d_ks.release(); c->d_shin.release(); c->d_vcol.release();
     c->d_acc.release();
@@ -1151,6 +1187,7 @@ int pr_diff_forward(void* ctx, const pr_frame_desc* frame, const pr_diff_params*
     std::lock_guard<std::mutex> lk(c->mu);
     int rc = validate_frame(c, frame);
     if (rc) return rc;
+    if (frame_msaa(frame) > 1) return fail(PR_ERR_UNSUPPORTED, "MSAA is not available in the adjoint");
     if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
     if ((rc = set_device(c))) return rc;
     // the AO factors need the colour pass: render into ctx storage when the caller wants no image
@@ -1196,6 +1233,7 @@ int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params
     std::lock_guard<std::mutex> lk(c->mu);
     int rc = validate_frame(c, frame);
     if (rc) return rc;
+    if (frame_msaa(frame) > 1) return fail(PR_ERR_UNSUPPORTED, "MSAA is not available in the adjoint");
     if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
     if ((rc = set_device(c))) return rc;
     prk::DiffParamsK K{};
@@ -1618,6 +1656,8 @@ int batch_run(Batch* b, uint32_t nv, const pr_batch_view* views) {
         const pr_outputs* o = bv.out;
         if (!o || o->size < sizeof(pr_outputs) || !(o->flags & PR_OUT_DEVICE_PTRS) || !o->rgba)
             return fail(PR_ERR_INVALID_ARG, "view %u: outputs must be device pointers with rgba set", v);
+        if (views[v].frame && views[v].frame->size >= PR_FRAME_DESC_SIZE_V1 && frame_msaa(views[v].frame) > 1)
+            return fail(PR_ERR_UNSUPPORTED, "view %u: MSAA is not available in batches", v);
         if (o->shadow_maps) return fail(PR_ERR_UNSUPPORTED, "view %u: shadow_maps output is not batched", v);
     }
     CUDA_TRY(cudaSetDevice(b->device));

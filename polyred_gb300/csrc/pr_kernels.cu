@@ -80,6 +80,13 @@ PR_DEV bool box_contains(const Box& a, V4 v) {
 
 // Pixel rectangle of drawClipped / drawDepth (render/raster.go:473-477),
 // clamped to the W x H buffer. Returns false when empty.
+// The viewport box and clip extent of a pass: float32(MSAA * size), the
+// reference's MSAA*buf.Bounds().Dx() with the buffer already n times the
+// image (render/raster.go:414-441, render/cull.go:15-23). Pixel boxes stay
+// clamped to the target (buf.In).
+PR_DEV float ext_w(const SetupParams& P) { return (float)(P.msaa > 1 ? P.W * P.msaa : P.W); }
+PR_DEV float ext_h(const SetupParams& P) { return (float)(P.msaa > 1 ? P.H * P.msaa : P.H); }
+
 PR_DEV bool pixel_box(V4 a, V4 b, V4 c, int W, int H, uint32_t* bx, uint32_t* by, uint32_t* area) {
     Box r = box3(a, b, c);
     long long xmin = go_f2i(__fsub_rn(pround(r.mnx), 1.0f));
@@ -411,7 +418,7 @@ PR_DEV bool transform_main_geom(const SetupParams& P, const ObjCache* C, uint32_
     if (cross_z(__fsub_rn(v[1].pos.x, v[0].pos.x), __fsub_rn(v[1].pos.y, v[0].pos.y), __fsub_rn(v[2].pos.x, v[0].pos.x),
                 __fsub_rn(v[2].pos.y, v[0].pos.y)) < 0.0f)
         return false;
-    const Box vp = {0.0f, 0.0f, -1.0f, (float)P.W, (float)P.H, 1.0f};
+    const Box vp = {0.0f, 0.0f, -1.0f, ext_w(P), ext_h(P), 1.0f};
     if (!box_intersect(vp, box3(v[0].pos, v[1].pos, v[2].pos))) return false;
     *contained = box_contains(vp, v[0].pos) && box_contains(vp, v[1].pos) && box_contains(vp, v[2].pos);
     *obj = o;
@@ -499,7 +506,7 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
         t = clip_list[j];
         transform_main(P, nullptr, t, v, recipw, &matid, &contained);
         V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
-        nc = sutherland_hodgman(in3, (float)P.W, (float)P.H, clips);
+        nc = sutherland_hodgman(in3, ext_w(P), ext_h(P), clips);
         if (nc < 0) {
             atomicOr(&P.cnt->overflow, 4u);
             nc = 0;
@@ -561,7 +568,7 @@ PR_DEV void setup_shadow_one(const SetupParams& P, const ObjCache* C, uint32_t t
                            __fsub_rn(v[2].pos.x, v[0].pos.x), __fsub_rn(v[2].pos.y, v[0].pos.y)) < 0.0f);
             // cullViewFrustum (render/cull.go:15-23): NewAABB((W,H,1),(0,0,0),(0,0,-1))
             if (ok) {
-                const Box vp = box3(V4{(float)P.W, (float)P.H, 1.0f, 1.0f}, V4{0, 0, 0, 1}, V4{0, 0, -1.0f, 1});
+                const Box vp = box3(V4{ext_w(P), ext_h(P), 1.0f, 1.0f}, V4{0, 0, 0, 1}, V4{0, 0, -1.0f, 1});
                 ok = box_intersect(vp, box3(v[0].pos, v[1].pos, v[2].pos));
             }
         }
@@ -1926,6 +1933,77 @@ int launch_ao_batch(const AoParams* views, int n_views, uint32_t* chunk_ctr, int
     ao_batch_kernel<<<n_blocks, kAoThreads, 0, (cudaStream_t)stream>>>(views, n_views, chunk_ctr);
     return check(cudaGetLastError());
 }
+// ---------------------------------------------------------------- MSAA resize
+
+constexpr int kMaxMsaa = 16;
+
+// createWeights8 (internal/imageutil/resize.go:161-181) for output index y:
+// the linear kernel's taps as int16 (x256, truncated) and the first input
+// index, in the reference's float32 order. len <= 2 * kMaxMsaa.
+PR_DEV int resize_taps(int y, float scale, float factor, int len, int16_t* coeff) {
+    float interp = __fsub_rn(__fmul_rn(scale, __fadd_rn((float)y, 0.5f)), 0.5f);
+    const int start = (int)interp - len / 2 + 1;  // int(interpX) truncates
+    interp = __fsub_rn(interp, (float)start);
+    for (int i = 0; i < len; i++) {
+        const float in = fabsf(__fmul_rn(__fsub_rn(interp, (float)i), factor));
+        const float k = in <= 1.0f ? __fsub_rn(1.0f, in) : 0.0f;  // linear()
+        coeff[i] = (int16_t)(int)__fmul_rn(k, 256.0f);
+    }
+    return start;
+}
+
+// resizeRGBA's edge rule (resize.go:98-105): inside [0, max) as is, at or
+// past max -> max, negative -> 0.
+PR_DEV int resize_clamp(int i, int max) { return (unsigned)i < (unsigned)max ? i : (i >= max ? max : 0); }
+
+PR_DEV uint8_t resize_div(int32_t acc, int32_t sum) {
+    const int32_t v = sum != 0 ? acc / sum : 0;
+    return (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+}
+
+// imageutil.Resize's two passes for one output pixel: the horizontal pass
+// (into the reference's transposed uint8 temporary) for every input row the
+// vertical taps reach, then the vertical pass over those values.
+__global__ void msaa_resize_kernel(const uchar4* __restrict__ in, int in_w, int in_h, uchar4* __restrict__ out, int w,
+                                   int h) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    // calcFactors, then createWeights8's filterLength and filterFactor
+    const float sx = __fdiv_rn((float)in_w, (float)w), sy = __fdiv_rn((float)in_h, (float)h);
+    const int lx = min(2 * max((int)ceilf(sx), 1), 2 * kMaxMsaa), ly = min(2 * max((int)ceilf(sy), 1), 2 * kMaxMsaa);
+    const float fx = fminf(__fdiv_rn(1.0f, sx), 1.0f), fy = fminf(__fdiv_rn(1.0f, sy), 1.0f);
+    int16_t cx[2 * kMaxMsaa], cy[2 * kMaxMsaa];
+    const int x0 = resize_taps(x, sx, fx, lx, cx);
+    const int y0 = resize_taps(y, sy, fy, ly, cy);
+    int32_t acc[4] = {0, 0, 0, 0}, sum_y = 0;
+    for (int j = 0; j < ly; j++) {
+        if (cy[j] == 0) continue;
+        const uchar4* row = in + (size_t)resize_clamp(y0 + j, in_h - 1) * in_w;
+        int32_t t[4] = {0, 0, 0, 0}, sum_x = 0;
+        for (int i = 0; i < lx; i++) {
+            if (cx[i] == 0) continue;
+            const uchar4 p = row[resize_clamp(x0 + i, in_w - 1)];
+            t[0] += cx[i] * (int32_t)p.x;
+            t[1] += cx[i] * (int32_t)p.y;
+            t[2] += cx[i] * (int32_t)p.z;
+            t[3] += cx[i] * (int32_t)p.w;
+            sum_x += cx[i];
+        }
+        for (int k = 0; k < 4; k++) acc[k] += cy[j] * (int32_t)resize_div(t[k], sum_x);
+        sum_y += cy[j];
+    }
+    out[(size_t)y * w + x] = make_uchar4(resize_div(acc[0], sum_y), resize_div(acc[1], sum_y), resize_div(acc[2], sum_y),
+                                         resize_div(acc[3], sum_y));
+}
+
+int launch_msaa_resize(const uchar4* in, int in_w, int in_h, uchar4* out, int w, int h, void* stream) {
+    if (w <= 0 || h <= 0 || in_w < w || in_h < h || in_w > w * kMaxMsaa || in_h > h * kMaxMsaa) return -1;
+    const dim3 block(32, 8), grid((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8));
+    msaa_resize_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(in, in_w, in_h, out, w, h);
+    return check(cudaGetLastError());
+}
+
 int launch_ao(const AoParams& p, void* stream) {
     // One pixel per thread for the largest possible list (every pixel): the
     // block scheduler balances the uneven per-pixel work; blocks past the

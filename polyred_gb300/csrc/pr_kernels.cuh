@@ -88,6 +88,7 @@ struct SetupParams {
     const int32_t* obj_matbase;  // [n_objects]
     uint32_t n_tris, n_objects;
     int W, H;                    // target size (framebuffer or shadow map)
+    int msaa;                    // render.MSAA: the viewport test and clipping use msaa x (W, H); 0 or 1: (W, H)
     int perspective;
     float pv[16];                // Proj.MulM(View)
     float viewport[16];
@@ -238,6 +239,9 @@ int launch_nan_cleanup(size_t n, uint32_t* a, uint32_t va, uint32_t* b, uint32_t
                        void* stream);
 int launch_shade(const ShadeParams& p, void* stream);
 int launch_ao(const AoParams& p, void* stream);
+// passAntialiasing's imageutil.Resize of the n*W x n*H image `in` to W x H
+// (rows top-down, both buffers on the device).
+int launch_msaa_resize(const uchar4* in, int in_w, int in_h, uchar4* out, int w, int h, void* stream);
 int launch_diff(const DiffParamsK& p, bool backward, void* stream);
 
 // ---- batches: many passes (views, shadow maps) per launch ----

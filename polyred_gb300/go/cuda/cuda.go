@@ -113,6 +113,11 @@ type FrameDesc struct {
 	Ambient      *float32
 	ShadowWidth  int32
 	ShadowHeight int32
+	// MSAA is render.MSAA (0 or 1: none). With n > 1 the frame renders at
+	// n*Width x n*Height and Outputs.RGBA receives the Width x Height image
+	// after imageutil.Resize; the other outputs are framebuffer-sized.
+	MSAA     int32
+	Reserved int32
 }
 
 // Outputs mirrors pr_outputs; nil fields are not produced.

@@ -206,6 +206,7 @@ class FrameDesc:
                    | (_abi.PR_FRAME_GAMMA if opts["gamma"] else 0))
         f.width = opts["width"]
         f.height = opts["height"]
+        f.msaa = int(opts.get("msaa", 1))
         v, p = cam.view_matrix(), cam.proj_matrix()
         for i in range(16):
             f.view[i] = float(v[i])
@@ -266,7 +267,9 @@ class Outputs:
               "face_nor": (4, F32), "world_pos": (4, F32), "uvd": (4, F32), "vcol": (4, np.uint8),
               "mat_id": (1, np.int32)}
 
-    def __init__(self, width, height, want=("rgba",), n_shadow=0, shadow_size=None, pinned=False):
+    def __init__(self, width, height, want=("rgba",), n_shadow=0, shadow_size=None, pinned=False, msaa=1):
+        """rgba is (height, width, 4); with msaa > 1 every other field has
+        the framebuffer's msaa*height x msaa*width pixels."""
         self.arrays = {}
         o = _abi.pr_outputs()
         o.size = C.sizeof(_abi.pr_outputs)
@@ -278,7 +281,8 @@ class Outputs:
                 a = alloc((max(n_shadow, 1), sh, sw), F32)
             else:
                 k, dt = self.FIELDS[name]
-                a = alloc((height, width, k) if k > 1 else (height, width), dt)
+                h, w = (height, width) if name == "rgba" else (height * msaa, width * msaa)
+                a = alloc((h, w, k) if k > 1 else (h, w), dt)
             self.arrays[name] = a
             setattr(o, name, a.ctypes.data)
         self.desc = o
@@ -304,8 +308,8 @@ class Renderer:
     def _apply(self, opts):
         for o in opts:
             o.fn(self._opts)
-        if self._opts["msaa"] != 1:
-            raise native.RenderError(_abi.PR_ERR_UNSUPPORTED, "MSAA != 1 is not supported on the CUDA path")
+        if not 1 <= self._opts["msaa"] <= 16:
+            raise native.RenderError(_abi.PR_ERR_INVALID_ARG, f"MSAA {self._opts['msaa']} outside 1..16")
         dev = self._opts["device"]
         if dev is None:
             if self._own_device is None:
@@ -363,8 +367,9 @@ class Renderer:
             self._init_shadow_maps()
         fd = FrameDesc(o, getattr(self, "_shadow_cams", {}))
         src, _ = o["scene"].lights()
-        sw, sh = o["shadow_size"] or (o["width"], o["height"])
-        out = Outputs(o["width"], o["height"], o["outputs"], n_shadow=len(src), shadow_size=(sw, sh))
+        m = o["msaa"]
+        sw, sh = o["shadow_size"] or (o["width"] * m, o["height"] * m)
+        out = Outputs(o["width"], o["height"], o["outputs"], n_shadow=len(src), shadow_size=(sw, sh), msaa=m)
         native.check(self._lib.pr_render(self.device.handle, C.byref(fd.desc), C.byref(out.desc)))
         st = _abi.pr_stats()
         st.size = C.sizeof(_abi.pr_stats)

@@ -12,10 +12,10 @@ THREADS = max(1, min(16, os.cpu_count() or 1))
 
 
 def options(scene, cam, W, H, shadow_map=False, gamma=True, background=(0, 0, 0, 0), shadow_size=None,
-            directional_shadows=False):
+            directional_shadows=False, msaa=1):
     return dict(width=W, height=H, camera=cam, scene=scene, perspective=isinstance(cam, sc.Perspective),
                 shadow_map=shadow_map, gamma=gamma, background=tuple(background), shadow_size=shadow_size,
-                directional_shadows=directional_shadows)
+                directional_shadows=directional_shadows, msaa=msaa)
 
 
 def shadow_cams(opts):
@@ -50,7 +50,8 @@ class Pair:
         native.check(lib.pr_shadow_reset(device.handle))
         src, _ = opts["scene"].lights()
         self.n_lights = len(src)
-        sw, sh = opts["shadow_size"] or (opts["width"], opts["height"])
+        self.msaa = opts.get("msaa", 1)
+        sw, sh = opts["shadow_size"] or (opts["width"] * self.msaa, opts["height"] * self.msaa)
         self.sshape = (max(self.n_lights, 1), sh, sw)
         self.shadow_state = np.zeros(self.sshape, np.float32)
         self.stats = None
@@ -61,14 +62,14 @@ class Pair:
         want = self.outputs + (("shadow_maps",) if with_shadow_maps else ())
         W, H = self.opts["width"], self.opts["height"]
         sw, sh = self.sshape[2], self.sshape[1]
-        gpu = render.Outputs(W, H, want, n_shadow=self.n_lights, shadow_size=(sw, sh))
+        gpu = render.Outputs(W, H, want, n_shadow=self.n_lights, shadow_size=(sw, sh), msaa=self.msaa)
         lib = native.load()
         native.check(lib.pr_render(self.device.handle, C.byref(fd.desc), C.byref(gpu.desc)))
         st = _abi.pr_stats()
         st.size = C.sizeof(_abi.pr_stats)
         native.check(lib.pr_frame_stats(self.device.handle, C.byref(st)))
         self.stats = {k: getattr(st, k) for k, _ in _abi.pr_stats._fields_}
-        cpu = render.Outputs(W, H, want, n_shadow=self.n_lights, shadow_size=(sw, sh))
+        cpu = render.Outputs(W, H, want, n_shadow=self.n_lights, shadow_size=(sw, sh), msaa=self.msaa)
         oracle.render(self.flat.desc(), fd.desc, cpu.desc, shadow_state=self.shadow_state, threads=self.threads)
         return gpu.arrays, cpu.arrays
 
