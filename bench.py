@@ -389,6 +389,60 @@ def measure_obj(steps=20, n_tori=32, nu=128, nv=64, width=1920, height=1080):
                              "sample": "obj.go restated in pure Python, first 1 MB of the same OBJ text"}}
 
 
+def _resident_frames(s, cam, width, height, steps, msaa=1, shadow_size=SHADOW):
+    """ms per resident frame of scene s (CUDA events on the context's stream)."""
+    import torch
+    from polyred_gb300 import _abi, native, render
+    dev = render.Device(0)
+    lib = native.load()
+    flat = render.FlatScene(s)
+    desc = flat.desc()
+    native.check(lib.pr_scene_upload(dev.handle, C.byref(desc)))
+    opts = dict(width=width, height=height, camera=cam, scene=s, perspective=True, shadow_map=True, gamma=True,
+                background=(0, 0, 0, 0), shadow_size=shadow_size, directional_shadows=True, msaa=msaa)
+    fd = render.FrameDesc(opts, shadow_cams(opts))
+    rgba = torch.empty((height, width, 4), dtype=torch.uint8, device="cuda")
+    od = _abi.pr_outputs()
+    od.size = C.sizeof(_abi.pr_outputs)
+    od.flags = _abi.PR_OUT_DEVICE_PTRS
+    od.rgba = rgba.data_ptr()
+    for _ in range(3):
+        native.check(lib.pr_render(dev.handle, C.byref(fd.desc), C.byref(od)))
+    stream = torch.cuda.ExternalStream(dev.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        native.check(lib.pr_render_async(dev.handle, C.byref(fd.desc), C.byref(od)))
+    e1.record(stream)
+    native.check(lib.pr_sync(dev.handle))
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    dev.close()
+    return ms
+
+
+def measure_msaa(steps=20):
+    """render.MSAA(2) on the workload: the 999,936-triangle sphere field into
+    a 3840x2160 framebuffer (viewport test and clipping at 7680x4320, shadow
+    maps 2048^2), resized to the 1920x1080 image."""
+    s, cam = workload()
+    ms = _resident_frames(s, cam, W, H, steps, msaa=2)
+    return {"workload": "sphere field, 1920x1080 image, MSAA 2 (3840x2160 framebuffer)", "n_tris": N_TRIS,
+            "ms_per_frame": ms, "value": N_TRIS / (ms / 1e3) / 1e6, "unit": "Mtri/s"}
+
+
+def measure_textured(steps=50, width=1920, height=1080):
+    """Image textures: procedural.textured_scene at 1920x1080 (a mipmapped
+    256^2 texture, a 37x300 mipmapped texture, a 64x16 texture without
+    mipmaps; 6,146 triangles; one shadow-casting light with a framebuffer-size
+    map), resident frames."""
+    from polyred_gb300 import procedural
+    s, cam = procedural.textured_scene(width, height)
+    ms = _resident_frames(s, cam, width, height, steps, shadow_size=None)
+    return {"workload": "textured spheres and ground, 1920x1080", "ms_per_frame": ms, "frames_per_s": 1e3 / ms}
+
+
 def measure_batch(reps=3):
     """The batched workload (32 sphere scenes of 1k-500k triangles, 8 ring
     views each at 1280x720, 16 casting point lights per scene with 1024^2
@@ -485,6 +539,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-views measurement")
     ap.add_argument("--no-soup", action="store_true", help="skip the 10M-triangle 4K soup measurement")
     ap.add_argument("--no-obj", action="store_true", help="skip the OBJ ingestion measurement")
+    ap.add_argument("--no-msaa", action="store_true", help="skip the MSAA and image-texture measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -626,6 +681,12 @@ def main():
             line["soup_4k"] = measure_soup()
         if not args.no_batch:
             line["batched"] = measure_batch()
+        if not args.no_msaa:
+            try:
+                line["msaa_2x"] = measure_msaa()
+                line["textured_1080p"] = measure_textured()
+            except Exception as e:  # the headline line must still print
+                line["msaa_2x"] = {"error": f"{type(e).__name__}: {e}"}
         if not args.no_obj:
             try:
                 line["obj_ingest"] = measure_obj()

@@ -98,11 +98,20 @@ typedef struct pr_object {
 typedef struct pr_material {
     uint8_t  diffuse[4];
     uint8_t  specular[4];
-    uint8_t  texture[4];    /* the texel of the 1x1 texture */
+    uint8_t  texture[4];    /* the texel of a uniform (1x1) texture */
     float    shininess;
     uint32_t flags;         /* PR_MAT_* */
-    int32_t  texture_size;  /* Texture.Size(); only 1 is supported */
+    int32_t  texture_size;  /* Texture.Size(): 1 for a uniform texture; ignored
+                               when pr_scene_desc.textures gives an image */
 } pr_material;
+
+/* An image texture, buffer.NewTexture(TextureImage(img)) (buffer/texture.go:
+ * 35-67): the library builds its mipmap (each level imageutil.Resize of the
+ * image) when the material has PR_MAT_MIPMAP. Host memory. */
+typedef struct pr_texture {
+    int32_t width, height;   /* 1..16384 */
+    const uint8_t* rgba;     /* [height][width][4] image.RGBA pixels, rows top-down; NULL: no image */
+} pr_texture;
 
 /* The triangle soup: per triangle three vertices (primitive.Vertex,
  * geometry/primitive/vertex.go:14-20). Arrays are host pointers unless
@@ -121,7 +130,14 @@ typedef struct pr_scene_desc {
     const int32_t* mat_id;   /* [n_tris] Triangle.MaterialID, geometry-local; <0 = vertex colour */
     const pr_object*   objects;    /* [n_objects] (host memory) */
     const pr_material* materials;  /* [n_materials] flat table (host memory) */
+    /* [n_materials] or NULL (host memory): the image texture of each
+     * material, sampled by Texture.Query (buffer/texture.go:83-187) at the
+     * FragmentShader's level of detail (shader/blinn_cpu.go:28-35); entries
+     * with rgba NULL keep the material's uniform texel. Not available in
+     * batches and the adjoint (PR_ERR_UNSUPPORTED). */
+    const pr_texture*  textures;
 } pr_scene_desc;
+#define PR_SCENE_DESC_SIZE_V1 80u  /* pr_scene_desc up to materials */
 
 /* ---- frame ------------------------------------------------------------ */
 

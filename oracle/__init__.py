@@ -26,6 +26,10 @@ def load():
         build()
         from polyred_gb300 import _abi
         lib = C.CDLL(LIB)
+        lib.orc_texture_build.restype = C.c_longlong
+        lib.orc_texture_build.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]
+        lib.orc_texture_query.restype = C.c_int
+        lib.orc_texture_query.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 6
         lib.orc_resize.restype = C.c_int
         lib.orc_resize.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         lib.orc_render.restype = C.c_int

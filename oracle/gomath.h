@@ -76,6 +76,44 @@ inline uint8_t go_f2u8(float x) {
     return (uint8_t)((uint32_t)(int32_t)x & 0xffu);
 }
 
+// Go math.Log (math/log.go): the fdlibm e_log.c reduction x = 2^k (1 + f),
+// s = f / (2 + f), R(s) polynomial, log = k ln2_hi - ((hfsq - (s (hfsq + R)
+// + k ln2_lo)) - f).
+inline double go_log(double x) {
+    static const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+    static const double lg[7] = {6.666666666666735130e-01, 3.999999999940941908e-01, 2.857142874366239149e-01,
+                                 2.222219843214978396e-01, 1.818357216161805012e-01, 1.531383769920937332e-01,
+                                 1.479819860511658591e-01};
+    if (std::isnan(x) || (std::isinf(x) && x > 0)) return x;
+    if (x < 0) return NAN;
+    if (x == 0) return -INFINITY;
+    int k;
+    double f1 = std::frexp(x, &k);
+    if (f1 < 0.70710678118654752440) {
+        f1 = f1 * 2;
+        k = k - 1;
+    }
+    double f = f1 - 1;
+    double s = f / (2 + f);
+    double z = s * s;
+    double w = z * z;
+    double odd = z * (lg[0] + w * (lg[2] + w * (lg[4] + w * lg[6])));
+    double even = w * (lg[1] + w * (lg[3] + w * lg[5]));
+    double r = odd + even;
+    double hfsq = 0.5 * f * f;
+    double dk = (double)k;
+    return dk * ln2_hi - ((hfsq - (s * (hfsq + r) + dk * ln2_lo)) - f);
+}
+
+// Go math.Log2 (math/log10.go): powers of two exactly, else Log(frac)/Ln2 + exp.
+inline double go_log2(double x) {
+    int e;
+    double frac = std::frexp(x, &e);
+    if (std::isfinite(x) && x > 0 && frac == 0.5) return (double)(e - 1);
+    if (!std::isfinite(x) || x <= 0) return go_log(x);
+    return go_log(frac) * 1.44269504088896340736 + (double)e;  // 1/Ln2 folded exactly, then rounded
+}
+
 // Go math.Frexp: frac in [0.5, 1), x = frac * 2^exp (Go math/frexp.go).
 inline double go_frexp(double x, int* e) {
     *e = 0;

@@ -26,6 +26,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <thread>
 #include <vector>
 
@@ -101,9 +102,12 @@ const SRGB& srgb() {
     return s;
 }
 
+struct OTex;
+
 struct Ctx {
     const pr_scene_desc* sc;
     const pr_frame_desc* fr;
+    const std::vector<const OTex*>* mat_tex = nullptr;  // image texture of each material, or null
     int W, H, SW, SH;
     int M;  // render.MSAA: W, H are already M times the image
     bool perspect;
@@ -431,12 +435,255 @@ bool shading_visibility(const Ctx& c, const ShadeUniforms& u, int li, const Frag
     return shadow > 0;
 }
 
+// ---- textures: buffer.NewTexture and Texture.Query (buffer/texture.go:35-187)
+
+// ---- passAntialiasing: imageutil.Resize (internal/imageutil/resize.go:16-181)
+
+float resize_linear(float in) {
+    in = std::fabs(in);
+    if (in <= 1) return 1 - in;
+    return 0;
+}
+
+// createWeights8 with the linear kernel: int16 taps (x256) and start indices
+void create_weights8(int dy, int filter_length, float scale, std::vector<int16_t>& coeffs, std::vector<int>& start,
+                     int& len) {
+    len = filter_length * (int)std::max(std::ceil(scale), 1.0f);
+    float factor = std::min(1.0f / scale, 1.0f);
+    coeffs.assign((size_t)dy * len, 0);
+    start.assign(dy, 0);
+    for (int y = 0; y < dy; y++) {
+        float interp = scale * ((float)y + 0.5f) - 0.5f;
+        start[y] = (int)interp - len / 2 + 1;
+        interp -= (float)start[y];
+        for (int i = 0; i < len; i++) {
+            float in = (interp - (float)i) * factor;
+            coeffs[(size_t)y * len + i] = (int16_t)(resize_linear(in) * 256);
+        }
+    }
+}
+
+// resizeRGBA: `in` has in_dx pixels per row; writes out (out_dx x out_dy),
+// out row y column x from in row x (the passes transpose).
+void resize_rgba(const uint8_t* in, int in_dx, uint8_t* out, int out_dx, int out_dy,
+                 const std::vector<int16_t>& coeffs, const std::vector<int>& start, int len) {
+    const int maxX = in_dx - 1;
+    for (int x = 0; x < out_dx; x++) {
+        const uint8_t* row = in + (size_t)x * in_dx * 4;
+        for (int y = 0; y < out_dy; y++) {
+            int32_t rgba[4] = {0, 0, 0, 0}, sum = 0;
+            for (int i = 0; i < len; i++) {
+                int32_t coeff = coeffs[(size_t)y * len + i];
+                if (coeff == 0) continue;
+                int xi = start[y] + i;
+                if ((unsigned)xi < (unsigned)maxX)
+                    xi *= 4;
+                else if (xi >= maxX)
+                    xi = 4 * maxX;
+                else
+                    xi = 0;
+                for (int k = 0; k < 4; k++) rgba[k] += coeff * (int32_t)row[xi + k];
+                sum += coeff;
+            }
+            for (int k = 0; k < 4; k++) {
+                int v = rgba[k] / sum;
+                out[((size_t)y * out_dx + x) * 4 + k] = (uint8_t)std::min(std::max(v, 0), 255);
+            }
+        }
+    }
+}
+
+void resize_image(const uint8_t* img, int dx, int dy, int width, int height, uint8_t* out) {
+    float scale_x = (float)dx / (float)width, scale_y = (float)dy / (float)height;
+    std::vector<int16_t> coeffs;
+    std::vector<int> start;
+    int len;
+    std::vector<uint8_t> temp((size_t)dy * width * 4);  // Dx = dy, Dy = width (transposed)
+    create_weights8(width, 2, scale_x, coeffs, start, len);
+    resize_rgba(img, dx, temp.data(), dy, width, coeffs, start, len);
+    create_weights8(height, 2, scale_y, coeffs, start, len);
+    resize_rgba(temp.data(), dy, out, width, height, coeffs, start, len);
+}
+
+
+struct OImg {  // image.RGBA: rows top-down
+    int w = 0, h = 0;
+    std::vector<uint8_t> pix;
+};
+
+struct OTex {
+    bool use_mipmap = true;
+    std::vector<OImg> mipmap;
+};
+
+// imageutil.Resize(width, height, img) (internal/imageutil/resize.go:16-66)
+OImg go_resize_img(int width, int height, const OImg& img) {
+    float scale_x, scale_y;  // calcFactors (resize.go:124-144)
+    const float old_w = (float)img.w, old_h = (float)img.h;
+    if (width == 0) {
+        if (height == 0) {
+            scale_x = 1.0f;
+            scale_y = 1.0f;
+        } else {
+            scale_y = old_h / (float)height;
+            scale_x = scale_y;
+        }
+    } else {
+        scale_x = old_w / (float)width;
+        if (height == 0)
+            scale_y = scale_x;
+        else
+            scale_y = old_h / (float)height;
+    }
+    if (width == 0) width = (int)(0.7f + old_w / scale_x);
+    if (height == 0) height = (int)(0.7f + old_h / scale_y);
+    if (width == img.w && height == img.h) return img;
+    if (img.w <= 0 || img.h <= 0) return img;
+    std::vector<uint8_t> temp((size_t)img.h * width * 4);  // image.NewRGBA(Rect(0, 0, Dy, width))
+    OImg out;
+    out.w = width;
+    out.h = height;
+    out.pix.assign((size_t)width * height * 4, 0);
+    std::vector<int16_t> coeffs;
+    std::vector<int> start;
+    int len;
+    create_weights8(width, 2, scale_x, coeffs, start, len);
+    resize_rgba(img.pix.data(), img.w, temp.data(), img.h, width, coeffs, start, len);
+    create_weights8(height, 2, scale_y, coeffs, start, len);
+    resize_rgba(temp.data(), img.h, out.pix.data(), width, height, coeffs, start, len);
+    return out;
+}
+
+// NewTexture (buffer/texture.go:35-67): every level a Resize of the image
+OTex new_texture(const OImg& image, bool use_mipmap) {
+    OTex t;
+    t.use_mipmap = use_mipmap;
+    const int dx = image.w, dy = image.h;
+    if (dx == 1 && dy == 1) {
+        t.mipmap.push_back(image);
+        return t;
+    }
+    const int L = (int)(float)gomath::go_log2((double)gomath::pmax((float)dx, (float)dy)) + 1;
+    t.mipmap.resize(L);
+    t.mipmap[0] = image;
+    for (int i = 1; i < L; i++) {
+        const int p = (int)(float)std::pow(2.0, (double)(float)i);
+        t.mipmap[i] = go_resize_img(dx / p, dy / p, image);
+    }
+    return t;
+}
+
+typedef std::array<uint8_t, 4> RGBA;
+
+RGBA rgba_at(const OImg& b, int64_t x, int64_t y) {  // image.RGBA.RGBAAt
+    if (x < 0 || y < 0 || x >= b.w || y >= b.h) return RGBA{0, 0, 0, 0};
+    const uint8_t* p = &b.pix[((size_t)y * b.w + (size_t)x) * 4];
+    return RGBA{p[0], p[1], p[2], p[3]};
+}
+
+RGBA lerp_c(RGBA from, RGBA to, float t) {  // math.LerpC (math/interpolate.go:55-62)
+    RGBA r;
+    for (int k = 0; k < 4; k++) r[k] = go_f2u8((float)from[k] + t * ((float)to[k] - (float)from[k]));
+    return r;
+}
+
+float go_floor32(float x) { return (float)std::floor((double)x); }
+
+RGBA query_l0(const OTex& t, float u, float v) {
+    const OImg& tex = t.mipmap[0];
+    const float dx = (float)tex.w, dy = (float)tex.h;
+    if (dx == 1 && dy == 1) return rgba_at(tex, 0, 0);
+    const int64_t x = go_f2i(go_floor32(u * (dx - 1)));
+    const int64_t y = go_f2i(go_floor32(v * (dy - 1)));
+    return rgba_at(tex, x, y);
+}
+
+RGBA query_bilinear(const OTex& t, int lod, float u, float v) {
+    const OImg& buf = t.mipmap[lod];
+    const int dx = buf.w, dy = buf.h;
+    if (dx == 1 && dy == 1) return rgba_at(buf, 0, 0);
+    const float x = u * ((float)dx - 1);
+    const float y = v * ((float)dy - 1);
+    const float x0 = go_floor32(x), y0 = go_floor32(y);
+    const int64_t i = go_f2i(x0), j = go_f2i(y0);
+    RGBA p1 = rgba_at(buf, i, j), p2, p3, p4;
+    if (i < dx - 1)
+        p2 = rgba_at(buf, i + 1, j);
+    else
+        p2 = rgba_at(buf, i, j);
+    RGBA interpo1 = lerp_c(p1, p2, x - x0);
+    if (j < dy - 1)
+        p3 = rgba_at(buf, i, j + 1);
+    else
+        p3 = rgba_at(buf, i, j);
+    if (i < dx - 1 && j < dy - 1)
+        p4 = rgba_at(buf, i + 1, j + 1);
+    else
+        p4 = rgba_at(buf, i, j);
+    RGBA interpo2 = lerp_c(p3, p4, x - x0);
+    return lerp_c(interpo1, interpo2, y - y0);
+}
+
+// math.Modf on float32 through float64; Modf(+-Inf) = +-Inf, NaN
+float go_modf32(float f, float* ip) {
+    if (std::isinf(f)) {
+        *ip = f;
+        return NAN;
+    }
+    double i;
+    const double fr = std::modf((double)f, &i);
+    *ip = (float)i;
+    return (float)fr;
+}
+
+// Texture.Query (buffer/texture.go:83-129); where the reference indexes
+// the mipmap out of range (NaN lod), transparent black.
+RGBA texture_query(const OTex& t, float lod, float u, float v) {
+    float iu, iv;
+    u = go_modf32(u, &iu);
+    if (iu != 0 && u == 0) u = 1;
+    if (u < 0) u = 1 - u;
+    v = go_modf32(v, &iv);
+    if (iv != 0 && v == 0) v = 1;
+    if (v < 0) v = 1 - v;
+    if (!t.use_mipmap) return query_l0(t, u, v);
+    const int n = (int)t.mipmap.size();
+    if (lod < 0)
+        lod = 0;
+    else if (lod >= (float)n)
+        lod = (float)(n - 1);
+    if (lod <= 1) return query_bilinear(t, 0, u, v);
+    lod -= 1;
+    const int64_t h = go_f2i(go_floor32(lod));
+    const int64_t l = h + 1;
+    if (h < 0 || h >= n) return RGBA{0, 0, 0, 0};
+    if (l >= n) return query_bilinear(t, (int)h, u, v);
+    const float p = lod - (float)h;
+    if ((float)std::fabs((double)(p - 0)) <= 1e-7f) return query_bilinear(t, (int)h, u, v);
+    return lerp_c(query_bilinear(t, (int)h, u, v), query_bilinear(t, (int)l, u, v), p);
+}
+
+// FragmentShader's lod and query (shader/blinn_cpu.go:28-36)
+RGBA texture_colour(const OTex& t, float du, float dv, float u, float v) {
+    float lod = 0;
+    if (t.use_mipmap) {
+        float siz = (float)t.mipmap[0].w * (float)std::sqrt((double)gomath::pmax(du, dv));
+        if (siz < 1) siz = 1;
+        lod = (float)gomath::go_log2((double)siz);
+    }
+    return texture_query(t, lod, u, 1 - v);
+}
+
 // FragmentShader (shader/blinn_cpu.go:24-106)
 void fragment_shader(const pr_material& m, const Frag& info, V3 cam, const pr_light* ls, int nl,
-                     const float* amb, int na, uint8_t out[4]) {
+                     const float* amb, int na, uint8_t out[4], const OTex* tex = nullptr) {
     // Uniform textures: Query returns the single texel whatever lod/u/v
     // (buffer/texture.go:83-129, queryBilinear 1x1 path :150-156).
     uint8_t col[4] = {m.texture[0], m.texture[1], m.texture[2], m.texture[3]};
+    if (tex) {
+        const RGBA c = texture_colour(*tex, info.du, info.dv, info.u, info.v);
+        std::memcpy(col, c.data(), 4);
+    }
     if (nl == 0) {
         std::memcpy(out, col, 4);
         return;
@@ -535,7 +782,9 @@ void shade_pixel(const Ctx& c, const ShadeUniforms& u, const std::vector<float>&
     std::memcpy(col, info.col, 4);
     if (mat) {
         V3 cam = {c.fr->cam_pos[0], c.fr->cam_pos[1], c.fr->cam_pos[2]};
-        fragment_shader(*mat, info, cam, c.fr->lights, (int)c.fr->n_lights, c.fr->ambient, (int)c.fr->n_ambient, col);
+        const OTex* tex = c.mat_tex ? (*c.mat_tex)[info.matid] : nullptr;
+        fragment_shader(*mat, info, cam, c.fr->lights, (int)c.fr->n_lights, c.fr->ambient, (int)c.fr->n_ambient, col,
+                        tex);
         if ((c.fr->flags & PR_FRAME_SHADOWMAP) && (mat->flags & PR_MAT_RECEIVE_SHADOW)) {
             float visibles = 0;
             size_t plane = (size_t)c.SW * c.SH;
@@ -573,74 +822,6 @@ void parallel_rows(int threads, int H, F&& fn) {
 }  // namespace
 
 // ---------------------------------------------------------------- C API
-
-// ---- passAntialiasing: imageutil.Resize (internal/imageutil/resize.go:16-181)
-
-float resize_linear(float in) {
-    in = std::fabs(in);
-    if (in <= 1) return 1 - in;
-    return 0;
-}
-
-// createWeights8 with the linear kernel: int16 taps (x256) and start indices
-void create_weights8(int dy, int filter_length, float scale, std::vector<int16_t>& coeffs, std::vector<int>& start,
-                     int& len) {
-    len = filter_length * (int)std::max(std::ceil(scale), 1.0f);
-    float factor = std::min(1.0f / scale, 1.0f);
-    coeffs.assign((size_t)dy * len, 0);
-    start.assign(dy, 0);
-    for (int y = 0; y < dy; y++) {
-        float interp = scale * ((float)y + 0.5f) - 0.5f;
-        start[y] = (int)interp - len / 2 + 1;
-        interp -= (float)start[y];
-        for (int i = 0; i < len; i++) {
-            float in = (interp - (float)i) * factor;
-            coeffs[(size_t)y * len + i] = (int16_t)(resize_linear(in) * 256);
-        }
-    }
-}
-
-// resizeRGBA: `in` has in_dx pixels per row; writes out (out_dx x out_dy),
-// out row y column x from in row x (the passes transpose).
-void resize_rgba(const uint8_t* in, int in_dx, uint8_t* out, int out_dx, int out_dy,
-                 const std::vector<int16_t>& coeffs, const std::vector<int>& start, int len) {
-    const int maxX = in_dx - 1;
-    for (int x = 0; x < out_dx; x++) {
-        const uint8_t* row = in + (size_t)x * in_dx * 4;
-        for (int y = 0; y < out_dy; y++) {
-            int32_t rgba[4] = {0, 0, 0, 0}, sum = 0;
-            for (int i = 0; i < len; i++) {
-                int32_t coeff = coeffs[(size_t)y * len + i];
-                if (coeff == 0) continue;
-                int xi = start[y] + i;
-                if ((unsigned)xi < (unsigned)maxX)
-                    xi *= 4;
-                else if (xi >= maxX)
-                    xi = 4 * maxX;
-                else
-                    xi = 0;
-                for (int k = 0; k < 4; k++) rgba[k] += coeff * (int32_t)row[xi + k];
-                sum += coeff;
-            }
-            for (int k = 0; k < 4; k++) {
-                int v = rgba[k] / sum;
-                out[((size_t)y * out_dx + x) * 4 + k] = (uint8_t)std::min(std::max(v, 0), 255);
-            }
-        }
-    }
-}
-
-void resize_image(const uint8_t* img, int dx, int dy, int width, int height, uint8_t* out) {
-    float scale_x = (float)dx / (float)width, scale_y = (float)dy / (float)height;
-    std::vector<int16_t> coeffs;
-    std::vector<int> start;
-    int len;
-    std::vector<uint8_t> temp((size_t)dy * width * 4);  // Dx = dy, Dy = width (transposed)
-    create_weights8(width, 2, scale_x, coeffs, start, len);
-    resize_rgba(img, dx, temp.data(), dy, width, coeffs, start, len);
-    create_weights8(height, 2, scale_y, coeffs, start, len);
-    resize_rgba(temp.data(), dy, out, width, height, coeffs, start, len);
-}
 
 extern "C" {
 
@@ -758,6 +939,59 @@ int orc_shadow_camera(const float light_pos[3], const float center[3], const flo
     return PR_OK;
 }
 
+// NewTexture's levels (level 0 alone without mipmaps): texels into out
+// (capacity cap, in texels), [n, w0, h0, off0, ...] into desc (1 + 3*16).
+long long orc_texture_build(int w, int h, const uint8_t* rgba, int mipmap, uint8_t* out, size_t cap, int32_t* desc) {
+    if (w < 1 || h < 1 || !rgba) return PR_ERR_INVALID_ARG;
+    OImg img;
+    img.w = w;
+    img.h = h;
+    img.pix.assign(rgba, rgba + (size_t)w * h * 4);
+    OTex t = new_texture(img, mipmap != 0);
+    const int n = mipmap ? (int)t.mipmap.size() : 1;
+    size_t off = 0;
+    if (desc) std::memset(desc, 0, sizeof(int32_t) * (1 + 3 * 16));
+    if (desc) desc[0] = n;
+    for (int i = 0; i < n && i < 16; i++) {
+        const OImg& lv = t.mipmap[i];
+        if (desc) {
+            desc[1 + 3 * i] = lv.w;
+            desc[2 + 3 * i] = lv.h;
+            desc[3 + 3 * i] = (int32_t)off;
+        }
+        const size_t cnt = (size_t)lv.w * lv.h;
+        if (out && off + cnt <= cap) std::memcpy(out + off * 4, lv.pix.data(), cnt * 4);
+        off += cnt;
+    }
+    return (long long)off;
+}
+
+// Texture.Query of n (lod, u, v) triples, or with du / dv the
+// FragmentShader's lod of (du[k], dv[k]); v is passed to Query as given.
+int orc_texture_query(int w, int h, const uint8_t* rgba, int mipmap, int n, const float* lod, const float* du,
+                      const float* dv, const float* u, const float* v, uint8_t* out) {
+    if (w < 1 || h < 1 || !rgba || !u || !v || !out || (!lod && !(du && dv))) return PR_ERR_INVALID_ARG;
+    OImg img;
+    img.w = w;
+    img.h = h;
+    img.pix.assign(rgba, rgba + (size_t)w * h * 4);
+    OTex t = new_texture(img, mipmap != 0);
+    for (int k = 0; k < n; k++) {
+        float l = lod ? lod[k] : 0.0f;
+        if (du && dv) {
+            l = 0;
+            if (t.use_mipmap) {
+                float siz = (float)t.mipmap[0].w * (float)std::sqrt((double)gomath::pmax(du[k], dv[k]));
+                if (siz < 1) siz = 1;
+                l = (float)gomath::go_log2((double)siz);
+            }
+        }
+        const RGBA c = texture_query(t, l, u[k], v[k]);
+        std::memcpy(out + 4 * k, c.data(), 4);
+    }
+    return PR_OK;
+}
+
 // imageutil.Resize of a dx x dy RGBA image (rows top-down) to w x h.
 int orc_resize(const uint8_t* img, int dx, int dy, int w, int h, uint8_t* out) {
     if (!img || !out || dx <= 0 || dy <= 0 || w <= 0 || h <= 0) return PR_ERR_INVALID_ARG;
@@ -776,6 +1010,23 @@ int orc_render(const pr_scene_desc* sc, const pr_frame_desc* fr, float* shadow_s
     c.sc = sc;
     c.fr = fr;
     c.M = (fr->size >= offsetof(pr_frame_desc, msaa) + sizeof(int32_t) && fr->msaa > 1) ? fr->msaa : 1;
+    // the materials' image textures (NewTexture once per render here)
+    std::vector<OTex> textures;
+    std::vector<const OTex*> mat_tex(sc->n_materials, nullptr);
+    const pr_texture* stex = sc->size >= offsetof(pr_scene_desc, textures) + sizeof(void*) ? sc->textures : nullptr;
+    if (stex) {
+        textures.reserve(sc->n_materials);
+        for (uint32_t m = 0; m < sc->n_materials; m++) {
+            if (!stex[m].rgba) continue;
+            OImg img;
+            img.w = stex[m].width;
+            img.h = stex[m].height;
+            img.pix.assign(stex[m].rgba, stex[m].rgba + (size_t)img.w * img.h * 4);
+            textures.push_back(new_texture(img, (sc->materials[m].flags & PR_MAT_MIPMAP) != 0));
+            mat_tex[m] = &textures.back();
+        }
+        c.mat_tex = &mat_tex;
+    }
     c.W = fr->width * c.M;
     c.H = fr->height * c.M;
     c.SW = fr->shadow_width > 0 ? fr->shadow_width : c.W;

@@ -22,6 +22,10 @@ typedef struct orc_stats {
 /* imageutil.Resize (internal/imageutil/resize.go:16-181) of a dx x dy RGBA
  * image, rows top-down, to w x h */
 int orc_resize(const uint8_t* img, int dx, int dy, int w, int h, uint8_t* out);
+/* NewTexture's levels and Texture.Query (buffer/texture.go:35-187), for tests */
+long long orc_texture_build(int w, int h, const uint8_t* rgba, int mipmap, uint8_t* out, size_t cap, int32_t* desc);
+int orc_texture_query(int w, int h, const uint8_t* rgba, int mipmap, int n, const float* lod, const float* du,
+                      const float* dv, const float* u, const float* v, uint8_t* out);
 int orc_render(const pr_scene_desc* scene, const pr_frame_desc* frame, float* shadow_state, int threads,
                pr_outputs* out, orc_stats* stats);
 

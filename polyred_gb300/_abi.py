@@ -54,12 +54,20 @@ class pr_material(C.Structure):
                 ("shininess", C.c_float), ("flags", C.c_uint32), ("texture_size", C.c_int32)]
 
 
+class pr_texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgba", C.c_void_p)]
+
+
+PR_SCENE_DESC_SIZE_V1 = 80
+
+
 class pr_scene_desc(C.Structure):
     _fields_ = [("size", C.c_uint32), ("flags", C.c_uint32), ("n_tris", C.c_uint32),
                 ("n_objects", C.c_uint32), ("n_materials", C.c_uint32), ("reserved", C.c_uint32),
                 ("pos", C.c_void_p), ("nor", C.c_void_p), ("uv", C.c_void_p), ("col", C.c_void_p),
                 ("mat_id", C.c_void_p), ("objects", C.POINTER(pr_object)),
-                ("materials", C.POINTER(pr_material))]
+                ("materials", C.POINTER(pr_material)),
+                ("textures", C.c_void_p)]
 
 
 class pr_light(C.Structure):

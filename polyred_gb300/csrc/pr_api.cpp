@@ -21,6 +21,10 @@
 
 using prh::M4;
 
+namespace prh {
+int build_texture(int w, int h, const uint8_t* rgba, bool mipmap, std::vector<uint32_t>& texels, prt::TexDesc& d);
+}
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -116,6 +120,10 @@ struct SceneBufs {
     DevBuf<int32_t> obj_matbase;
     DevBuf<pr_material> dmats;
     DevBuf<uint32_t> blk_obj;              // object of the first triangle of each 128-triangle block
+    DevBuf<uint32_t> texels;               // image textures: every mipmap level, packed RGBA8
+    DevBuf<prt::TexDesc> tex;
+    DevBuf<int32_t> mat_tex;               // [n_materials] texture of each material, -1: uniform
+    bool has_tex = false;
     HostBuf tables;                        // page-locked staging of the small tables (submitted uploads)
     cudaEvent_t ev_uploaded = nullptr;     // the upload into these buffers has landed
     cudaEvent_t ev_released = nullptr;     // the last frame that read them is past shading
@@ -123,6 +131,8 @@ struct SceneBufs {
         pos.release(); nor.release(); uv.release(); col.release(); mat.release();
         obj_first.release(); tri_flags.release(); obj_model.release(); obj_normal.release();
         obj_matbase.release(); dmats.release(); blk_obj.release(); tables.release();
+        texels.release(); tex.release(); mat_tex.release();
+        has_tex = false;
         if (ev_uploaded) cudaEventDestroy(ev_uploaded);
         if (ev_released) cudaEventDestroy(ev_released);
         ev_uploaded = ev_released = nullptr;
@@ -194,9 +204,21 @@ M4 loadm(const float* p) {
     return m;
 }
 
+// The image textures of a scene descriptor (NULL for descriptors without the field).
+const pr_texture* scene_textures(const pr_scene_desc* s) {
+    return s->size >= offsetof(pr_scene_desc, textures) + sizeof(void*) ? s->textures : nullptr;
+}
+
+bool scene_has_images(const pr_scene_desc* s) {
+    const pr_texture* t = scene_textures(s);
+    for (uint32_t m = 0; t && m < s->n_materials; m++)
+        if (t[m].rgba) return true;
+    return false;
+}
+
 int validate_scene(const pr_scene_desc* s) {
     if (!s) return fail(PR_ERR_INVALID_ARG, "scene is NULL");
-    if (s->size < sizeof(pr_scene_desc)) return fail(PR_ERR_INVALID_ARG, "scene->size %u < %zu", s->size, sizeof(pr_scene_desc));
+    if (s->size < PR_SCENE_DESC_SIZE_V1) return fail(PR_ERR_INVALID_ARG, "scene->size %u < %u", s->size, PR_SCENE_DESC_SIZE_V1);
     if (s->n_tris > 0 && (!s->pos || !s->nor || !s->uv || !s->col || !s->mat_id))
         return fail(PR_ERR_INVALID_ARG, "scene arrays must be non-NULL when n_tris > 0");
     if (s->n_tris >= (1u << 29)) return fail(PR_ERR_INVALID_ARG, "n_tris %u exceeds 2^29 (draw-order key limit)", s->n_tris);
@@ -211,9 +233,14 @@ int validate_scene(const pr_scene_desc* s) {
         expect += s->objects[o].n_tris;
     }
     if (expect != s->n_tris) return fail(PR_ERR_INVALID_ARG, "objects cover %u triangles, scene has %u", expect, s->n_tris);
+    const pr_texture* tx = scene_textures(s);
     for (uint32_t m = 0; m < s->n_materials; m++) {
-        if (s->materials[m].texture_size != 1)
-            return fail(PR_ERR_UNSUPPORTED, "material %u: only uniform (1x1) textures are supported", m);
+        if (tx && tx[m].rgba) {
+            if (tx[m].width < 1 || tx[m].height < 1 || tx[m].width > 16384 || tx[m].height > 16384)
+                return fail(PR_ERR_INVALID_ARG, "material %u: texture %dx%d outside 1..16384", m, tx[m].width, tx[m].height);
+        } else if (s->materials[m].texture_size != 1) {
+            return fail(PR_ERR_UNSUPPORTED, "material %u: texture_size %d without an image", m, s->materials[m].texture_size);
+        }
     }
     return PR_OK;
 }
@@ -295,6 +322,33 @@ int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool stage
     if ((rc = upload(b.blk_obj, t_blk, blk.size(), false, st))) return rc;
     if ((rc = b.tri_flags.ensure(std::max<uint32_t>(n, 1)))) return rc;
     KTRY(prk::launch_tri_flags(b.pos.p, n, b.tri_flags.p, st));
+    // image textures: NewTexture's levels built here, once per upload
+    b.has_tex = false;
+    if (scene_has_images(s)) {
+        const pr_texture* tx = scene_textures(s);
+        std::vector<uint32_t> texels;
+        std::vector<prt::TexDesc> descs;
+        std::vector<int32_t> mat_tex(nm, -1);
+        try {
+            for (uint32_t m = 0; m < nm; m++) {
+                if (!tx[m].rgba) continue;
+                prt::TexDesc d;
+                if (prh::build_texture(tx[m].width, tx[m].height, tx[m].rgba, (s->materials[m].flags & PR_MAT_MIPMAP) != 0,
+                                       texels, d))
+                    return fail(PR_ERR_INVALID_ARG, "material %u: texture %dx%d rejected", m, tx[m].width, tx[m].height);
+                if (texels.size() >= (1ull << 32)) return fail(PR_ERR_INVALID_ARG, "textures exceed 2^32 texels");
+                mat_tex[m] = (int32_t)descs.size();
+                descs.push_back(d);
+            }
+        } catch (const std::bad_alloc&) {
+            return fail(PR_ERR_OOM, "host allocation failed while building texture mipmaps");
+        }
+        // pageable sources: each copy has left them when cudaMemcpyAsync returns
+        if ((rc = upload(b.texels, texels.data(), texels.size(), false, st))) return rc;
+        if ((rc = upload(b.tex, descs.data(), descs.size(), false, st))) return rc;
+        if ((rc = upload(b.mat_tex, mat_tex.data(), mat_tex.size(), false, st))) return rc;
+        b.has_tex = true;
+    }
     b.objects.assign(s->objects, s->objects + no);
     b.materials.assign(s->materials, s->materials + nm);
     b.n_tris = n;
@@ -413,6 +467,11 @@ void collect_stats(Ctx* c) {
 // The frame-level fields of the deferred pass: size, flags, materials,
 // lights (render/raster.go:275-295), camera, background, matrices, gamma.
 void fill_shade_frame(const Ctx* c, const pr_frame_desc* f, const M4& s2w, int SW, int SH, prk::ShadeParams& sp) {
+    if (c->sb.has_tex) {
+        sp.mat_tex = c->sb.mat_tex.p;
+        sp.tex = c->sb.tex.p;
+        sp.texels = c->sb.texels.p;
+    }
     sp.W = f->width;
     sp.H = f->height;
     sp.flags = f->flags;
@@ -1116,6 +1175,7 @@ namespace {
 int diff_setup(Ctx* c, const pr_frame_desc* f, const pr_diff_params* prm, prk::DiffParamsK& K) {
     int rc;
     const uint32_t nm = (uint32_t)c->sb.materials.size();
+    if (c->sb.has_tex) return fail(PR_ERR_UNSUPPORTED, "image textures are not available in the adjoint");
     if (prm && prm->size < sizeof(pr_diff_params)) return fail(PR_ERR_INVALID_ARG, "params->size too small");
     if (prm && prm->n_materials != nm && (prm->kd || prm->ks || prm->shininess))
         return fail(PR_ERR_INVALID_ARG, "params->n_materials (%u) differs from the scene's (%u)", prm->n_materials, nm);
@@ -1823,6 +1883,8 @@ int pr_batch_destroy(void* batch) {
 int pr_batch_add_scene(void* batch, const pr_scene_desc* scene, uint32_t* out_index) {
     Batch* b = (Batch*)batch;
     if (!b || !scene || !out_index) return fail(PR_ERR_INVALID_ARG, "NULL argument");
+    if (scene->size >= PR_SCENE_DESC_SIZE_V1 && scene_has_images(scene))
+        return fail(PR_ERR_UNSUPPORTED, "image textures are not available in batches");
     std::lock_guard<std::mutex> lk(b->mu);
     void* c = nullptr;
     int rc = pr_create(b->device, &c);

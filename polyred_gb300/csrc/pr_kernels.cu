@@ -1083,6 +1083,14 @@ PR_DEV bool shadow_hit_fast(const ShadeParams& P, const LightK& L, V4 ws, size_t
 
 // Returns true for a pixel that AO still has to finish (its pre-AO colour is
 // in rgba; the caller lists it).
+// The colour of an image texture at a fragment (Texture.Query at the
+// FragmentShader's lod), out of line: the shade kernel's other paths keep
+// their registers.
+static __device__ __noinline__ uint32_t texture_colour(const prt::TexDesc* td, const uint32_t* texels, float du,
+                                                       float dv, float u, float v) {
+    return prt::tex_query(*td, texels, prt::tex_lod(*td, du, dv), u, v);
+}
+
 PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
     if (x >= P.W || r >= P.H) return false;
     const int W = P.W, H = P.H;
@@ -1129,8 +1137,14 @@ PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
         const float uvX = __fmul_rn(wsum(A.uv[0], A.uv[2], A.uv[4], wc1, wc2, wc3), norm);
         const float uvY = __fmul_rn(wsum(A.uv[1], A.uv[3], A.uv[5], wc1, wc2, wc3), norm);
         const int matid = A.matid;
+        // a mipmapped image texture needs the derivatives for its lod
+        bool need_lod = false;
+        if (P.mat_tex && matid >= 0 && (uint32_t)matid < P.n_mats) {
+            const int t = P.mat_tex[matid];
+            need_lod = t >= 0 && P.tex[t].use_mipmap;
+        }
         float du = 0.0f, dv = 0.0f;
-        if (matid >= 0 && P.guvd) {  // the UV derivatives only feed that G-buffer
+        if (matid >= 0 && (P.guvd || need_lod)) {  // the UV derivatives feed that G-buffer and the lod
             float bx3[3], by3[3];
             barycoord_s(__fadd_rn(fx, 1.0f), fy, X0, Y0, X1, Y1, X2, Y2, sabc, bx3);
             float wc1x = __fmul_rn(rw0, bx3[0]), wc2x = __fmul_rn(rw1, bx3[1]), wc3x = __fmul_rn(rw2, bx3[2]);
@@ -1172,8 +1186,17 @@ PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
         float shadow_w = 1.0f;
         const pr_material* mat = (matid >= 0 && (uint32_t)matid < P.n_mats) ? &P.mats[matid] : nullptr;
         if (mat) {
-            // FragmentShader (shader/blinn_cpu.go:24-106), uniform texture
-            const uint32_t t0 = mat->texture[0], t1 = mat->texture[1], t2 = mat->texture[2], t3 = mat->texture[3];
+            // FragmentShader (shader/blinn_cpu.go:24-106): the texture colour
+            // Query(lod, U, 1-V); a uniform texture gives its texel at any lod
+            uint32_t t0 = mat->texture[0], t1 = mat->texture[1], t2 = mat->texture[2], t3 = mat->texture[3];
+            const int tix = P.mat_tex ? P.mat_tex[matid] : -1;  // the material's image texture, if any
+            if (tix >= 0) {
+                const uint32_t tc = texture_colour(P.tex + tix, P.texels, du, dv, uvX, __fsub_rn(1.0f, uvY));
+                t0 = tc & 0xffu;
+                t1 = (tc >> 8) & 0xffu;
+                t2 = (tc >> 16) & 0xffu;
+                t3 = tc >> 24;
+            }
             if (P.n_lights == 0) {
                 c0 = t0; c1 = t1; c2 = t2; c3 = t3;
             } else {

@@ -9,6 +9,7 @@
 #include <vector_types.h>
 
 #include "../../include/polyred_cuda.h"
+#include "pr_texture.h"
 
 namespace prk {
 
@@ -137,6 +138,9 @@ struct ShadeParams {
     const AttrRec* arec;
     const pr_material* mats;
     uint32_t n_mats;
+    const int32_t* mat_tex;     // [n_mats] image texture of each material (-1: uniform texel), or null: none
+    const prt::TexDesc* tex;    // image textures
+    const uint32_t* texels;     // their mipmap levels, packed RGBA8
     int n_lights, n_ambient;
     LightK lights[kMaxLights];
     float ambient[kMaxAmbient];

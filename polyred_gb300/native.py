@@ -47,6 +47,10 @@ def load(build_if_missing=False):
     lib.pr_debug_ao_probe.argtypes = [C.c_void_p] * 7 + [C.c_int]
     lib.pr_debug_fma_probe.restype = C.c_int
     lib.pr_debug_fma_probe.argtypes = [C.c_void_p] * 5 + [C.c_int]
+    lib.pr_debug_texture_build.restype = C.c_longlong
+    lib.pr_debug_texture_build.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.pr_debug_texture_query.restype = C.c_int
+    lib.pr_debug_texture_query.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 6
     if lib.pr_abi_version() != _abi.ABI_VERSION:
         raise NativeUnavailable("ABI version mismatch")
     _lib = lib

@@ -8,6 +8,8 @@
                   U[-10,10]^3, radii U[0.2,1.5], 4 materials, point +
                   directional light, AO and shadow maps
   triangle_soup   small random triangles with log-normal screen area
+  textured_scene  spheres and a ground with image textures (mipmapped and
+                  not, square and not)
   obj_tori        Wavefront OBJ / MTL text of a field of tori (quads with vt
                   and vn, three materials, some triangle+quad objects, some
                   negative indices) for the OBJ loading path
@@ -129,6 +131,46 @@ def small_scene(width=800, height=500):
     sphere = sc.Geometry(uv_sphere(64, 32, 1.0), mat)
     ground = sc.Geometry(ground_plane(10.0, -1.0))
     s = sc.Scene(sphere, ground, sc.Point(position=(4, 4, 2), intensity=1.0), sc.Ambient(intensity=0.1))
+    cam = sc.Perspective(position=(0, 1.5, 4), target=(0, 0, 0), up=(0, 1, 0), fov=45, aspect=width / height,
+                         near=0.1, far=100)
+    return s, cam
+
+
+def checker_image(width, height, cells=8, seed=0x7E47):
+    """A seeded RGBA8 test image: a colour checkerboard of cells x cells
+    squares with a noise band and a transparent corner (rows top-down)."""
+    y, x = np.mgrid[0:height, 0:width]
+    cx, cy = (x * cells) // max(width, 1), (y * cells) // max(height, 1)
+    img = np.zeros((height, width, 4), np.uint8)
+    odd = (cx + cy) % 2 == 1
+    img[..., 0] = np.where(odd, 230, 40)
+    img[..., 1] = (x * 255 // max(width - 1, 1)).astype(np.uint8)
+    img[..., 2] = (y * 255 // max(height - 1, 1)).astype(np.uint8)
+    img[..., 3] = 255
+    rng = np.random.default_rng(seed)
+    band = slice(height // 3, height // 3 + max(height // 8, 1))
+    img[band, :, :3] = rng.integers(0, 256, img[band, :, :3].shape, dtype=np.uint8)
+    img[: height // 4, : width // 4, 3] = 0
+    return img
+
+
+def textured_scene(width=800, height=500):
+    """Image textures: a 64x32 UV sphere with a mipmapped 256x256 checker,
+    a ground with a 64x16 texture sampled without mipmaps (queryL0), and a
+    second sphere with a 37x300 mipmapped texture (non-square, not a power
+    of two); one shadow-casting point light and ambient 0.15."""
+    ks = sc.color_from_value(0.5, 0.5, 0.5, 1.0)
+    m_sphere = sc.BlinnPhong(diffuse=sc.color_from_value(0.8, 0.8, 0.8, 1.0), specular=ks, shininess=32,
+                             texture=sc.ImageTexture(checker_image(256, 256), mipmap=True))
+    m_ground = sc.BlinnPhong(diffuse=sc.color_from_value(0.6, 0.6, 0.6, 1.0), specular=ks, shininess=8,
+                             texture=sc.ImageTexture(checker_image(64, 16, cells=4, seed=3), mipmap=False))
+    m_small = sc.BlinnPhong(diffuse=sc.color_from_value(0.9, 0.9, 0.9, 1.0), specular=ks, shininess=16,
+                            texture=sc.ImageTexture(checker_image(37, 300, cells=5, seed=5), mipmap=True))
+    sphere = sc.Geometry(uv_sphere(64, 32, 1.0), m_sphere)
+    small = sc.Geometry(uv_sphere(32, 16, 0.5), m_small).translate(1.6, -0.5, 0.6)
+    ground = sc.Geometry(ground_plane(10.0, -1.0, material_id=0), m_ground)
+    s = sc.Scene(sphere, small, ground, sc.Point(position=(4, 4, 2), intensity=1.0, cast_shadow=True),
+                 sc.Ambient(intensity=0.15))
     cam = sc.Perspective(position=(0, 1.5, 4), target=(0, 0, 0), up=(0, 1, 0), fov=45, aspect=width / height,
                          near=0.1, far=100)
     return s, cam

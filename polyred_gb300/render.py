@@ -161,11 +161,21 @@ class FlatScene:
         self.col = cat(col, (0, 3, 4), np.uint8)
         self.mat_id = cat(mid, (0,), np.int32)
         self.materials = (_abi.pr_material * max(len(mats), 1))()
+        images = [mt.texture if isinstance(mt.texture, sc.ImageTexture) else None for mt in mats]
+        self.textures = None  # pr_texture per material when any material has an image
+        if any(t is not None for t in images):
+            self.textures = (_abi.pr_texture * len(mats))()
+            for k, t in enumerate(images):
+                if t is not None:
+                    self.textures[k].width = t.rgba.shape[1]
+                    self.textures[k].height = t.rgba.shape[0]
+                    self.textures[k].rgba = t.rgba.ctypes.data
+        self._images = images  # keep the pixel arrays alive with the descriptor
         for k, mt in enumerate(mats):
             dst = self.materials[k]
             dst.diffuse[:] = mt.diffuse
             dst.specular[:] = mt.specular
-            dst.texture[:] = mt.texture
+            dst.texture[:] = (255, 255, 255, 255) if images[k] is not None else mt.texture
             dst.shininess = float(mt.shininess)
             dst.flags = ((_abi.PR_MAT_FLAT_SHADING if mt.flat_shading else 0)
                          | (_abi.PR_MAT_AO if mt.ambient_occlusion else 0)
@@ -188,6 +198,7 @@ class FlatScene:
         d.mat_id = self.mat_id.ctypes.data
         d.objects = self.objects
         d.materials = self.materials
+        d.textures = C.cast(self.textures, C.c_void_p) if self.textures is not None else None
         return d
 
 

@@ -110,20 +110,38 @@ class Ambient:
 
 # ---------------------------------------------------------------- material
 
+class ImageTexture:
+    """buffer.NewTexture(TextureImage(img), TextureIsoMipmap(mipmap))
+    (buffer/texture.go:35-67, 216-226): an RGBA8 image, rows top-down as
+    image.RGBA stores them; the library builds the mipmap levels."""
+
+    def __init__(self, rgba, mipmap=True):
+        a = np.ascontiguousarray(rgba, np.uint8)
+        if a.ndim != 3 or a.shape[2] != 4 or a.shape[0] < 1 or a.shape[1] < 1:
+            raise ValueError(f"texture image must be (height, width, 4) uint8, got {a.shape}")
+        self.rgba = a
+        self.mipmap = bool(mipmap)
+
+    def size(self):
+        """Texture.Size(): the image width."""
+        return self.rgba.shape[1]
+
+
 class BlinnPhong:
-    """material.BlinnPhong (material/material.go:43-72) with a uniform texture
-    (buffer.NewUniformTexture). Colours are RGBA8 tuples."""
+    """material.BlinnPhong (material/material.go:43-72). The texture is an
+    RGBA8 tuple (buffer.NewUniformTexture) or an ImageTexture. Colours are
+    RGBA8 tuples."""
 
     def __init__(self, diffuse=None, specular=None, shininess=1.0, texture=(255, 255, 255, 255), flat_shading=False,
                  ambient_occlusion=False, receive_shadow=False, mipmap=True):
         self.diffuse = tuple(diffuse) if diffuse is not None else color_from_value(0.5, 0.5, 0.5, 1.0)
         self.specular = tuple(specular) if specular is not None else color_from_value(0.5, 0.5, 0.5, 1.0)
         self.shininess = F32(shininess)
-        self.texture = tuple(int(c) for c in texture)
+        self.texture = texture if isinstance(texture, ImageTexture) else tuple(int(c) for c in texture)
         self.flat_shading = bool(flat_shading)
         self.ambient_occlusion = bool(ambient_occlusion)
         self.receive_shadow = bool(receive_shadow)
-        self.mipmap = bool(mipmap)
+        self.mipmap = texture.mipmap if isinstance(texture, ImageTexture) else bool(mipmap)
 
 
 # ---------------------------------------------------------------- geometry
