@@ -1091,6 +1091,9 @@ static __device__ __noinline__ uint32_t texture_colour(const prt::TexDesc* td, c
     return prt::tex_query(*td, texels, prt::tex_lod(*td, du, dv), u, v);
 }
 
+// kTex: the scene has image textures (P.mat_tex set); without them the
+// texture code is compiled out and the kernel keeps its registers.
+template <bool kTex>
 PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
     if (x >= P.W || r >= P.H) return false;
     const int W = P.W, H = P.H;
@@ -1139,7 +1142,7 @@ PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
         const int matid = A.matid;
         // a mipmapped image texture needs the derivatives for its lod
         bool need_lod = false;
-        if (P.mat_tex && matid >= 0 && (uint32_t)matid < P.n_mats) {
+        if (kTex && matid >= 0 && (uint32_t)matid < P.n_mats) {
             const int t = P.mat_tex[matid];
             need_lod = t >= 0 && P.tex[t].use_mipmap;
         }
@@ -1189,7 +1192,7 @@ PR_DEV bool shade_one(const ShadeParams& P, int x, int r) {
             // FragmentShader (shader/blinn_cpu.go:24-106): the texture colour
             // Query(lod, U, 1-V); a uniform texture gives its texel at any lod
             uint32_t t0 = mat->texture[0], t1 = mat->texture[1], t2 = mat->texture[2], t3 = mat->texture[3];
-            const int tix = P.mat_tex ? P.mat_tex[matid] : -1;  // the material's image texture, if any
+            const int tix = kTex ? P.mat_tex[matid] : -1;  // the material's image texture, if any
             if (tix >= 0) {
                 const uint32_t tc = texture_colour(P.tex + tix, P.texels, du, dv, uvX, __fsub_rn(1.0f, uvY));
                 t0 = tc & 0xffu;
@@ -1309,9 +1312,10 @@ PR_DEV void ao_append_tile(const ShadeParams& P, bool pending, uint32_t i) {
         P.ao_list[o] = i;
     }
 }
+template <bool kTex>
 __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
-    const bool pending = shade_one(P, x, r);
+    const bool pending = shade_one<kTex>(P, x, r);
     if (P.ao_list) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
 }
 
@@ -1783,7 +1787,7 @@ __global__ void __launch_bounds__(256) shade_batch_kernel(const ShadeParams* vie
     const uint32_t b = blockIdx.x - blk[v], tiles_x = (uint32_t)(P.W + 31) / 32u;
     const uint32_t ty = b / tiles_x, tx = b - ty * tiles_x;
     const int x = (int)(tx * 32u + (threadIdx.x & 31u)), r = (int)(ty * 8u + (threadIdx.x >> 5));
-    const bool pending = shade_one(P, x, r);
+    const bool pending = shade_one<false>(P, x, r);  // batches carry no image textures
     if (P.ao_list) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
 }
 
@@ -1910,7 +1914,10 @@ int launch_nan_cleanup(size_t n, uint32_t* a, uint32_t va, uint32_t* b, uint32_t
 int launch_shade(const ShadeParams& p, void* stream) {
     dim3 blk(32, 8);
     dim3 grd((p.W + 31) / 32, (p.H + 7) / 8);
-    shade_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
+    if (p.mat_tex)
+        shade_kernel<true><<<grd, blk, 0, (cudaStream_t)stream>>>(p);
+    else
+        shade_kernel<false><<<grd, blk, 0, (cudaStream_t)stream>>>(p);
     return check(cudaGetLastError());
 }
 int launch_tri_flags(const float4* pos, uint32_t n, uint8_t* flags, void* stream) {
