@@ -525,6 +525,20 @@ int pr_obj_destroy(void* obj);
 int pr_obj_parse(void* obj, int kind, const char* text, size_t len);
 int pr_obj_get(void* obj, pr_obj_info* out);
 
+/* ---- image helpers for texture loading --------------------------------
+ * imageutil.LoadImage (internal/imageutil/image.go:47-106) decodes an image
+ * file, converts it to image.RGBA and, with GammaCorrect(true), maps R, G, B
+ * from sRGB to linear. Host only. */
+/* The byte map of that gamma correction: out[b] = uint8(FromsRGB2Linear(
+ * float32(b)/0xff)*0xff + 0.5) (color/srgb.go:35-75). */
+int pr_srgb_decode_table(uint8_t out[256]);
+/* PNG scanline reconstruction (the five filter types of the PNG
+ * specification, as Go's image/png undoes them): `in` holds height rows of
+ * a filter byte and row_bytes bytes, bpp = bytes per complete pixel (at
+ * least 1); writes height rows of row_bytes bytes to out. PR_ERR_INVALID_ARG
+ * for an unknown filter type. */
+int pr_png_unfilter(const uint8_t* in, int height, size_t row_bytes, int bpp, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -240,6 +240,8 @@ ENTRY_POINTS = [
     ("pr_obj_destroy", C.c_int, [VP]),
     ("pr_obj_parse", C.c_int, [VP, C.c_int, C.c_char_p, C.c_size_t]),
     ("pr_obj_get", C.c_int, [VP, C.POINTER(pr_obj_info)]),
+    ("pr_srgb_decode_table", C.c_int, [VP]),
+    ("pr_png_unfilter", C.c_int, [VP, C.c_int, C.c_size_t, C.c_int, VP]),
 ]
 
 

@@ -194,6 +194,78 @@ void gamma_table(uint8_t out[256]) {
     }
 }
 
+// Go math.Pow (math/pow.go) for finite x > 0 and y > 0, the cases the
+// sRGB tables use: Exp(yf*Log(x)) for the fractional part, repeated squaring
+// of Frexp's mantissa for the integer part, Ldexp at the end.
+double go_pow_pos(double x, double y) {
+    if (y == 0 || x == 1) return 1;
+    if (y == 1) return x;
+    if (y == 0.5) return std::sqrt(x);
+    double yi;
+    double yf = std::modf(y, &yi);
+    double a1 = 1.0;
+    long long ae = 0;
+    if (yf != 0) {
+        if (yf > 0.5) {
+            yf -= 1;
+            yi += 1;
+        }
+        a1 = std::exp(yf * std::log(x));
+    }
+    int xe_i;
+    double x1 = std::frexp(x, &xe_i);
+    long long xe = xe_i;
+    for (long long i = (long long)yi; i != 0; i >>= 1) {
+        if (xe < -(1 << 12) || (1 << 12) < xe) {
+            ae += xe;
+            break;
+        }
+        if ((i & 1) == 1) {
+            a1 *= x1;
+            ae += xe;
+        }
+        x1 *= x1;
+        xe <<= 1;
+        if (x1 < .5) {
+            x1 += x1;
+            xe--;
+        }
+    }
+    if (ae > 4096) ae = 4096;
+    if (ae < -4096) ae = -4096;
+    return std::ldexp(a1, (int)ae);
+}
+
+void srgb_decode_table(uint8_t out[256]) {
+    // sRGB2linLUT (color/srgb.go:60-75): v/12.92 below the knee, else
+    // Pow((v+0.055)/1.055, 2.4), in float64 at i/1024
+    double lut[1025];
+    for (int i = 0; i < 1024; i++) {
+        double v = (double)i / 1024;
+        lut[i] = v <= 0.04045 ? v / 12.92 : go_pow_pos((v + 0.055) / 1.055, 2.4);
+    }
+    lut[1024] = lut[1023];
+    // LoadImage's byte map (internal/imageutil/image.go:75-101):
+    // uint8(FromsRGB2Linear(float32(b)/0xff)*0xff + 0.5) in float32
+    for (int c = 0; c < 256; c++) {
+        float v = (float)c / 255.0f;
+        float s;
+        if (v <= 0) {
+            s = 0;
+        } else if (v >= 1) {
+            s = 1;
+        } else {
+            float i = v * 1024.0f;
+            int ifl = (int)i & 1023;
+            float v0 = (float)lut[ifl], v1 = (float)lut[ifl + 1];
+            i -= (float)ifl;
+            s = v0 * (1.0f - i) + v1 * i;
+        }
+        float q = s * 255.0f + 0.5f;
+        out[c] = (uint8_t)((uint32_t)(int32_t)q & 0xffu);
+    }
+}
+
 void ao_directions(float cosv[8], float sinv[8], int* n) {
     const float limit = (float)(6.28318530717958647692 - 1e-4);  // TwoPi - 1e-4 as float32
     const float step = 0.785398163397448309616f;                  // Pi/4 as float32

@@ -21,6 +21,7 @@ M4 ortho(float l, float r, float b, float t, float n, float f);                 
 bool shadow_camera(const float light_pos[3], const float center[3], const M4& cam_view, const M4& cam_proj,
                    M4* out_view, M4* out_proj);          // render/shadow.go:41-85
 void gamma_table(uint8_t out[256]);                      // shader/gamma.go:13-18 + color/srgb.go
+void srgb_decode_table(uint8_t out[256]);                // LoadImage's GammaCorrect map (color/srgb.go)
 void ao_directions(float cosv[8], float sinv[8], int* n); // material/ao.go:28
 // Which AO directions may use the device's tap offset table on a W x H frame
 // (fast[k]), and which component is tiny and negative (tiny[k]: 0, 1 = x, 2 = y).

@@ -4,6 +4,7 @@
 // (pr_texture.h) behind two test entry points.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <new>
@@ -146,6 +147,64 @@ int build_texture(int w, int h, const uint8_t* rgba, bool mipmap, std::vector<ui
 }
 
 }  // namespace prh
+
+// ---- host image helpers (ABI) ----
+
+namespace prh {
+void srgb_decode_table(uint8_t out[256]);
+}
+
+extern "C" {
+
+int pr_srgb_decode_table(uint8_t out[256]) {
+    if (!out) return prk::set_last_error(PR_ERR_INVALID_ARG, "pr_srgb_decode_table: NULL argument");
+    prh::srgb_decode_table(out);
+    return PR_OK;
+}
+
+int pr_png_unfilter(const uint8_t* in, int height, size_t row_bytes, int bpp, uint8_t* out) {
+    if ((!in || !out) && height > 0) return prk::set_last_error(PR_ERR_INVALID_ARG, "pr_png_unfilter: NULL argument");
+    if (height < 0 || bpp < 1 || bpp > 8) return prk::set_last_error(PR_ERR_INVALID_ARG, "pr_png_unfilter: bad size");
+    const uint8_t* prev = nullptr;
+    for (int y = 0; y < height; y++) {
+        const uint8_t* src = in + (size_t)y * (row_bytes + 1);
+        const uint8_t f = src[0];
+        src++;
+        uint8_t* cur = out + (size_t)y * row_bytes;
+        switch (f) {
+            case 0:  // None
+                std::memcpy(cur, src, row_bytes);
+                break;
+            case 1:  // Sub
+                for (size_t i = 0; i < row_bytes; i++) cur[i] = (uint8_t)(src[i] + (i >= (size_t)bpp ? cur[i - bpp] : 0));
+                break;
+            case 2:  // Up
+                for (size_t i = 0; i < row_bytes; i++) cur[i] = (uint8_t)(src[i] + (prev ? prev[i] : 0));
+                break;
+            case 3:  // Average
+                for (size_t i = 0; i < row_bytes; i++) {
+                    const int a = i >= (size_t)bpp ? cur[i - bpp] : 0, b = prev ? prev[i] : 0;
+                    cur[i] = (uint8_t)(src[i] + ((a + b) >> 1));
+                }
+                break;
+            case 4:  // Paeth
+                for (size_t i = 0; i < row_bytes; i++) {
+                    const int a = i >= (size_t)bpp ? cur[i - bpp] : 0, b = prev ? prev[i] : 0;
+                    const int c = (i >= (size_t)bpp && prev) ? prev[i - bpp] : 0;
+                    const int p = a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+                    const int pred = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+                    cur[i] = (uint8_t)(src[i] + pred);
+                }
+                break;
+            default:
+                return prk::set_last_error(PR_ERR_INVALID_ARG, "png: invalid format: bad filter type");
+        }
+        prev = cur;
+    }
+    return PR_OK;
+}
+
+}  // extern "C"
 
 // ---- test entry points (not part of the ABI header) ----
 

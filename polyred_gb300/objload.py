@@ -16,10 +16,9 @@ each an error where the reference would go on:
     or more corners, or triangles with such polygons but no quads) raises
     ValueError here; the reference builds a Geometry with a nil mesh, which
     panics on first use (AABB, Triangles);
-  - materials with map_Kd raise NotImplementedError unless
-    image_textures="ignore" (then they keep the uniform blue texture the
-    reference gives materials without map_Kd): image textures are not on the
-    device path.
+  - map_Kd images are decoded by polyred_gb300.imageload, which reads PNG
+    only; another format raises NotImplementedError (image_textures="ignore"
+    gives such materials the uniform blue texture instead).
 """
 import ctypes as C
 import os
@@ -205,21 +204,25 @@ BLUE = (0, 0, 255, 255)  # color.Blue
 
 def _materials(f, path, image_textures):
     """loadObj's material table (model/load.go:47-84): name -> BlinnPhong for
-    every material the .mtl left in place."""
+    every material the .mtl left in place; a map_Kd image is loaded with
+    GammaCorrect(true) and sampled with isotropic mipmaps."""
+    from . import imageload
     out = {}
     for name, m in f.materials.items():
         if m is None:
             continue
         if m["Illum"] not in (0, 2):
             raise ObjPanic("unsupported illumination model")
-        if m["MapKd"]:
-            if image_textures != "ignore":
-                tex = _go_join(os.path.normpath(f.mtl_dir), os.path.normpath(m["MapKd"]))
-                raise NotImplementedError(
-                    f"material {name!r} of {path} has an image texture ({tex}); image textures are not on "
-                    "the device path (pass image_textures='ignore' to render it with the uniform blue texture)")
+        texture = BLUE
+        if m["MapKd"] and image_textures != "ignore":
+            tex = _go_join(os.path.normpath(f.mtl_dir), os.path.normpath(m["MapKd"]))
+            try:
+                texture = sc.ImageTexture(imageload.load_image(tex, gamma_correct=True), mipmap=True)
+            except NotImplementedError as e:
+                raise NotImplementedError(f"material {name!r} of {path}: {e} (pass image_textures='ignore' to "
+                                          "render it with the uniform blue texture)") from None
         out[name] = sc.BlinnPhong(diffuse=m["Diffuse"], specular=m["Specular"], shininess=m["Shininess"],
-                                  texture=BLUE, flat_shading=False, ambient_occlusion=False,
+                                  texture=texture, flat_shading=False, ambient_occlusion=False,
                                   receive_shadow=False)
     return out
 
@@ -258,7 +261,7 @@ def _check_range(idx, n, what, path):
         raise ObjPanic(f"{path}: {what} index {bad} out of range [0, {n})")
 
 
-def load(path, image_textures="error", skip_faceless=False):
+def load(path, image_textures="load", skip_faceless=False):
     """model.Load (model/load.go:23-38, loadObj 40-152): a Group holding one
     Geometry per OBJ object ('o' / 'g'), each with its own materials.
 
@@ -282,7 +285,7 @@ def load(path, image_textures="error", skip_faceless=False):
     return build_group(f, path, image_textures, skip_faceless)
 
 
-def build_group(f, path="", image_textures="error", skip_faceless=False):
+def build_group(f, path="", image_textures="load", skip_faceless=False):
     """loadObj's second half (model/load.go:47-152) on a parsed ObjFile."""
     mats = _materials(f, path, image_textures)
     default = default_material()
