@@ -533,9 +533,15 @@ def test_faceless_objects(tmp_path):
 
 
 def test_image_texture_policy(tmp_path):
+    """A missing map_Kd file raises (MustLoadImage panics); a file that is
+    not PNG raises NotImplementedError; image_textures='ignore' keeps the
+    uniform blue texture."""
     path = write(tmp_path, "mtllib m.mtl\nusemtl a\nv 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n",
                  "newmtl a\nKd 1 1 1\nillum 2\nmap_Kd tex.png\n")
-    with pytest.raises(NotImplementedError, match="tex.png"):
+    with pytest.raises(FileNotFoundError):
+        objload.load(path)
+    (tmp_path / "tex.png").write_bytes(b"\xff\xd8\xff\xe0" + bytes(16))  # a JPEG header
+    with pytest.raises(NotImplementedError, match="tex.png|PNG"):
         objload.load(path)
     g = objload.load(path, image_textures="ignore")
     assert g.objects[0].materials[0].texture == (0, 0, 255, 255)
