@@ -83,6 +83,15 @@ type SceneDesc struct {
 	MatID      *int32
 	Objects    *Object
 	Materials  *Material
+	// Textures is nil or one entry per material: the image of a
+	// buffer.NewTexture(TextureImage(img)) (RGBA nil keeps the uniform texel).
+	Textures *Texture
+}
+
+// Texture mirrors pr_texture: an *image.RGBA's size and Pix (rows top-down).
+type Texture struct {
+	Width, Height int32
+	RGBA          *uint8
 }
 
 // Light mirrors pr_light.
