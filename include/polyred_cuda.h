@@ -133,8 +133,10 @@ typedef struct pr_scene_desc {
     /* [n_materials] or NULL (host memory): the image texture of each
      * material, sampled by Texture.Query (buffer/texture.go:83-187) at the
      * FragmentShader's level of detail (shader/blinn_cpu.go:28-35); entries
-     * with rgba NULL keep the material's uniform texel. Not available in
-     * batches and the adjoint (PR_ERR_UNSUPPORTED). */
+     * with rgba NULL keep the material's uniform texel. The mipmaps are
+     * built on the host at every pr_scene_upload / pr_frame_submit that
+     * carries the images. Not available in batches and the adjoint
+     * (PR_ERR_UNSUPPORTED). */
     const pr_texture*  textures;
 } pr_scene_desc;
 #define PR_SCENE_DESC_SIZE_V1 80u  /* pr_scene_desc up to materials */
