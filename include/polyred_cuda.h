@@ -515,10 +515,13 @@ typedef struct pr_obj_info {     /* views into the handle, valid until its next 
     const pr_obj_material* materials;
     int64_t n_warnings;
     const int32_t* warnings;         /* string offsets, File.Warnings */
-    const char* strings;  int64_t strings_len;   /* NUL-terminated entries */
+    /* string entries: a native-endian uint32 length n, n bytes (which may
+     * hold NUL, as Go strings may), a NUL */
+    const char* strings;  int64_t strings_len;
     int32_t matlib;                  /* last mtllib file name; -1: none */
     int32_t current_material;        /* matCurrent; -1: none */
     int64_t line;                    /* File.line after the last parse */
+    const char* error;  int64_t error_len;  /* the last parse's error message, all its bytes; empty: none */
 } pr_obj_info;
 
 int pr_obj_create(void** out);

@@ -200,6 +200,7 @@ class pr_obj_info(C.Structure):
         ("n_warnings", C.c_int64), ("warnings", C.POINTER(C.c_int32)),
         ("strings", C.c_void_p), ("strings_len", C.c_int64),
         ("matlib", C.c_int32), ("current_material", C.c_int32), ("line", C.c_int64),
+        ("error", C.c_void_p), ("error_len", C.c_int64),
     ]
 
 

@@ -71,8 +71,12 @@ struct ObjState {
     int64_t line = 1;
     std::string error;
 
+    // entries: a native-endian uint32 length, the bytes (Go strings may hold
+    // NUL), a NUL
     int32_t intern(const char* p, size_t n) {
         int32_t off = (int32_t)strings.size();
+        const uint32_t len = (uint32_t)n;
+        strings.append((const char*)&len, 4);
         strings.append(p, n);
         strings.push_back('\0');
         return off;
@@ -722,6 +726,7 @@ int pr_obj_parse(void* h, int kind, const char* text, size_t len) {
         // is parsed; the counter starts at 1 and advances after every line
         // but the last.
         st.line = 1;
+        st.error.clear();
         size_t pos = 0;
         for (;;) {
             const char* nl = len > pos ? (const char*)memchr(text + pos, '\n', len - pos) : nullptr;
@@ -793,6 +798,8 @@ int pr_obj_get(void* h, pr_obj_info* out) {
     out->matlib = st.matlib;
     out->current_material = st.mat_current;
     out->line = st.line;
+    out->error = st.error.data();
+    out->error_len = (int64_t)st.error.size();
     return PR_OK;
 }
 

@@ -22,6 +22,7 @@ each an error where the reference would go on:
 """
 import ctypes as C
 import os
+import struct
 
 import numpy as np
 
@@ -40,6 +41,19 @@ class ObjError(ValueError):
 class ObjPanic(RuntimeError):
     """The reference panics on this input (e.g. an .mtl colour outside
     [0, 1], an .mtl property before any newmtl, illum other than 0 or 2)."""
+
+
+def _entry(blob, off):
+    """One string of the parser's table: uint32 length, bytes, NUL."""
+    n = struct.unpack_from("=I", blob, off)[0]
+    return blob[off + 4:off + 4 + n].decode("utf-8", errors="surrogateescape")
+
+
+def _info(lib, handle):
+    info = _abi.pr_obj_info()
+    info.size = C.sizeof(_abi.pr_obj_info)
+    native.check(lib.pr_obj_get(handle, C.byref(info)))
+    return info
 
 
 def _np(ptr, n, dtype):
@@ -67,7 +81,7 @@ class ObjFile:
         blob = C.string_at(info.strings, info.strings_len) if info.strings_len else b""
 
         def s(off):
-            return blob[off:blob.index(b"\0", off)].decode("utf-8", errors="surrogateescape")
+            return _entry(blob, off)
 
         self.vertices = _np(info.vertices, 3 * info.n_vertices, F32).reshape(-1, 3)
         self.normals = _np(info.normals, 3 * info.n_normals, F32).reshape(-1, 3)
@@ -127,7 +141,9 @@ def _feed(lib, handle, kind, data):
     st = lib.pr_obj_parse(handle, kind, data, len(data))
     if st == _abi.PR_OK:
         return None
-    msg = lib.pr_last_error().decode("utf-8", errors="replace")
+    info = _info(lib, handle)  # the message with every byte (pr_last_error stops at a NUL)
+    msg = C.string_at(info.error, info.error_len).decode("utf-8", errors="surrogateescape") if info.error_len \
+        else lib.pr_last_error().decode("utf-8", errors="replace")
     if st == _abi.PR_ERR_FATAL:
         raise ObjPanic(msg)
     if st == _abi.PR_ERR_INVALID_ARG:
@@ -136,12 +152,10 @@ def _feed(lib, handle, kind, data):
 
 
 def _matlib(lib, handle):
-    info = _abi.pr_obj_info()
-    info.size = C.sizeof(_abi.pr_obj_info)
-    native.check(lib.pr_obj_get(handle, C.byref(info)))
+    info = _info(lib, handle)
     if info.matlib < 0:
         return ""
-    return C.string_at(info.strings + info.matlib).decode("utf-8", errors="surrogateescape")
+    return _entry(C.string_at(info.strings, info.strings_len), info.matlib)
 
 
 def parse_file(path):

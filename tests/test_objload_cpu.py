@@ -100,6 +100,10 @@ def compare_model(path):
         with pytest.raises(objload.ObjPanic):
             objload.load(path, image_textures="ignore", skip_faceless=True)
         return None
+    except OSError:  # a missing mtllib file: the reference panics
+        with pytest.raises(OSError):
+            objload.load(path, image_textures="ignore", skip_faceless=True)
+        return None
     if any(g is None for g in og):
         with pytest.raises(objload.ObjError, match="no triangle or quad faces"):
             objload.load(path, image_textures="ignore")
@@ -577,3 +581,45 @@ def test_null_arguments(native_lib):
     info = _abi.pr_obj_info()
     assert native_lib.pr_obj_get(h, C.byref(info)) == _abi.PR_ERR_INVALID_ARG  # size unset
     assert native_lib.pr_obj_destroy(h) == _abi.PR_OK
+
+
+def test_nul_bytes_in_names_and_errors(tmp_path):
+    """Go strings hold NUL: names, warnings and error messages keep it."""
+    path = write(tmp_path, b"o a\x00b\nv 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\nx\x00y 1\n")
+    f = compare_file(path)
+    assert f.objects[0][0] == "a\x00b" and "x\x00y" in f.warnings[0]
+    path = write(tmp_path, b"v 1\x002 3\n", name="e.obj")
+    with pytest.raises(objload.ObjError, match="\x00"):
+        objload.parse_file(path)
+    compare_file(path)
+
+
+def _mutate(rng, data):
+    toks = [b"v", b"f", b"o", b"/", b"//", b"-", b"e", b".", b"0x", b"_", b"inf", b"\t", b"\r\n", b"\n", b" ",
+            b"\xc2\xa0", b"\xff", b"\x00", b"1", b"-1", b"2147483648", b"1e39", b"0", b"usemtl", b"Kd", b"illum"]
+    data = bytearray(data)
+    for _ in range(rng.randrange(1, 6)):
+        k, pos = rng.randrange(4), rng.randrange(len(data) + 1)
+        if k == 0 and data:
+            del data[pos:pos + rng.randrange(1, 8)]
+        elif k == 1:
+            data[pos:pos] = rng.choice(toks)
+        elif k == 2 and data:
+            data[min(pos, len(data) - 1)] = rng.randrange(256)
+        else:
+            data[pos:pos] = bytes(rng.randrange(256) for _ in range(rng.randrange(1, 5)))
+    return bytes(data)
+
+
+@pytest.mark.parametrize("seed", range(150))
+def test_mutated_files_match_oracle(tmp_path, seed):
+    """Seeded mutations of valid files and random bytes: the same values or
+    the same error as the oracle (a larger run of this generator found the
+    NUL-byte cases above)."""
+    rng = random.Random(0xF022 + seed)
+    obj, mtl = random_obj(random.Random(seed), consistent=True)
+    obj_b = bytes(rng.randrange(256) for _ in range(rng.randrange(200))) if seed % 5 == 0 else _mutate(rng, obj.encode())
+    mtl_b = _mutate(rng, mtl.encode()) if seed % 3 == 0 else mtl.encode()
+    path = write(tmp_path, obj_b, mtl_b)
+    compare_file(path)
+    compare_model(path)
