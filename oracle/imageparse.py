@@ -125,22 +125,46 @@ def decode(data):
     assert data[:8] == b"\x89PNG\r\n\x1a\n"
     pos = 8
     ihdr, plte, trns, idat = None, None, None, b""
+    allowed = {0: (1, 2, 4, 8, 16), 2: (8, 16), 3: (1, 2, 4, 8), 4: (8, 16), 6: (8, 16)}
     while pos < len(data):
         n, kind = struct.unpack(">I4s", data[pos:pos + 8])
         body = data[pos + 8:pos + 8 + n]
+        if len(body) != n or len(data[pos + 8 + n:pos + 12 + n]) != 4:
+            raise ValueError("png: unexpected EOF")
         if zlib.crc32(kind + body) & 0xFFFFFFFF != struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0]:
             raise ValueError("png: invalid format: invalid checksum")
-        if kind == b"IHDR":
+        if ihdr is None and kind != b"IHDR":
+            raise ValueError("png: invalid format: chunk out of order")
+        if kind == b"IHDR":  # parseIHDR's checks
+            if n != 13:
+                raise ValueError("png: invalid format: bad IHDR length")
             ihdr = struct.unpack(">IIBBBBB", body)
+            w_, h_, d_, c_, comp, filt, inter_ = ihdr
+            if comp != 0 or filt != 0 or inter_ not in (0, 1):
+                raise ValueError("png: unsupported feature: compression, filter or interlace method")
+            if c_ not in allowed or d_ not in allowed[c_]:
+                raise ValueError("png: unsupported feature: bit depth / color type")
+            if w_ <= 0 or h_ <= 0 or w_ >= 1 << 31 or h_ >= 1 << 31:
+                raise ValueError("png: invalid format: invalid dimension")
         elif kind == b"PLTE":
+            if idat or n % 3 or n == 0 or n // 3 > 256 or (ihdr[3] == 3 and n // 3 > 1 << ihdr[2]):
+                raise ValueError("png: invalid format: bad PLTE")
             plte = [tuple(body[3 * i:3 * i + 3]) + (0xFF,) for i in range(n // 3)]
         elif kind == b"tRNS":
+            c_ = ihdr[3]
+            if c_ in (4, 6) or idat or (c_ == 3 and plte is None) or (c_ == 0 and n != 2) or (c_ == 2 and n != 6) \
+                    or n > 256:
+                raise ValueError("png: invalid format: bad tRNS")
             trns = body
         elif kind == b"IDAT":
+            if ihdr[3] == 3 and plte is None:
+                raise ValueError("png: invalid format: chunk out of order")
             idat += body
         elif kind == b"IEND":
             break
         pos += 12 + n
+    if ihdr is None or not idat:
+        raise ValueError("png: invalid format: missing IDAT")
     w, h, depth, ctype, _, _, inter = ihdr
     raw = zlib.decompress(idat)
     nch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
@@ -161,6 +185,8 @@ def decode(data):
         if pw <= 0 or ph <= 0:
             continue
         row_bytes = (pw * bits + 7) // 8
+        if pos + ph * (row_bytes + 1) > len(raw):
+            raise ValueError("png: invalid format: not enough pixel data")
         rows, pos = _unfilter(raw, pos, ph, row_bytes, bpp)
         for ry, row in enumerate(rows):
             for rx in range(pw):
@@ -200,6 +226,8 @@ def decode(data):
                 else:
                     px = _nrgba64(*s) if depth == 16 else _nrgba(*s)
                 img[y0 + ry * dy, x0 + rx * dx] = px
+    if pos != len(raw):
+        raise ValueError("png: invalid format: too much pixel data")
     return img
 
 

@@ -124,6 +124,8 @@ def decode_png(data):
                 raise PNGError("png: invalid format: non-positive dimension")
             ihdr = (w, h, depth, ctype, inter)
         elif kind == b"PLTE":
+            if idat:
+                raise PNGError("png: invalid format: chunk out of order")
             if len(body) % 3 or len(body) // 3 > 256 or len(body) == 0:
                 raise PNGError("png: invalid format: bad PLTE length")
             n = n_plte = len(body) // 3
@@ -131,8 +133,14 @@ def decode_png(data):
             palette[:, 3] = 0xFF  # entries past the palette: opaque black
             palette[:n, :3] = np.frombuffer(body, np.uint8).reshape(n, 3)
         elif kind == b"tRNS":
+            if ihdr[3] in (4, 6):
+                raise PNGError("png: invalid format: tRNS, color type mismatch")
+            if idat or (ihdr[3] == 3 and palette is None):
+                raise PNGError("png: invalid format: chunk out of order")
             trns = body
         elif kind == b"IDAT":
+            if ihdr[3] == 3 and palette is None:
+                raise PNGError("png: invalid format: chunk out of order")
             idat.append(body)
     if ihdr is None or not idat:
         raise PNGError("png: invalid format: missing IDAT")

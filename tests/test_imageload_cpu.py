@@ -171,3 +171,55 @@ def test_obj_map_kd_png(tmp_path):
     assert np.array_equal(tex.rgba, ip.load_image(str(tmp_path / "tex.png"), gamma_correct=True))
     g2 = objload.load(str(tmp_path / "m.obj"), image_textures="ignore")
     assert g2.objects[0].materials[0].texture == (0, 0, 255, 255)
+
+
+def _reassemble(chunks):
+    return b"\x89PNG\r\n\x1a\n" + b"".join(_chunk(k, bytes(b)) for k, b in chunks)
+
+
+def _split(data):
+    pos, out = 8, []
+    while pos < len(data):
+        n, kind = struct.unpack(">I4s", data[pos:pos + 8])
+        out.append([kind, bytearray(data[pos + 8:pos + 8 + n])])
+        pos += 12 + n
+    return out
+
+
+@pytest.mark.parametrize("seed", range(120))
+def test_mutated_pngs_match_oracle(seed):
+    """Seeded damage with valid CRCs (scanline bytes, IHDR fields, a tRNS of
+    any length, chunk order): both decoders give the same image or both
+    reject the file."""
+    import random
+    rng = random.Random(0x9A1 + seed)
+    ctype, depth = rng.choice(CASES)
+    h, w = rng.randrange(1, 12), rng.randrange(1, 12)
+    top = (1 << depth) - 1
+    s = np.random.default_rng(seed).integers(0, top + 1, (h, w, NCH[ctype]))
+    plte = np.random.default_rng(seed).integers(0, 256, (min(top + 1, 6), 3)) if ctype == 3 else None
+    cs = _split(encode_png(s, depth, ctype, plte, None, rng.random() < 0.5, seed))
+    k = rng.randrange(4)
+    if k == 0:
+        raw = bytearray(zlib.decompress(b"".join(bytes(b) for kind, b in cs if kind == b"IDAT")))
+        for _ in range(rng.randrange(1, 4)):
+            if raw and rng.random() < 0.5:
+                raw[rng.randrange(len(raw))] = rng.randrange(256)
+            elif raw and rng.random() < 0.5:
+                del raw[rng.randrange(len(raw))]
+            else:
+                raw.insert(rng.randrange(len(raw) + 1), rng.randrange(256))
+        cs = [c for c in cs if c[0] != b"IDAT"]
+        cs.insert(-1, [b"IDAT", bytearray(zlib.compress(bytes(raw)))])
+    elif k == 1:
+        cs[0][1][rng.choice([8, 9, 12])] = rng.choice([0, 1, 2, 3, 4, 6, 8, 16, 7])
+    elif k == 2:
+        cs.insert(rng.randrange(1, len(cs)), [b"tRNS", bytearray(rng.randrange(256) for _ in range(rng.choice([2, 3, 6, 9])))])
+    data = _reassemble(cs)
+    try:
+        want = ip.decode(data)
+    except ValueError:
+        with pytest.raises(ValueError):
+            imageload.decode_png(data)
+        return
+    assert np.array_equal(imageload.decode_png(data), want)
