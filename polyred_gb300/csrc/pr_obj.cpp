@@ -21,7 +21,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <climits>
 #include <new>
+#include <stdexcept>
 #include <string>
 #include <system_error>
 #include <unordered_map>
@@ -74,6 +76,7 @@ struct ObjState {
     // entries: a native-endian uint32 length, the bytes (Go strings may hold
     // NUL), a NUL
     int32_t intern(const char* p, size_t n) {
+        if (strings.size() + n + 5 > (size_t)INT32_MAX) throw std::length_error("string table exceeds 2 GiB");
         int32_t off = (int32_t)strings.size();
         const uint32_t len = (uint32_t)n;
         strings.append((const char*)&len, 4);
@@ -743,6 +746,8 @@ int pr_obj_parse(void* h, int kind, const char* text, size_t len) {
         }
     } catch (const std::bad_alloc&) {
         return prk::set_last_error(PR_ERR_OOM, "pr_obj_parse: out of host memory");
+    } catch (const std::length_error&) {
+        return prk::set_last_error(PR_ERR_OVERFLOW, "pr_obj_parse: names and warnings exceed 2 GiB");
     }
     return PR_OK;
 }
