@@ -114,6 +114,26 @@ def main(ref):
     out["color_from_value"] = {"cite": "color/color.go:33-44 (used by material.Diffuse/Specular)",
                                "cases": [[[0.8, 0.3, 0.2, 1.0], [204, 77, 51, 255]],
                                          [[0.5, 0.5, 0.5, 1.0], [128, 128, 128, 255]]]}
+    # TestQuery (buffer/texture_test.go:25-166): Texture.Query(lod, u, v)
+    t = open(os.path.join(ref, "buffer/texture_test.go")).read()
+    pix = [int(v) for v in floats(re.search(r"Pix: \[\]uint8\{(.*?)\}", t, re.S).group(1))]
+    rect = [int(v) for v in floats(re.search(r"Rect:\s*image\.Rect\(([^)]*)\)", t).group(1))]
+    cases = []
+    pat = (r'\{\s*"([^"]+)",\s*(.*?),\s*(-?[\d.]+),\s*(-?[\d.]+),\s*(-?[\d.]+),\s*'
+           r"color\.RGBA\{R:\s*(\d+),\s*G:\s*(\d+),\s*B:\s*(\d+),\s*A:\s*(\d+)\}")
+    for m in re.finditer(pat, t[t.index("tests = []struct"):t.index("func TestQuery")], re.S):
+        name, tex = m.group(1), m.group(2)
+        if "TextureImage(data)" in tex:
+            kind = {"image": "data", "mipmap": "TextureIsoMipmap(true)" in tex}
+        elif "mustLoadTexture" in tex:
+            kind = {"asset": os.path.basename(re.search(r'"([^"]+)"', tex).group(1)), "mipmap": True,
+                    "gamma_correct": False}
+        else:
+            kind = {"default": True}
+        cases.append({"name": name, "texture": kind, "u": float(m.group(3)), "v": float(m.group(4)),
+                      "lod": float(m.group(5)), "want": [int(m.group(k)) for k in range(6, 10)]})
+    out["texture_query"] = {"cite": "buffer/texture_test.go:25-166 (TestQuery)", "data_pix": pix,
+                            "data_rect": rect, "cases": cases}
     json.dump(out, open(os.path.join(HERE, "reference_kats.json"), "w"), indent=1)
     print("wrote", os.path.join(HERE, "reference_kats.json"))
 

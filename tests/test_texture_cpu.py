@@ -93,3 +93,53 @@ def test_shader_lod_matches_oracle(native_lib, w, h):
     got = _query(native_lib.pr_debug_texture_query, img, True, u, v, du=du, dv=dv)
     want = _query(oracle.load().orc_texture_query, img, True, u, v, du=du, dv=dv)
     assert np.array_equal(got, want)
+
+
+# ---------------------------------------------------------------- reference known answers
+
+def _kats():
+    import json
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "golden", "reference_kats.json")) as fh:
+        return json.load(fh)["texture_query"]
+
+
+KATS = _kats()
+
+
+def _kat_texture(case):
+    """The texture of one TestQuery case: NewTexture() (1x1 white, mipmap
+    on), the test's 2x2 image, or a reference asset loaded without gamma
+    correction (MustLoadImage(path)); None when the asset is absent."""
+    import os
+    import sys
+    t = case["texture"]
+    if t.get("default"):
+        return np.full((1, 1, 4), 255, np.uint8), True
+    if t.get("image") == "data":
+        x0, y0, x1, y1 = KATS["data_rect"]
+        return np.array(KATS["data_pix"], np.uint8).reshape(y1 - y0, x1 - x0, 4), t["mipmap"]
+    if not t["asset"].endswith(".png"):
+        pytest.skip(f"{t['asset']}: only PNG images are decoded")
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_obj_fixtures as mk
+    path = os.path.join(mk.testdata_dir(), t["asset"])
+    if not os.path.exists(path):
+        pytest.skip("reference test assets not present")
+    from polyred_gb300 import imageload
+    return imageload.load_image(path, gamma_correct=t["gamma_correct"]), t["mipmap"]
+
+
+@pytest.mark.parametrize("k", range(len(KATS["cases"])))
+def test_reference_texture_query_kats(native_lib, k):
+    """TestQuery's vectors (buffer/texture_test.go): Query(lod, u, v) of the
+    library (its mipmap levels and the kernel's query source) and of the
+    oracle equal the reference's answers."""
+    case = KATS["cases"][k]
+    img, mip = _kat_texture(case)
+    img = np.ascontiguousarray(img)
+    u, v, lod = (np.array([case[x]], F32) for x in ("u", "v", "lod"))
+    want = np.array([case["want"]], np.uint8)
+    assert np.array_equal(_query(native_lib.pr_debug_texture_query, img, mip, u, v, lod=lod), want)
+    assert np.array_equal(_query(oracle.load().orc_texture_query, img, mip, u, v, lod=lod), want)
