@@ -223,3 +223,19 @@ def test_mutated_pngs_match_oracle(seed):
             imageload.decode_png(data)
         return
     assert np.array_equal(imageload.decode_png(data), want)
+
+
+def test_reference_load_image_golden():
+    """TestLoadImage (internal/imageutil/image_test.go:16-41): ground.png
+    loaded with GammaCorrect(true) equals golden.png pixel for pixel."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_obj_fixtures as mk
+    d = mk.testdata_dir()
+    ground, golden = os.path.join(d, "ground.png"), os.path.join(d, "golden.png")
+    if not (os.path.exists(ground) and os.path.exists(golden)):
+        pytest.skip("reference test assets not present")
+    got = imageload.load_image(ground, gamma_correct=True)
+    want = imageload.load_image(golden, gamma_correct=False)
+    assert got.shape == want.shape
+    assert np.array_equal(got, want)
