@@ -1249,6 +1249,7 @@ int pr_diff_forward(void* ctx, const pr_frame_desc* frame, const pr_diff_params*
     if (rc) return rc;
     if (frame_msaa(frame) > 1) return fail(PR_ERR_UNSUPPORTED, "MSAA is not available in the adjoint");
     if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
+    if (c->sb.has_tex) return fail(PR_ERR_UNSUPPORTED, "image textures are not available in the adjoint");
     if ((rc = set_device(c))) return rc;
     // the AO factors need the colour pass: render into ctx storage when the caller wants no image
     pr_outputs o{};
