@@ -2,7 +2,7 @@
 
 A restatement of polyred's Go CPU renderer in C++ (oracle.cpp), loaded with
 ctypes. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
-use it, always as the checker; the product never imports it.
+use it, always as the reference to compare with; the product never imports it.
 """
 import ctypes as C
 import os

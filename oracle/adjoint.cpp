@@ -6,9 +6,9 @@
 // shader/blinn_cpu.go:24-106, times the fixed shadow / AO factor of
 // render/raster.go:339-356 and material/ao.go:34-37; material-less pixels show
 // the perspective-correct interpolation of vertex colours,
-// render/raster.go:324-334, 546-549) and serves as the checker of the GPU
-// radiance, of the GPU gradients, and (through orc_diff_forward64) of central
-// finite differences.
+// render/raster.go:324-334, 546-549). The tests compare the GPU radiance,
+// the GPU gradients and (through orc_diff_forward64) central finite
+// differences with it.
 #include <cmath>
 #include <cstdint>
 #include <cstring>

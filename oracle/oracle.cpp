@@ -1,6 +1,6 @@
 // oracle.cpp — CPU restatement of polyred's render path, single-worker order.
 //
-// TEST INFRASTRUCTURE. This is the checker the CUDA path is compared with; it
+// TEST INFRASTRUCTURE. This is the reference the CUDA path is compared with; it
 // is used only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
 // leg. The product (libpolyred_cuda.so) never links or calls it.
 //

@@ -1,7 +1,7 @@
 // oracle.h — C API of the CPU oracle (liboracle.so).
 //
 // TEST INFRASTRUCTURE: loaded only by tests/, __graft_entry__.smoke() and
-// bench.py's CPU-baseline leg, as the checker. It shares the scene/frame/
+// bench.py's CPU-baseline leg, to compare with. It shares the scene/frame/
 // output descriptors of include/polyred_cuda.h so both sides read the same
 // inputs.
 #pragma once

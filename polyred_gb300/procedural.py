@@ -136,7 +136,7 @@ def small_scene(width=800, height=500):
     return s, cam
 
 
-def checker_image(width, height, cells=8, seed=0x7E47):
+def checkerboard_image(width, height, cells=8, seed=0x7E47):
     """A seeded RGBA8 test image: a colour checkerboard of cells x cells
     squares with a noise band and a transparent corner (rows top-down)."""
     y, x = np.mgrid[0:height, 0:width]
@@ -155,17 +155,17 @@ def checker_image(width, height, cells=8, seed=0x7E47):
 
 
 def textured_scene(width=800, height=500):
-    """Image textures: a 64x32 UV sphere with a mipmapped 256x256 checker,
+    """Image textures: a 64x32 UV sphere with a mipmapped 256x256 checkerboard,
     a ground with a 64x16 texture sampled without mipmaps (queryL0), and a
     second sphere with a 37x300 mipmapped texture (non-square, not a power
     of two); one shadow-casting point light and ambient 0.15."""
     ks = sc.color_from_value(0.5, 0.5, 0.5, 1.0)
     m_sphere = sc.BlinnPhong(diffuse=sc.color_from_value(0.8, 0.8, 0.8, 1.0), specular=ks, shininess=32,
-                             texture=sc.ImageTexture(checker_image(256, 256), mipmap=True))
+                             texture=sc.ImageTexture(checkerboard_image(256, 256), mipmap=True))
     m_ground = sc.BlinnPhong(diffuse=sc.color_from_value(0.6, 0.6, 0.6, 1.0), specular=ks, shininess=8,
-                             texture=sc.ImageTexture(checker_image(64, 16, cells=4, seed=3), mipmap=False))
+                             texture=sc.ImageTexture(checkerboard_image(64, 16, cells=4, seed=3), mipmap=False))
     m_small = sc.BlinnPhong(diffuse=sc.color_from_value(0.9, 0.9, 0.9, 1.0), specular=ks, shininess=16,
-                            texture=sc.ImageTexture(checker_image(37, 300, cells=5, seed=5), mipmap=True))
+                            texture=sc.ImageTexture(checkerboard_image(37, 300, cells=5, seed=5), mipmap=True))
     sphere = sc.Geometry(uv_sphere(64, 32, 1.0), m_sphere)
     small = sc.Geometry(uv_sphere(32, 16, 0.5), m_small).translate(1.6, -0.5, 0.6)
     ground = sc.Geometry(ground_plane(10.0, -1.0, material_id=0), m_ground)

@@ -59,7 +59,7 @@ def test_obj_png_texture_bitexact(device, tmp_path):
     import numpy as np
     obj, mtl, _ = procedural.obj_tori(6, 24, 12)
     mtl = mtl.replace(b"newmtl m0\n", b"newmtl m0\nmap_Kd wood.png\n")
-    img = procedural.checker_image(128, 64, cells=6, seed=12)[..., :3]
+    img = procedural.checkerboard_image(128, 64, cells=6, seed=12)[..., :3]
     (tmp_path / "tori.obj").write_bytes(obj)
     (tmp_path / "tori.mtl").write_bytes(mtl)
     (tmp_path / "wood.png").write_bytes(_png_rgb(np.ascontiguousarray(img)))
