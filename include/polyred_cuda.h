@@ -284,6 +284,18 @@ int pr_stream(void* ctx, void** out_stream);
 int pr_host_alloc(size_t bytes, void** out_ptr);
 int pr_host_free(void* ptr);
 
+/* Device memory for outputs kept on the GPU (PR_OUT_DEVICE_PTRS) by hosts
+ * that have no device allocator of their own: the frame's fragments stay
+ * device-resident, as the reference's deferred seam wants them
+ * (render/gpudeferred.go:110-187), and the host reads what it needs.
+ * pr_device_alloc / pr_device_free: cudaMalloc / cudaFree on the context's
+ * GPU. pr_device_read copies `bytes` from device address `src` to host
+ * memory `dst` after every frame already issued on the context (it waits
+ * for them), and returns when the copy is done. */
+int pr_device_alloc(void* ctx, size_t bytes, void** out_ptr);
+int pr_device_free(void* ctx, void* ptr);
+int pr_device_read(void* ctx, const void* src, size_t bytes, void* dst);
+
 /* ---- host math helpers --------------------------------------------------
  * f32 arithmetic exactly as the reference's Go (amd64) evaluates it, so a
  * host that is not Go can build the same matrices. Matrices are row-major. */

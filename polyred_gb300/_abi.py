@@ -220,6 +220,9 @@ ENTRY_POINTS = [
     ("pr_stream", C.c_int, [VP, C.POINTER(VP)]),
     ("pr_host_alloc", C.c_int, [C.c_size_t, C.POINTER(VP)]),
     ("pr_host_free", C.c_int, [VP]),
+    ("pr_device_alloc", C.c_int, [VP, C.c_size_t, C.POINTER(VP)]),
+    ("pr_device_free", C.c_int, [VP, VP]),
+    ("pr_device_read", C.c_int, [VP, VP, C.c_size_t, VP]),
     ("pr_view_matrix", C.c_int, [FP, FP, FP, FP]),
     ("pr_perspective_matrix", C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, FP]),
     ("pr_orthographic_matrix", C.c_int, [C.c_float] * 6 + [FP]),

@@ -1117,6 +1117,45 @@ int pr_host_alloc(size_t bytes, void** out_ptr) {
     return PR_OK;
 }
 
+int pr_device_alloc(void* ctx, size_t bytes, void** out_ptr) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !out_ptr || bytes == 0) return fail(PR_ERR_INVALID_ARG, "NULL ctx or out_ptr, or zero bytes");
+    *out_ptr = nullptr;
+    std::lock_guard<std::mutex> lk(c->mu);
+    int rc = set_device(c);
+    if (rc) return rc;
+    cudaError_t e = cudaMalloc(out_ptr, bytes);
+    if (e != cudaSuccess) {
+        *out_ptr = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? PR_ERR_OOM : PR_ERR_CUDA, "cudaMalloc(%zu): %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    return PR_OK;
+}
+
+int pr_device_free(void* ctx, void* ptr) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !ptr) return fail(PR_ERR_INVALID_ARG, "NULL ctx or ptr");
+    std::lock_guard<std::mutex> lk(c->mu);
+    int rc = set_device(c);
+    if (rc) return rc;
+    CUDA_TRY(cudaFree(ptr));
+    return PR_OK;
+}
+
+int pr_device_read(void* ctx, const void* src, size_t bytes, void* dst) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || ((!src || !dst) && bytes)) return fail(PR_ERR_INVALID_ARG, "NULL ctx, src or dst");
+    if (bytes == 0) return PR_OK;
+    std::lock_guard<std::mutex> lk(c->mu);
+    int rc = set_device(c);
+    if (rc) return rc;
+    // after the frames on the context's stream (their outputs land there)
+    CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return PR_OK;
+}
+
 int pr_host_free(void* ptr) {
     if (!ptr) return fail(PR_ERR_INVALID_ARG, "ptr is NULL");
     cudaError_t e = cudaFreeHost(ptr);

@@ -1,6 +1,6 @@
 // Package cuda binds libpolyred_cuda.so (include/polyred_cuda.h) for the Go
 // renderer through purego, keeping polyred cgo-free. It is the Go half of the
-// render.CUDA(dev) option; see INTEGRATION.md for the render package hook.
+// render.CUDA(dev) option.
 //
 // The library is opened like the reference opens its graphics drivers
 // (gpu/backend_gl_lib_linux.go:18-25): purego.Dlopen + RegisterLibFunc. Every
@@ -10,6 +10,7 @@ package cuda
 import (
 	"errors"
 	"fmt"
+	"image"
 	"os"
 	"runtime"
 	"sync"
@@ -161,6 +162,9 @@ var (
 	prSync         func(ctx uintptr) int32
 	prHostAlloc    func(bytes uintptr, out *unsafe.Pointer) int32
 	prHostFree     func(p unsafe.Pointer) int32
+	prDeviceAlloc  func(ctx uintptr, bytes uintptr, out *unsafe.Pointer) int32
+	prDeviceFree   func(ctx uintptr, p unsafe.Pointer) int32
+	prDeviceRead   func(ctx uintptr, src unsafe.Pointer, bytes uintptr, dst unsafe.Pointer) int32
 )
 
 // LibraryPath is where Open looks for the library unless POLYRED_CUDA_LIB
@@ -190,6 +194,9 @@ func load() error {
 		purego.RegisterLibFunc(&prSync, lib, "pr_sync")
 		purego.RegisterLibFunc(&prHostAlloc, lib, "pr_host_alloc")
 		purego.RegisterLibFunc(&prHostFree, lib, "pr_host_free")
+		purego.RegisterLibFunc(&prDeviceAlloc, lib, "pr_device_alloc")
+		purego.RegisterLibFunc(&prDeviceFree, lib, "pr_device_free")
+		purego.RegisterLibFunc(&prDeviceRead, lib, "pr_device_read")
 	})
 	return loadErr
 }
@@ -343,4 +350,136 @@ func HostFree(p unsafe.Pointer) error {
 		return err
 	}
 	return check(prHostFree(p))
+}
+
+// Fragment is one pixel of a GBuffer, the fields of buffer.Fragment
+// (buffer/buffer.go) that the frame produces.
+type Fragment struct {
+	Ok         bool
+	X, Y       int
+	Depth      float32
+	U, V       float32
+	Du, Dv     float32
+	Nor        [4]float32
+	FaceNor    [4]float32
+	WordPos    [4]float32
+	Col        [4]uint8
+	MaterialID int64
+	TriID      uint32
+}
+
+// GBuffer is a frame's outputs kept in device memory: render into it with
+// d.Render(f, g.Outputs()) and read the fragments or the image on demand,
+// instead of copying every field of every pixel to the host after each pass
+// (the per-pass marshal of render/gpudeferred.go:110-187). Fields are W x H
+// (the framebuffer); rows are top-down, row r holding raster row H-1-r.
+type GBuffer struct {
+	dev    *Device
+	W, H   int
+	fields map[string]unsafe.Pointer
+	out    Outputs
+}
+
+var gbufferFields = []struct {
+	name  string
+	bytes int
+}{
+	{"rgba", 4}, {"tri_id", 4}, {"depth", 4}, {"nor", 16}, {"face_nor", 16},
+	{"world_pos", 16}, {"uvd", 16}, {"vcol", 4}, {"mat_id", 4},
+}
+
+// NewGBuffer allocates device outputs for w x h frames on d.
+func (d *Device) NewGBuffer(w, h int) (*GBuffer, error) {
+	if w <= 0 || h <= 0 {
+		return nil, &Error{Status: -1, Detail: "GBuffer size must be positive"}
+	}
+	d.mu.Lock()
+	ctx := d.ctx
+	d.mu.Unlock()
+	if ctx == 0 {
+		return nil, ErrClosed
+	}
+	g := &GBuffer{dev: d, W: w, H: h, fields: map[string]unsafe.Pointer{}}
+	for _, f := range gbufferFields {
+		var p unsafe.Pointer
+		if err := check(prDeviceAlloc(ctx, uintptr(w*h*f.bytes), &p)); err != nil {
+			g.Free()
+			return nil, err
+		}
+		g.fields[f.name] = p
+	}
+	g.out = Outputs{
+		Flags:    1, // PR_OUT_DEVICE_PTRS
+		RGBA:     (*uint8)(g.fields["rgba"]),
+		TriID:    (*uint32)(g.fields["tri_id"]),
+		Depth:    (*float32)(g.fields["depth"]),
+		Nor:      (*float32)(g.fields["nor"]),
+		FaceNor:  (*float32)(g.fields["face_nor"]),
+		WorldPos: (*float32)(g.fields["world_pos"]),
+		UVD:      (*float32)(g.fields["uvd"]),
+		VCol:     (*uint8)(g.fields["vcol"]),
+		MatID:    (*int32)(g.fields["mat_id"]),
+	}
+	runtime.SetFinalizer(g, func(g *GBuffer) { g.Free() })
+	return g, nil
+}
+
+// Outputs is the pr_outputs that renders into this GBuffer.
+func (g *GBuffer) Outputs() *Outputs { return &g.out }
+
+func (g *GBuffer) read(name string, index, size int, dst unsafe.Pointer) error {
+	src := unsafe.Add(g.fields[name], index*size)
+	return check(prDeviceRead(g.dev.ctx, src, uintptr(size), dst))
+}
+
+// Fragment reads the fragment at raster (x, y) (FragmentBuffer.UnsafeGet).
+func (g *GBuffer) Fragment(x, y int) (Fragment, error) {
+	var f Fragment
+	if x < 0 || y < 0 || x >= g.W || y >= g.H {
+		return f, nil // FragmentBuffer.Get: the zero fragment outside the buffer
+	}
+	i := (g.H-1-y)*g.W + x
+	var uvd [4]float32
+	var mat int32
+	reads := []struct {
+		name string
+		size int
+		dst  unsafe.Pointer
+	}{
+		{"tri_id", 4, unsafe.Pointer(&f.TriID)}, {"depth", 4, unsafe.Pointer(&f.Depth)},
+		{"nor", 16, unsafe.Pointer(&f.Nor)}, {"face_nor", 16, unsafe.Pointer(&f.FaceNor)},
+		{"world_pos", 16, unsafe.Pointer(&f.WordPos)}, {"uvd", 16, unsafe.Pointer(&uvd)},
+		{"vcol", 4, unsafe.Pointer(&f.Col)}, {"mat_id", 4, unsafe.Pointer(&mat)},
+	}
+	for _, r := range reads {
+		if err := g.read(r.name, i, r.size, r.dst); err != nil {
+			return Fragment{}, err
+		}
+	}
+	f.Ok = f.TriID != 0xFFFFFFFF // PR_TRI_NONE
+	f.X, f.Y = x, y
+	f.U, f.V, f.Du, f.Dv = uvd[0], uvd[1], uvd[2], uvd[3]
+	f.MaterialID = int64(mat)
+	return f, nil
+}
+
+// Image reads the frame's RGBA8 image (the buffer.Image() layout).
+func (g *GBuffer) Image() (*image.RGBA, error) {
+	img := image.NewRGBA(image.Rect(0, 0, g.W, g.H))
+	err := check(prDeviceRead(g.dev.ctx, g.fields["rgba"], uintptr(len(img.Pix)), unsafe.Pointer(&img.Pix[0])))
+	return img, err
+}
+
+// Free releases the device memory.
+func (g *GBuffer) Free() error {
+	var err error
+	for name, p := range g.fields {
+		if p != nil {
+			if e := check(prDeviceFree(g.dev.ctx, p)); e != nil && err == nil {
+				err = e
+			}
+		}
+		delete(g.fields, name)
+	}
+	return err
 }

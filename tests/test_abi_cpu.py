@@ -73,6 +73,9 @@ def test_null_arguments_are_errors(native_lib):
     assert native_lib.pr_host_free(None) == _abi.PR_ERR_INVALID_ARG
     assert native_lib.pr_frame_submit(None, None, None, None) == _abi.PR_ERR_INVALID_ARG
     assert native_lib.pr_sync(None) == _abi.PR_ERR_INVALID_ARG
+    assert native_lib.pr_device_alloc(None, 16, None) == _abi.PR_ERR_INVALID_ARG
+    assert native_lib.pr_device_free(None, None) == _abi.PR_ERR_INVALID_ARG
+    assert native_lib.pr_device_read(None, None, 4, None) == _abi.PR_ERR_INVALID_ARG
 
 
 def test_singular_inverse(native_lib):
