@@ -16,6 +16,11 @@ sRGB gamma. Metric: Mtri/s = input triangles per second of frame time.
   --impl reference  the CPU restatement of the reference renderer (oracle/),
          all host threads, single-worker draw order
 
+Further legs in the same line (each skippable): diff (the adjoint, --no-diff),
+soup_4k (10M triangles at 3840x2160, --no-soup), batched (many views in one
+job, --no-batch), msaa_2x and textured_1080p (--no-msaa), obj_ingest
+(loading a 41 MB Wavefront OBJ, --no-obj), cpu_baseline (--no-cpu-baseline).
+
 Multi-GPU: frames do not shard (one view); N ranks render N independent
 replicas (weak scaling), the value is the total over ranks.
 """
