@@ -144,56 +144,100 @@ def ncu_traffic():
     return None
 
 
+def bench_config(world):
+    """The workload's config dict; both arms print this same dict."""
+    return {"workload": "sphere_field_1M_1080p", "n_tris": N_TRIS, "width": W, "height": H,
+            "shadow_maps": "2 x 2048^2 (point + directional)", "ao": True, "gamma": True,
+            "l2": "inputs larger than L2 (136 MB triangle soup per frame)",
+            "parallelism": f"replicas x{world}"}
+
+
+def oracle_frame(threads, want=("rgba", "tri_id", "depth")):
+    """Scene, frame and outputs of the workload built without the product
+    library: pmath's matrix helpers run on the oracle's host math, so the
+    process maps liboracle.so alone. Returns a callable rendering one frame
+    with the oracle."""
+    import numpy as np
+    import oracle
+    from oracle import hostmath
+    from polyred_gb300 import pmath, render
+    prev = pmath._backend
+    pmath.set_backend(hostmath)
+    try:
+        s, cam = workload()
+        opts = frame_opts(s, cam)
+        flat = render.FlatScene(s)
+        fd = render.FrameDesc(opts, shadow_cams(opts))
+    finally:
+        pmath.set_backend(prev)
+    state = np.zeros((3, SHADOW[1], SHADOW[0]), np.float32)
+    out = render.Outputs(W, H, want)
+    sd = flat.desc()
+
+    def frame():
+        oracle.render(sd, fd.desc, out.desc, shadow_state=state, threads=threads)
+    frame.keep = (flat, fd, out, state)
+    return frame
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
-    import numpy as np
-    import oracle
-    from polyred_gb300 import render
     threads = os.cpu_count() or 1
-    s, cam = workload()
-    opts = frame_opts(s, cam)
-    flat = render.FlatScene(s)
-    fd = render.FrameDesc(opts, shadow_cams(opts))
-    state = np.zeros((3, SHADOW[1], SHADOW[0]), np.float32)
-    out = render.Outputs(W, H, ("rgba", "tri_id", "depth"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    frame = oracle_frame(threads)
     for _ in range(args.warmup):
-        oracle.render(flat.desc(), fd.desc, out.desc, shadow_state=state, threads=threads)
+        frame()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.render(flat.desc(), fd.desc, out.desc, shadow_state=state, threads=threads)
+        frame()
     dt = (time.perf_counter() - t0) / args.steps
     v = N_TRIS / dt / 1e6
     line = {"impl": "reference", "metric": "1080p Mtri/s", "value": v, "unit": "Mtri/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "sphere_field_1M_1080p", "n_tris": N_TRIS, "width": W, "height": H,
-                       "shadow_maps": "2 x 2048^2", "ao": True},
+            "config": bench_config(world),
             "cpu_baseline": {"value": v, "unit": "Mtri/s", "cores": threads, "kind": "port",
                              "sample": "full frames of the workload, C++ restatement of the Go CPU renderer "
                                        "(row-band threads, single-worker draw order)"},
             "e2e": {"value": v, "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "frames_per_s": 1.0 / dt}
+            "frames_per_s": 1.0 / dt,
+            "native_libraries": mapped_libraries()}
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_sample():
-    """The oracle on one full frame with every host core (bounded: one frame)."""
-    import numpy as np
-    import oracle
-    from polyred_gb300 import render
+def mapped_libraries():
+    """The shared objects of this repository mapped into this process."""
+    try:
+        maps = open("/proc/self/maps").read().split("\n")
+    except OSError:
+        return None
+    root = os.path.realpath(ROOT)
+    found = set()
+    for ln in maps:
+        path = ln.split()[-1] if ln.split() else ""
+        if path.startswith(root) and path.endswith(".so"):
+            found.add(os.path.relpath(path, root))
+    return sorted(found)
+
+
+def cpu_baseline_sample(single_thread=True):
+    """The oracle on one full frame with every host core, and (bounded: one
+    frame each) with one thread, the parity order of render.Workers(1)."""
     threads = os.cpu_count() or 1
-    s, cam = workload()
-    opts = frame_opts(s, cam)
-    flat = render.FlatScene(s)
-    fd = render.FrameDesc(opts, shadow_cams(opts))
-    state = np.zeros((3, SHADOW[1], SHADOW[0]), np.float32)
-    out = render.Outputs(W, H, ("rgba",))
+    frame = oracle_frame(threads, ("rgba",))
     t0 = time.perf_counter()
-    oracle.render(flat.desc(), fd.desc, out.desc, shadow_state=state, threads=threads)
+    frame()
     dt = time.perf_counter() - t0
-    return {"value": N_TRIS / dt / 1e6, "unit": "Mtri/s", "cores": threads, "kind": "port",
-            "sample": "1 full frame of the workload (C++ restatement of the Go CPU renderer, row-band threads)"}
+    out = {"value": N_TRIS / dt / 1e6, "unit": "Mtri/s", "cores": threads, "kind": "port",
+           "sample": "1 full frame of the workload (C++ restatement of the Go CPU renderer, row-band threads)"}
+    if single_thread:
+        one = oracle_frame(1, ("rgba",))
+        t0 = time.perf_counter()
+        one()
+        d1 = time.perf_counter() - t0
+        out["single_thread"] = {"value": N_TRIS / d1 / 1e6, "unit": "Mtri/s", "cores": 1, "s_per_frame": d1}
+    return out
 
 
 def max_over_ranks(ms, world, device):
@@ -665,10 +709,7 @@ def main():
         line = {"metric": "1080p Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "sphere_field_1M_1080p", "n_tris": N_TRIS, "width": W, "height": H,
-                           "shadow_maps": "2 x 2048^2 (point + directional)", "ao": True, "gamma": True,
-                           "l2": "inputs larger than L2 (136 MB triangle soup per frame)",
-                           "parallelism": f"replicas x{world}"},
+                "config": bench_config(world),
                 "frames_per_s": world * 1e3 / ms,
                 "e2e": {"value": job_throughput(N_TRIS, world, ems), "unit": "Mtri/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "ms_per_step": ems},

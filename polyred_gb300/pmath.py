@@ -14,6 +14,20 @@ from . import native
 
 F32 = np.float32
 
+# Another implementation of the six matrix functions below (same names and
+# results), or None for the library's C helpers.
+_backend = None
+
+
+def set_backend(backend):
+    """Route mat4_mul, mat4_inv, view_matrix, perspective_matrix,
+    orthographic_matrix and shadow_camera through `backend` (a module or
+    object with functions of those names), or back to the library with
+    None. A process that must not load the library uses this to build
+    scenes and frames with a CPU implementation of the same arithmetic."""
+    global _backend
+    _backend = backend
+
 
 def _fp(a):
     a = np.ascontiguousarray(a, dtype=np.float32)
@@ -26,6 +40,8 @@ def identity():
 
 def mat4_mul(a, b):
     """Mat4.MulM (math/mat4.go:201-220): a * b, row-major 16 floats."""
+    if _backend is not None:
+        return _backend.mat4_mul(a, b)
     lib = native.load()
     a, pa = _fp(a)
     b, pb = _fp(b)
@@ -35,6 +51,8 @@ def mat4_mul(a, b):
 
 
 def mat4_inv(m):
+    if _backend is not None:
+        return _backend.mat4_inv(m)
     lib = native.load()
     m, pm = _fp(m)
     out, po = _fp(np.zeros(16, np.float32))
@@ -44,6 +62,8 @@ def mat4_inv(m):
 
 def view_matrix(pos, target, up):
     """camera.ViewMatrix (camera/camera.go:42-53)."""
+    if _backend is not None:
+        return _backend.view_matrix(pos, target, up)
     lib = native.load()
     a, pa = _fp(pos)
     b, pb = _fp(target)
@@ -54,6 +74,8 @@ def view_matrix(pos, target, up):
 
 
 def perspective_matrix(fov, aspect, near, far):
+    if _backend is not None:
+        return _backend.perspective_matrix(fov, aspect, near, far)
     lib = native.load()
     out, po = _fp(np.zeros(16, np.float32))
     native.check(lib.pr_perspective_matrix(float(F32(fov)), float(F32(aspect)), float(F32(near)), float(F32(far)), po))
@@ -61,6 +83,8 @@ def perspective_matrix(fov, aspect, near, far):
 
 
 def orthographic_matrix(left, right, bottom, top, near, far):
+    if _backend is not None:
+        return _backend.orthographic_matrix(left, right, bottom, top, near, far)
     lib = native.load()
     out, po = _fp(np.zeros(16, np.float32))
     vals = [float(F32(v)) for v in (left, right, bottom, top, near, far)]
@@ -69,6 +93,8 @@ def orthographic_matrix(left, right, bottom, top, near, far):
 
 
 def shadow_camera(light_pos, center, cam_view, cam_proj):
+    if _backend is not None:
+        return _backend.shadow_camera(light_pos, center, cam_view, cam_proj)
     lib = native.load()
     a, pa = _fp(light_pos)
     b, pb = _fp(center)
