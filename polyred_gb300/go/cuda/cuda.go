@@ -32,6 +32,7 @@ const (
 	ErrUnsupported = -8
 	ErrNoDevice    = -9
 	ErrSingular    = -10
+	ErrFatal       = -11
 )
 
 const (
@@ -197,8 +198,27 @@ func load() error {
 		purego.RegisterLibFunc(&prDeviceAlloc, lib, "pr_device_alloc")
 		purego.RegisterLibFunc(&prDeviceFree, lib, "pr_device_free")
 		purego.RegisterLibFunc(&prDeviceRead, lib, "pr_device_read")
+		for _, f := range registerExtra {
+			if err := f(lib); err != nil {
+				loadErr = err
+				return
+			}
+		}
 	})
 	return loadErr
+}
+
+// registerExtra binds the entry points of the binding's other files (diff.go).
+var registerExtra []func(lib uintptr) error
+
+// register binds C function name of lib to the Go function variable fptr.
+func register(fptr any, lib uintptr, name string) error {
+	sym, err := purego.Dlsym(lib, name)
+	if err != nil {
+		return fmt.Errorf("cuda: %s: %w", name, err)
+	}
+	purego.RegisterFunc(fptr, sym)
+	return nil
 }
 
 // Error is a non-OK status with the library's detail message.
