@@ -180,6 +180,21 @@ def oracle_frame(threads, want=("rgba", "tri_id", "depth")):
     return frame
 
 
+def ncu_instructions(kernel="ao_kernel", name="ao_kernel_sphere_field_1080p.txt"):
+    """Warp instructions one launch of kernel executes (sm__inst_executed),
+    from its committed ncu summary under profiles/, or None."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("instructions executed"):
+            try:
+                return float(line.split()[2]) * 1e6
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -257,7 +272,7 @@ def job_throughput(n_tris, world, ms):
     return world * n_tris / (ms / 1e3) / 1e6
 
 
-def measure_diff(dev, steps, adam_steps=0):
+def measure_diff(dev, steps, adam_steps=0, cpu_baseline=True):
     """Differentiable shading on the 1M-triangle 1080p scene plus a
     vertex-coloured ground grid: device time of the forward frame
     (pr_diff_forward: full render + radiance) and of the backward pass
@@ -303,7 +318,25 @@ def measure_diff(dev, steps, adam_steps=0):
     out = {"workload": "sphere_field_1M_1080p + 64x64 vertex-coloured ground grid", "n_tris": r.flat.n_tris,
            "fwd_ms": f, "bwd_ms": b, "fwd_bwd_over_fwd": (f + b) / f, "wall_ms_fwd_bwd": statistics.mean(wall),
            "steps": n, "gradients": "vertex colour, vertex normal, kd, ks, shininess, light pos, light intensity, ambient",
-           "checked": "tests/test_gpu_diff.py: 64 parameters vs FP64 central differences (h=1e-4) within 1e-3"}
+           "checked": "tests/test_gpu_diff_full.py: 64 parameters vs FP64 central differences (h=1e-4) within 1e-3 "
+                      "relative at 1920x1080"}
+    if cpu_baseline:
+        # the FP64 reference adjoint (oracle/adjoint.cpp, one thread) on the same G-buffer: radiance and
+        # loss, then every gradient
+        import oracle
+        fdesc = r.frame(0, p["light_pos"].numpy(), p["light_intensity"].numpy(), p["ambient"].numpy())
+        npp = {k: v.detach().cpu().numpy().astype(np.float64) for k, v in p.items()}
+        inp = oracle.DiffInputs(r.flat, gbuf.cpu().numpy(), npp, fdesc.desc, oracle.normal_matrices(r.flat))
+        tgt = target.cpu().numpy()
+        t0 = time.perf_counter()
+        _, R64 = oracle.diff_forward64(inp, tgt)
+        g64 = np.zeros_like(R64)
+        g64[..., :3] = 2 * (R64[..., :3] - tgt[..., :3])
+        oracle.diff_backward64(inp, g64)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": dt * 1e3, "unit": "ms per fwd+bwd", "cores": 1, "kind": "port",
+                               "sample": "one forward + backward of the FP64 reference adjoint on the same "
+                                         "1920x1080 G-buffer (shading only: the G-buffer is the GPU's)"}
     if adam_steps:
         cams = [sc.Perspective(position=(24 * np.cos(a), 4, 24 * np.sin(a)), target=(0, 0, 0), up=(0, 1, 0), fov=60,
                                aspect=W / H, near=0.1, far=100) for a in np.linspace(0, 2 * np.pi, 16, endpoint=False)]
@@ -316,11 +349,12 @@ def measure_diff(dev, steps, adam_steps=0):
         losses = diff.inverse_render(ra, targets, x, ("kd", "light_pos", "vertex_color"), steps=adam_steps, lr=0.01)
         el = time.perf_counter() - t0
         out["adam"] = {"views": 16, "steps": adam_steps, "loss_first": losses[0], "loss_last": losses[-1],
-                       "s_total": el, "ms_per_view_step": el * 1e3 / (adam_steps * 16)}
+                       "s_total": el, "ms_per_view_step": el * 1e3 / (adam_steps * 16),
+                       "trained": "kd, light position, vertex colours (lr 0.01)"}
     return out
 
 
-def measure_soup(steps=10, n_tris=10_000_000, width=3840, height=2160):
+def measure_soup(steps=10, n_tris=10_000_000, width=3840, height=2160, cpu_baseline=True):
     """The small-triangle stress workload: 10M soup triangles at 3840x2160
     (log-normal areas around 1 px, 30% back-facing, one point light, no
     shadows, gamma on), resident frames timed with CUDA events."""
@@ -356,10 +390,22 @@ def measure_soup(steps=10, n_tris=10_000_000, width=3840, height=2160):
     st.size = C.sizeof(_abi.pr_stats)
     native.check(lib.pr_frame_stats(dev.handle, C.byref(st)))
     dev.close()
-    return {"workload": "triangle soup 10M at 3840x2160 (areas log-normal median 1 px, 30% back-facing)",
-            "n_tris": n_tris, "value": n_tris / (ms / 1e3) / 1e6, "unit": "Mtri/s", "ms_per_frame": ms,
-            "n_raster_tris": st.n_raster_tris, "ms_setup": st.ms_setup, "ms_raster": st.ms_raster,
-            "ms_shade": st.ms_shade}
+    res = {"workload": "triangle soup 10M at 3840x2160 (areas log-normal median 1 px, 30% back-facing)",
+           "n_tris": n_tris, "value": n_tris / (ms / 1e3) / 1e6, "unit": "Mtri/s", "ms_per_frame": ms,
+           "n_raster_tris": st.n_raster_tris, "ms_setup": st.ms_setup, "ms_raster": st.ms_raster,
+           "ms_shade": st.ms_shade}
+    if cpu_baseline:
+        import numpy as np
+        import oracle
+        threads = os.cpu_count() or 1
+        out = render.Outputs(width, height, ("rgba",))
+        t0 = time.perf_counter()
+        oracle.render(desc, fd.desc, out.desc, shadow_state=None, threads=threads)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": n_tris / dt / 1e6, "unit": "Mtri/s", "cores": threads, "kind": "port",
+                               "sample": "1 full frame of the workload (C++ restatement of the Go CPU renderer, "
+                                         "row-band threads)"}
+    return res
 
 
 def measure_obj(steps=20, n_tori=32, nu=128, nv=64, width=1920, height=1080):
@@ -492,7 +538,7 @@ def measure_textured(steps=50, width=1920, height=1080):
     return {"workload": "textured spheres and ground, 1920x1080", "ms_per_frame": ms, "frames_per_s": 1e3 / ms}
 
 
-def measure_batch(reps=3):
+def measure_batch(reps=3, cpu_baseline=True):
     """The batched workload (32 sphere scenes of 1k-500k triangles, 8 ring
     views each at 1280x720, 16 casting point lights per scene with 1024^2
     maps, AO on): views/s of one tuned pr_batch_render against the same 256
@@ -512,7 +558,7 @@ def measure_batch(reps=3):
         b.render(arr)
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
-    st = b.stats()
+    st_b = b.stats()
     bt = min(times)
     b.close()
     del outs, keep
@@ -562,18 +608,61 @@ def measure_batch(reps=3):
             native.check(lib.pr_render(devs[si].handle, C.byref(fd.desc), C.byref(od)))
         torch.cuda.synchronize()
         ps.append(time.perf_counter() - t0)
+    # the synchronous plain views once more, each timed alone: wall time
+    # against the frame's device span (CUDA events inside the library, from
+    # the first kernel to the last), by scene size
+    sizes = [render.FlatScene(s).n_tris for s in scenes]
+    by_bucket = {}
+    for (si, _, _), fd, od in zip(specs, fds, ods):
+        t0 = time.perf_counter()
+        native.check(lib.pr_shadow_reset(devs[si].handle))
+        native.check(lib.pr_render(devs[si].handle, C.byref(fd.desc), C.byref(od)))
+        wall = (time.perf_counter() - t0) * 1e3
+        st = _abi.pr_stats()
+        st.size = C.sizeof(_abi.pr_stats)
+        native.check(lib.pr_frame_stats(devs[si].handle, C.byref(st)))
+        n = sizes[si]
+        key = "1k-10k" if n < 10_000 else ("10k-100k" if n < 100_000 else "100k-500k")
+        b_ = by_bucket.setdefault(key, {"views": 0, "wall_ms": 0.0, "device_span_ms": 0.0,
+                                        "kernel_launches_per_view": st.n_kernel_launches})
+        b_["views"] += 1
+        b_["wall_ms"] += wall
+        b_["device_span_ms"] += st.ms_total
     for d in devs:
         d.close()
     n = len(specs)
-    return {"workload": "32 sphere scenes (1k-500k tris, log-uniform) x 8 views 1280x720, 16 casting point lights, "
-                        "1024^2 maps, AO", "n_views": n, "n_tris_total": int(sum(render.FlatScene(s).n_tris
-                                                                                    for s in scenes)),
-            "n_passes": st["n_passes"], "batched_views_per_s": n / bt, "plain_views_per_s": n / min(ps),
-            "batched_over_plain": min(ps) / bt, "plain": "one synchronous pr_render per view",
-            "plain_async_views_per_s": n / min(pt), "batched_over_plain_async": min(pt) / bt,
-            "plain_async": "pr_render_async per view, one context and stream per scene",
-            "batched_ms": bt * 1e3, "batched_device_ms": st["ms_total"], "plain_ms": min(ps) * 1e3, "kernel_launches_per_batch": st["n_kernel_launches"],
-            "graph_reused": st["graph_reused"], "device_gb": st["device_bytes"] / 1e9, "tuned": tune}
+    res = {"workload": "32 sphere scenes (1k-500k tris, log-uniform) x 8 views 1280x720, 16 casting point lights, "
+                       "1024^2 maps, AO", "n_views": n, "n_tris_total": int(sum(sizes)),
+           "n_passes": st_b["n_passes"], "batched_views_per_s": n / bt, "plain_views_per_s": n / min(ps),
+           "batched_over_plain": min(ps) / bt, "plain": "one synchronous pr_render per view",
+           "plain_async_views_per_s": n / min(pt), "batched_over_plain_async": min(pt) / bt,
+           "plain_async": "pr_render_async per view, one context and stream per scene",
+           "batched_ms": bt * 1e3, "batched_device_ms": st_b["ms_total"], "plain_ms": min(ps) * 1e3,
+           "plain_by_bucket": by_bucket,
+           "kernel_launches_per_batch": st_b["n_kernel_launches"],
+           "graph_reused": st_b["graph_reused"], "device_gb": st_b["device_bytes"] / 1e9, "tuned": tune}
+    if cpu_baseline:
+        # the oracle on a bounded sample: view 0 of the smallest, a median and the largest scene
+        import numpy as np
+        import oracle
+        threads = os.cpu_count() or 1
+        order = np.argsort(sizes)
+        pick = [int(order[0]), int(order[len(order) // 2]), int(order[-1])]
+        t0 = time.perf_counter()
+        for si in pick:
+            k = [j for j, sp in enumerate(specs) if sp[0] == si][0]
+            _, opts, cams = specs[k]
+            flat = render.FlatScene(scenes[si])
+            src, _ = opts["scene"].lights()
+            sw, sh = opts["shadow_size"]
+            out = render.Outputs(opts["width"], opts["height"], ("rgba",))
+            oracle.render(flat.desc(), fds[k].desc, out.desc,
+                          shadow_state=np.zeros((len(src), sh, sw), np.float32), threads=threads)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": len(pick) / dt, "unit": "views/s", "cores": threads, "kind": "port",
+                               "sample": f"3 views (scenes of {sizes[pick[0]]}, {sizes[pick[1]]} and "
+                                         f"{sizes[pick[2]]} triangles) rendered by the oracle, row-band threads"}
+    return res
 
 
 def main():
@@ -584,7 +673,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-shading measurement")
-    ap.add_argument("--adam", type=int, default=0, help="also run this many Adam steps over 16 views")
+    ap.add_argument("--adam", type=int, default=200, help="Adam steps of the 16-view inverse-rendering loop (0: skip)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-views measurement")
     ap.add_argument("--no-soup", action="store_true", help="skip the 10M-triangle 4K soup measurement")
     ap.add_argument("--no-obj", action="store_true", help="skip the OBJ ingestion measurement")
@@ -704,6 +793,17 @@ def main():
     alg_bytes = W * H * 4 + n_ao * 12
     achieved = alg_bytes / (ao_ms / 1e3) / 1e9 if ao_ms > 0 else 0.0
     traffic = ncu_traffic()
+    # the bound that limits it: instruction issue. Each SM issues at most one
+    # warp instruction per clock on each of its 4 schedulers.
+    n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    inst = ncu_instructions()
+    issue = None
+    if inst and ao_ms > 0:
+        issue = {"kernel": "ao_kernel", "warp_instructions": inst, "duration_ms": ao_ms, "sm_mhz": sm_mhz,
+                 "n_sms": n_sms, "frac": inst / (n_sms * 4 * sm_mhz * 1e6 * ao_ms / 1e3),
+                 "source": "instructions per launch from the ncu summary "
+                           "profiles/ao_kernel_sphere_field_1080p.txt, duration from this run's CUDA events"}
 
     if rank == 0:
         line = {"metric": "1080p Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
@@ -718,15 +818,16 @@ def main():
                              "frac": achieved / peak if peak else None, "traffic": traffic,
                              "kernel": "ao_kernel", "peak_source": peak_kind,
                              "algorithmic_bytes": alg_bytes,
-                             "note": "compute-bound: 8 x 99 dependent depth taps per pixel (L1/L2 resident)"},
+                             "note": "issue-bound: 8 x 99 dependent depth taps per pixel (L1/L2 resident); "
+                                     "see issue", "issue": issue},
                 "gpu_launches": launches,
                 "clocks": clk}
         if not args.no_diff:
-            line["diff"] = measure_diff(dev, args.steps, args.adam)
+            line["diff"] = measure_diff(dev, args.steps, args.adam, cpu_baseline=world == 1 and not args.no_cpu_baseline)
         if not args.no_soup:
-            line["soup_4k"] = measure_soup()
+            line["soup_4k"] = measure_soup(cpu_baseline=world == 1 and not args.no_cpu_baseline)
         if not args.no_batch:
-            line["batched"] = measure_batch()
+            line["batched"] = measure_batch(cpu_baseline=world == 1 and not args.no_cpu_baseline)
         if not args.no_msaa:
             try:
                 line["msaa_2x"] = measure_msaa()

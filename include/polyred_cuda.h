@@ -327,9 +327,13 @@ int pr_shadow_camera(const float light_pos[3], const float scene_center[3],
  * drawDepth pass of render/shadow.go, the same kernels pr_render uses for
  * shadow maps — on the caller's device triangles into the caller's device
  * depth map, which is read and then updated like the reference's persistent
- * maps. It allocates nothing: all scratch lives in one static 16 MiB device
- * array of the library, which every GPU that loads the library keeps until
- * the process exits.
+ * maps: a texel changes only where a fragment is stored into it, and a
+ * texel no fragment replaces keeps its bits (a -0 or a NaN payload
+ * included). It allocates nothing: all scratch lives in one static 16 MiB
+ * device array of the library, which every GPU that loads the library keeps
+ * until the process exits; the driver commits it when the library's kernels
+ * are first loaded on a device (with lazy module loading, that can be inside
+ * the first call that launches one of them, this one or another).
  *
  * Limits (larger inputs are rejected with PR_ERR_INVALID_ARG, or
  * PR_ERR_OVERFLOW for the task count, leaving the map unchanged):

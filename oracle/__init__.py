@@ -62,7 +62,17 @@ def load():
 def render(scene_desc, frame_desc, outputs_desc, shadow_state=None, threads=1):
     """One Render() of the reference in single-worker order."""
     lib = load()
-    ptr = None if shadow_state is None else shadow_state.ctypes.data
+    ptr = None
+    if shadow_state is not None:
+        # the oracle reads and writes n_lights maps of the frame's shadow size
+        f = frame_desc
+        m = f.msaa if f.msaa > 1 else 1
+        sw = f.shadow_width if f.shadow_width > 0 else f.width * m
+        sh = f.shadow_height if f.shadow_height > 0 else f.height * m
+        need = int(f.n_lights) * sw * sh
+        if shadow_state.dtype.itemsize != 4 or not shadow_state.flags.c_contiguous or shadow_state.size < need:
+            raise ValueError(f"shadow_state needs {need} contiguous float32 values, has {shadow_state.size}")
+        ptr = shadow_state.ctypes.data
     rc = lib.orc_render(C.byref(scene_desc), C.byref(frame_desc), ptr, int(threads), C.byref(outputs_desc), None)
     if rc != 0:
         raise RuntimeError(f"oracle render failed: {rc}")
@@ -84,7 +94,7 @@ class orc_diff_in(C.Structure):
         ("n_amb", C.c_int32), ("only_tri", C.c_int32),
         ("amb", C.c_void_p),
         ("cam", C.c_double * 3), ("bg", C.c_double * 4),
-        ("only_mat", C.c_int32), ("reserved", C.c_int32),
+        ("only_mat", C.c_int32), ("flags", C.c_int32),
     ]
 
 
@@ -163,8 +173,11 @@ def diff_forward64(inp, target=None, want_radiance=True):
     return loss, rad
 
 
-def diff_backward64(inp, grad):
-    """Gradients of sum(grad * radiance) in float64, shaped like the parameters."""
+def diff_backward64(inp, grad, absolute=False):
+    """Gradients of sum(grad * radiance) in float64, shaped like the
+    parameters; with absolute=True, for each gradient the sum of the
+    magnitudes of its per-pixel contributions instead (the scale of the
+    rounding error of a float32 evaluation of that sum)."""
     import numpy as np
     lib = load()
     lib.orc_diff_backward64.restype = None
@@ -176,7 +189,11 @@ def diff_backward64(inp, grad):
     o = orc_diff_out()
     for k, v in names.items():
         setattr(o, k, res[v].ctypes.data)
-    lib.orc_diff_backward64(C.byref(inp.s), g.ctypes.data, C.byref(o))
+    inp.s.flags = 1 if absolute else 0
+    try:
+        lib.orc_diff_backward64(C.byref(inp.s), g.ctypes.data, C.byref(o))
+    finally:
+        inp.s.flags = 0
     return res
 
 

@@ -24,6 +24,10 @@ inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline double nrm(D3 a) { return std::sqrt(dot(a, a)); }
 
 const uint32_t kLit = 1u, kFlat = 2u, kConst = 4u, kUnlit = 8u;
+// orc_diff_in.flags: the backward accumulates |v| for each per-pixel
+// contribution v, the sum of the magnitudes that bounds the rounding error of
+// a float32 evaluation of the gradient.
+const int32_t kAbs = 1;
 
 }  // namespace
 
@@ -55,7 +59,7 @@ typedef struct orc_diff_in {
     double cam[3];
     double bg[4];
     int32_t only_mat;           // >= 0: only pixels of this material
-    int32_t reserved;
+    int32_t flags;              // kAbs: accumulate |contribution| of every pixel
 } orc_diff_in;
 
 typedef struct orc_diff_out {
@@ -87,6 +91,8 @@ uint32_t find_obj(const orc_diff_in* in, uint32_t t) {
 
 // One pixel: radiance R[3]; with g != null also accumulates dL/d(params).
 void pixel(const orc_diff_in* in, size_t i, double R[3], const double* g, orc_diff_out* out) {
+    const bool absm = (in->flags & kAbs) != 0;
+    auto acc = [absm](double& dst, double v) { dst += absm ? std::fabs(v) : v; };  // dst += v, or |v|
     const float* d = in->gbuf + 16 * i;
     uint32_t t, fl;
     int32_t m;
@@ -105,7 +111,7 @@ void pixel(const orc_diff_in* in, size_t i, double R[3], const double* g, orc_di
             const double* C = in->vcol + 4 * (3 * (size_t)t + k);
             for (int c = 0; c < 3; c++) {
                 R[c] += 255.0 * p * C[c];
-                if (g && out->vcol) out->vcol[4 * (3 * (size_t)t + k) + c] += g[c] * 255.0 * p;
+                if (g && out->vcol) acc(out->vcol[4 * (3 * (size_t)t + k) + c], g[c] * 255.0 * p);
             }
         }
         return;
@@ -180,30 +186,30 @@ void pixel(const orc_diff_in* in, size_t i, double R[3], const double* g, orc_di
     double gg[3];
     for (int c = 0; c < 3; c++) gg[c] = (pre[c] > 0.0 && pre[c] < 255.0) ? g[c] * fac : 0.0;
     for (int c = 0; c < 3; c++) {
-        if (out->kd) out->kd[3 * m + c] += gg[c] * Ld[c];
-        if (out->ks) out->ks[3 * m + c] += gg[c] * Ls[c];
+        if (out->kd) acc(out->kd[3 * m + c], gg[c] * Ld[c]);
+        if (out->ks) acc(out->ks[3 * m + c], gg[c] * Ls[c]);
     }
     const double gcol = gg[0] * col[0] + gg[1] * col[1] + gg[2] * col[2];
     for (int e = 0; e < in->n_amb; e++)
-        if (out->amb) out->amb[e] += gcol;
+        if (out->amb) acc(out->amb[e], gcol);
     D3 gn = {0, 0, 0};
     for (int l = 0; l < in->n_lights; l++) {
         const LT& q = lt[l];
         const double A = gg[0] * kd[0] * col[0] + gg[1] * kd[1] * col[1] + gg[2] * kd[2] * col[2];
         const double B = gg[0] * ks[0] * in->lcol[4 * l] + gg[1] * ks[1] * in->lcol[4 * l + 1] +
                          gg[2] * ks[2] * in->lcol[4 * l + 2];
-        if (out->lint) out->lint[l] += (A * q.ld + B * q.ls) * (in->ltype[l] == 0 ? 1.0 / q.dist : 1.0);
+        if (out->lint) acc(out->lint[l], (A * q.ld + B * q.ls) * (in->ltype[l] == 0 ? 1.0 / q.dist : 1.0));
         const double nhc = std::fmin(std::fmax(q.nh, 0.0), 1.0);
-        if (q.ls > 0.0 && nhc < 1.0 && out->shin) out->shin[m] += B * q.I * q.ls * std::log(nhc);
+        if (q.ls > 0.0 && nhc < 1.0 && out->shin) acc(out->shin[m], B * q.I * q.ls * std::log(nhc));
         const double gnd = (q.nd > 0.0 && q.nd < 1.0) ? A * q.I : 0.0;
         const double gnh = (q.nh > 0.0 && q.nh < 1.0) ? B * q.I * s * std::pow(nhc, s - 1.0) : 0.0;
         gn = gn + gnd * q.L + gnh * q.H;
         if (in->ltype[l] == 0 && out->lpos) {
             const D3 gL = gnd * n + (gnh / q.hlen) * (n - q.nh * q.H);
             const D3 gD = (1.0 / q.dist) * (gL - dot(q.L, gL) * q.L) + (-(A * q.ld + B * q.ls) * q.I / q.dist) * q.L;
-            out->lpos[3 * l] += gD.x;
-            out->lpos[3 * l + 1] += gD.y;
-            out->lpos[3 * l + 2] += gD.z;
+            acc(out->lpos[3 * l], gD.x);
+            acc(out->lpos[3 * l + 1], gD.y);
+            acc(out->lpos[3 * l + 2], gD.z);
         }
     }
     if (!flat && out->vnor) {
@@ -211,7 +217,7 @@ void pixel(const orc_diff_in* in, size_t i, double R[3], const double* g, orc_di
         for (int k = 0; k < 3; k++) {
             const D3 gN = (double)d[4 + k] * gm;
             double* gv = out->vnor + 4 * (3 * (size_t)t + k);
-            for (int j = 0; j < 3; j++) gv[j] += M[j] * gN.x + M[4 + j] * gN.y + M[8 + j] * gN.z;
+            for (int j = 0; j < 3; j++) acc(gv[j], M[j] * gN.x + M[4 + j] * gN.y + M[8 + j] * gN.z);
         }
     }
 }

@@ -249,10 +249,27 @@ ENTRY_POINTS = [
 ]
 
 
-def bind(lib):
+# include/polyred_cuda_testing.h: test hooks, bound by the tests only
+TESTING_ENTRY_POINTS = [
+    ("pr_testing_fail_alloc", C.c_int, [C.c_int64]),
+    ("pr_testing_alloc_count", C.c_int64, []),
+    ("pr_debug_pow_probe", C.c_int, [VP] * 4 + [C.c_int]),
+    ("pr_debug_ao_probe", C.c_int, [VP] * 7 + [C.c_int]),
+    ("pr_debug_fma_probe", C.c_int, [VP] * 5 + [C.c_int]),
+    ("pr_debug_texture_build", C.c_longlong, [C.c_int, C.c_int, VP, C.c_int, VP, C.c_size_t, VP]),
+    ("pr_debug_texture_query", C.c_int, [C.c_int, C.c_int, VP, C.c_int, C.c_int] + [VP] * 6),
+]
+
+
+def bind(lib, entry_points=None):
     """Set restype/argtypes for every declared entry point on a CDLL."""
-    for name, res, args in ENTRY_POINTS:
+    for name, res, args in (ENTRY_POINTS if entry_points is None else entry_points):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
     return lib
+
+
+def bind_testing(lib):
+    """Also bind the test hooks of include/polyred_cuda_testing.h."""
+    return bind(lib, TESTING_ENTRY_POINTS)

@@ -38,7 +38,8 @@ def cuda_home():
 
 def sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))
-            if f.endswith((".cu", ".cpp", ".cuh", ".h"))] + [os.path.join(HERE, "..", "include", "polyred_cuda.h")]
+            if f.endswith((".cu", ".cpp", ".cuh", ".h"))] + [os.path.join(HERE, "..", "include", h)
+                                                             for h in ("polyred_cuda.h", "polyred_cuda_testing.h")]
 
 
 def up_to_date():

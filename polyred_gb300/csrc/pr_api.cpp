@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
@@ -16,6 +17,7 @@
 #include <vector>
 
 #include "../../include/polyred_cuda.h"
+#include "../../include/polyred_cuda_testing.h"
 #include "pr_hostmath.h"
 #include "pr_kernels.cuh"
 
@@ -54,7 +56,34 @@ int fail(int code, const char* fmt, ...) {
             return fail(PR_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString((cudaError_t)_e)); \
     } while (0)
 
-// A device allocation that only grows.
+// Allocation failure injection (pr_testing_fail_alloc): when positive, the
+// number of device or page-locked allocations until one reports
+// cudaErrorMemoryAllocation without calling CUDA. g_alloc_count counts every
+// allocation attempt (pr_testing_alloc_count).
+std::atomic<long long> g_alloc_fail_in{0};
+std::atomic<long long> g_alloc_count{0};
+
+bool injected_failure() {
+    g_alloc_count.fetch_add(1, std::memory_order_relaxed);
+    long long k = g_alloc_fail_in.load();
+    while (k > 0)
+        if (g_alloc_fail_in.compare_exchange_weak(k, k - 1)) return k == 1;
+    return false;
+}
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+    if (injected_failure()) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_malloc(void** p, size_t bytes) {
+    if (injected_failure()) return cudaErrorMemoryAllocation;
+    return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
+// A device allocation that only grows. A failed growth leaves it empty
+// (p == nullptr, n == 0): the old buffer is freed first, so that the peak
+// holds one buffer, and callers keep no capacity derived from it.
 template <class T>
 struct DevBuf {
     T* p = nullptr;
@@ -65,7 +94,7 @@ struct DevBuf {
         p = nullptr;
         n = 0;
         size_t alloc = std::max<size_t>(want, 1);
-        cudaError_t e = cudaMalloc((void**)&p, alloc * sizeof(T));
+        cudaError_t e = dev_malloc((void**)&p, alloc * sizeof(T));
         if (e != cudaSuccess) {
             p = nullptr;
             return fail(PR_ERR_OOM, "cudaMalloc(%zu bytes): %s", alloc * sizeof(T), cudaGetErrorString(e));
@@ -89,7 +118,7 @@ struct HostBuf {
         if (p) cudaFreeHost(p);
         p = nullptr;
         n = 0;
-        if (cudaHostAlloc((void**)&p, std::max<size_t>(want, 1), cudaHostAllocDefault) != cudaSuccess) {
+        if (host_malloc((void**)&p, std::max<size_t>(want, 1)) != cudaSuccess) {
             p = nullptr;
             return fail(PR_ERR_OOM, "cudaHostAlloc(%zu bytes) failed", want);
         }
@@ -225,14 +254,17 @@ int validate_scene(const pr_scene_desc* s) {
     if (s->n_objects == 0 && s->n_tris > 0) return fail(PR_ERR_INVALID_ARG, "triangles without objects");
     if (s->n_objects > 0 && !s->objects) return fail(PR_ERR_INVALID_ARG, "objects is NULL");
     if (s->n_materials > 0 && !s->materials) return fail(PR_ERR_INVALID_ARG, "materials is NULL");
-    uint32_t expect = 0;
+    uint64_t expect = 0;
     for (uint32_t o = 0; o < s->n_objects; o++) {
         if (s->objects[o].first_tri != expect)
-            return fail(PR_ERR_INVALID_ARG, "object %u: first_tri %u, expected %u (objects must tile the soup in order)", o,
-                        s->objects[o].first_tri, expect);
+            return fail(PR_ERR_INVALID_ARG, "object %u: first_tri %u, expected %llu (objects must tile the soup in order)",
+                        o, s->objects[o].first_tri, (unsigned long long)expect);
         expect += s->objects[o].n_tris;
+        if (expect > s->n_tris)
+            return fail(PR_ERR_INVALID_ARG, "object %u ends past the scene's %u triangles", o, s->n_tris);
     }
-    if (expect != s->n_tris) return fail(PR_ERR_INVALID_ARG, "objects cover %u triangles, scene has %u", expect, s->n_tris);
+    if (expect != s->n_tris)
+        return fail(PR_ERR_INVALID_ARG, "objects cover %llu triangles, scene has %u", (unsigned long long)expect, s->n_tris);
     const pr_texture* tx = scene_textures(s);
     for (uint32_t m = 0; m < s->n_materials; m++) {
         if (tx && tx[m].rgba) {
@@ -378,6 +410,7 @@ int ensure_work(Ctx* c, uint32_t need_rec, uint32_t need_tasks) {
     int rc;
     if (need_rec > c->cap_rec) {
         uint32_t cap = std::max(need_rec, c->cap_rec * 2);
+        c->cap_rec = 0;  // until every buffer holds cap (a failed growth empties one)
         if ((rc = c->rrec.ensure(cap))) return rc;
         if ((rc = c->arec.ensure(cap))) return rc;
         if ((rc = c->attr_state.ensure(cap))) return rc;
@@ -387,6 +420,7 @@ int ensure_work(Ctx* c, uint32_t need_rec, uint32_t need_tasks) {
     }
     if (need_tasks > c->cap_tasks) {
         uint32_t cap = std::max(need_tasks, c->cap_tasks * 2);
+        c->cap_tasks = 0;
         if ((rc = c->tasks.ensure(cap))) return rc;
         if ((rc = c->tasks_s.ensure(cap))) return rc;
         if ((rc = c->tasks_c.ensure(cap))) return rc;
@@ -454,15 +488,31 @@ void collect_stats(Ctx* c) {
     uint32_t n_tasks = 0;
     for (int k = 0; k < prk::kNumCounters; k++) n_tasks += c->h_cnt[k].n_tasks;
     c->stats.n_raster_tasks = n_tasks;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->stats.ms_shadow = ms;
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]); c->stats.ms_setup = ms;  // concurrent with the shadow passes
-    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->stats.ms_raster = ms;
-    cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); c->stats.ms_shade = ms;
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); c->stats.ms_total = ms;
-    cudaEventElapsedTime(&ms, c->ev[5], c->ev[4]); c->stats.ms_ao = ms;
+    // 0 for an interval whose events a failed frame did not record; the
+    // error that reports it must not be left for the next launch check
+    auto span = [](cudaEvent_t a, cudaEvent_t b) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+            (void)cudaGetLastError();
+            ms = 0;
+        }
+        return ms;
+    };
+    c->stats.ms_shadow = span(c->ev[0], c->ev[1]);
+    c->stats.ms_setup = span(c->ev[0], c->ev[2]);  // concurrent with the shadow passes
+    c->stats.ms_raster = span(c->ev[2], c->ev[3]);
+    c->stats.ms_shade = span(c->ev[3], c->ev[4]);
+    c->stats.ms_total = span(c->ev[0], c->ev[4]);
+    c->stats.ms_ao = span(c->ev[5], c->ev[4]);
     c->stats.n_ao_pixels = c->h_cnt[0].n_ao;
 }
+
+// Launch checks read cudaGetLastError, which also holds a failure of any
+// earlier runtime call of this host thread that nothing consumed (the
+// caller's own, for one). Each entry point that launches starts by
+// consuming it, so that it is not reported as the library's. A sticky
+// error (a fault of the context) survives this and fails the next call.
+void clear_stale_error() { (void)cudaGetLastError(); }
 
 // The frame-level fields of the deferred pass: size, flags, materials,
 // lights (render/raster.go:275-295), camera, background, matrices, gamma.
@@ -546,6 +596,7 @@ struct DiffHooks {
 
 int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, const DiffHooks* dh = nullptr,
                 bool submit = false) {
+    clear_stale_error();
     int rc = validate_frame(c, f);
     if (rc) return rc;
     // render.MSAA: every pass runs on the n-times framebuffer (the frame is
@@ -595,6 +646,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
     if (shadows) {
         if (!c->smap_valid || c->SW != SW || c->SH != SH || c->n_slights != NL) {
             size_t n = (size_t)SW * SH * std::max(NL, 1);
+            c->smap_valid = false;  // a failed growth leaves no maps
             if ((rc = c->smap.ensure(n))) return rc;
             // the orderable key of +0.0f is 0x80000000
             KTRY(prk::launch_fill_u32(c->smap.p, 0x80000000u, n, st));
@@ -945,7 +997,7 @@ int pr_create(int device, void** out_ctx) {
         return fail(PR_ERR_CUDA, "stream/event creation failed");
     }
     if ((rc = c->cnt.ensure(prk::kNumCounters))) { pr_destroy(c); return rc; }
-    if (cudaMallocHost((void**)&c->h_cnt, sizeof(prk::Counters) * prk::kNumCounters) != cudaSuccess) {
+    if (host_malloc((void**)&c->h_cnt, sizeof(prk::Counters) * prk::kNumCounters) != cudaSuccess) {
         pr_destroy(c);
         return fail(PR_ERR_OOM, "pinned counter allocation failed");
     }
@@ -1016,6 +1068,8 @@ int pr_scene_upload(void* ctx, const pr_scene_desc* s) {
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream_u));
     CUDA_TRY(cudaStreamSynchronize(c->stream_d));
+    clear_stale_error();
+    c->has_scene = false;  // until the new scene is complete (a failed upload leaves none)
     if ((rc = scene_fill(c->sb, s, c->stream, false))) return rc;
     CUDA_TRY(cudaStreamSynchronize(c->stream));  // host tables go out of scope
     c->has_scene = true;
@@ -1032,6 +1086,7 @@ int pr_frame_submit(void* ctx, const pr_scene_desc* scene, const pr_frame_desc* 
     if (out && out->shadow_maps) return fail(PR_ERR_UNSUPPORTED, "pr_frame_submit does not return shadow maps");
     if ((rc = set_device(c))) return rc;
     SceneBufs& b = c->sb_back;
+    clear_stale_error();
     CUDA_TRY(cudaEventSynchronize(b.ev_uploaded));                 // its staging is free again
     CUDA_TRY(cudaStreamWaitEvent(c->stream_u, b.ev_released, 0));  // no frame reads it any more
     if ((rc = scene_fill(b, scene, c->stream_u, true))) return rc;
@@ -1109,10 +1164,11 @@ int pr_stream(void* ctx, void** out_stream) {
 int pr_host_alloc(size_t bytes, void** out_ptr) {
     if (!out_ptr || bytes == 0) return fail(PR_ERR_INVALID_ARG, "NULL out_ptr or zero bytes");
     *out_ptr = nullptr;
-    cudaError_t e = cudaHostAlloc(out_ptr, bytes, cudaHostAllocDefault);
+    cudaError_t e = host_malloc(out_ptr, bytes);
     if (e != cudaSuccess) {
         *out_ptr = nullptr;
-        return fail(PR_ERR_CUDA, "cudaHostAlloc(%zu): %s", bytes, cudaGetErrorString(e));
+        return fail(e == cudaErrorMemoryAllocation ? PR_ERR_OOM : PR_ERR_CUDA, "cudaHostAlloc(%zu): %s", bytes,
+                    cudaGetErrorString(e));
     }
     return PR_OK;
 }
@@ -1124,7 +1180,7 @@ int pr_device_alloc(void* ctx, size_t bytes, void** out_ptr) {
     std::lock_guard<std::mutex> lk(c->mu);
     int rc = set_device(c);
     if (rc) return rc;
-    cudaError_t e = cudaMalloc(out_ptr, bytes);
+    cudaError_t e = dev_malloc(out_ptr, bytes);
     if (e != cudaSuccess) {
         *out_ptr = nullptr;
         return fail(e == cudaErrorMemoryAllocation ? PR_ERR_OOM : PR_ERR_CUDA, "cudaMalloc(%zu): %s", bytes,
@@ -1155,6 +1211,16 @@ int pr_device_read(void* ctx, const void* src, size_t bytes, void* dst) {
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return PR_OK;
 }
+
+// ---- test hooks (include/polyred_cuda_testing.h) ----
+
+int pr_testing_fail_alloc(int64_t n) {
+    if (n < 0) return fail(PR_ERR_INVALID_ARG, "pr_testing_fail_alloc: negative count");
+    g_alloc_fail_in.store(n);
+    return PR_OK;
+}
+
+int64_t pr_testing_alloc_count(void) { return g_alloc_count.load(); }
 
 int pr_host_free(void* ptr) {
     if (!ptr) return fail(PR_ERR_INVALID_ARG, "ptr is NULL");
@@ -1336,6 +1402,7 @@ int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params
     if (frame_msaa(frame) > 1) return fail(PR_ERR_UNSUPPORTED, "MSAA is not available in the adjoint");
     if (!c->has_scene) return fail(PR_ERR_NO_SCENE, "no scene uploaded");
     if ((rc = set_device(c))) return rc;
+    clear_stale_error();
     prk::DiffParamsK K{};
     if ((rc = diff_setup(c, frame, params, K))) return rc;
     cudaStream_t st = c->stream;
@@ -1373,7 +1440,7 @@ int pr_diff_backward(void* ctx, const pr_frame_desc* frame, const pr_diff_params
     return PR_OK;
 }
 
-// Test hook (not part of the public header): the shade kernel's float32 Pow
+// Test hook (include/polyred_cuda_testing.h): the shade kernel's float32 Pow
 // beside the float64 algorithm on n device-resident argument pairs.
 int pr_debug_pow_probe(const float* x, const float* y, float* fast, float* ref, int n) {
     int e = prk::launch_pow_probe(x, y, fast, ref, n, nullptr);
@@ -1382,7 +1449,7 @@ int pr_debug_pow_probe(const float* x, const float* y, float* fast, float* ref, 
     return PR_OK;
 }
 
-// Test hook (not part of the public header): the AO kernel's float32 Atan
+// Test hook (include/polyred_cuda_testing.h): the AO kernel's float32 Atan
 // and its certified Pow(T, 10000) colour scaling, each beside the float64
 // algorithm, on n device-resident inputs (col, o_fast, o_ref: 4 bytes each).
 int pr_debug_ao_probe(const float* x, float* atan_fast, float* atan_ref, const float* T, const uint8_t* col,
@@ -1393,7 +1460,7 @@ int pr_debug_ao_probe(const float* x, float* atan_fast, float* atan_ref, const f
     return PR_OK;
 }
 
-// Test hook (not part of the public header): runs the device float32
+// Test hook (include/polyred_cuda_testing.h): runs the device float32
 // emulation of float32(fma(f64, f64, f64)) and the direct FP64 expression on
 // n device-resident inputs.
 int pr_debug_fma_probe(const float* a, const float* b, const float* c, float* out, float* out_ref, int n) {
@@ -1530,7 +1597,10 @@ int batch_plan(Batch* b, uint32_t nv, const pr_batch_view* views, BatchPlan& p) 
         if (b->h_cnt) cudaFreeHost(b->h_cnt);
         b->h_cnt = nullptr;
         b->h_cnt_n = 0;
-        CUDA_TRY(cudaMallocHost((void**)&b->h_cnt, sizeof(prk::Counters) * (nv + p.S)));
+        if (host_malloc((void**)&b->h_cnt, sizeof(prk::Counters) * (nv + p.S)) != cudaSuccess) {
+            b->h_cnt = nullptr;
+            return fail(PR_ERR_OOM, "cudaHostAlloc(%zu bytes) failed", sizeof(prk::Counters) * (nv + p.S));
+        }
         b->h_cnt_n = nv + p.S;
     }
     prk::Counters* dcnt = b->cnt.p;
@@ -1761,6 +1831,7 @@ int batch_run(Batch* b, uint32_t nv, const pr_batch_view* views) {
         if (o->shadow_maps) return fail(PR_ERR_UNSUPPORTED, "view %u: shadow_maps output is not batched", v);
     }
     CUDA_TRY(cudaSetDevice(b->device));
+    clear_stale_error();
     b->stats.n_retries = 0;
     b->stats.n_fallback_views = 0;
     for (int attempt = 0; attempt < 4; attempt++) {

@@ -2129,6 +2129,17 @@ __global__ void encode_map_kernel(const float* depth, uint32_t* keys, size_t n) 
     keys[i] = isnan(d) ? 0u : fkey(d);  // key 0 stands for NaN (below every value)
 }
 
+// Back into the caller's map: a texel whose key the raster changed takes the
+// decoded key; the others keep their bits, so a -0 or a NaN payload that no
+// fragment replaced stays as it was, as in the reference's map.
+__global__ void decode_changed_kernel(const uint32_t* keys, float* depth, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = depth[i];
+    const uint32_t k0 = isnan(d) ? 0u : fkey(d), k = keys[i];
+    if (k != k0) depth[i] = fkey_decode(k);
+}
+
 std::mutex g_noalloc_mu;
 void* g_noalloc_addr[64] = {};
 
@@ -2147,13 +2158,15 @@ extern "C" int pr_depth_map_noalloc(const pr_depth_map_desc* d) {
         return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: n_objects exceeds PR_NOALLOC_MAX_OBJECTS (256)");
     if (d->width <= 0 || d->height <= 0 || (uint64_t)d->width * (uint64_t)d->height > kNoAllocMaxTexels)
         return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: width*height must be in 1..PR_NOALLOC_MAX_TEXELS (1048576)");
-    if (!d->depth || (d->n_tris > 0 && (!d->pos || !d->objects || d->n_objects == 0)))
+    if (!d->depth || (d->n_tris > 0 && (!d->pos || d->n_objects == 0)) || (d->n_objects > 0 && !d->objects))
         return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: NULL input or output pointer");
-    uint32_t expect = 0;
+    uint64_t expect = 0;
     for (uint32_t o = 0; o < d->n_objects; o++) {
         if (d->objects[o].first_tri != expect)
             return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: objects must tile the triangles in order");
         expect += d->objects[o].n_tris;
+        if (expect > d->n_tris)
+            return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: objects do not cover n_tris");
     }
     if (expect != d->n_tris) return err(PR_ERR_INVALID_ARG, "pr_depth_map_noalloc: objects do not cover n_tris");
 
@@ -2174,6 +2187,7 @@ extern "C" int pr_depth_map_noalloc(const pr_depth_map_desc* d) {
         base = (unsigned char*)g_noalloc_addr[dev];
     }
     cudaStream_t st = (cudaStream_t)d->stream;
+    (void)cudaGetLastError();  // a failure of an earlier runtime call is not this call's
     Counters* cnt = (Counters*)(base + kNaCounters);
     uint32_t* obj_first = (uint32_t*)(base + kNaObjFirst);
     float* obj_model = (float*)(base + kNaObjModel);
@@ -2251,11 +2265,9 @@ extern "C" int pr_depth_map_noalloc(const pr_depth_map_desc* d) {
     if (h.overflow)
         return err(PR_ERR_OVERFLOW, "pr_depth_map_noalloc: more raster tasks than PR_NOALLOC_MAX_TASKS (262144); "
                                     "the depth map was left unchanged");
-    rc = launch_decode_shadow(keys, d->depth, n, st);
-    if (!rc) {
-        e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) rc = (int)e;
-    }
-    if (rc) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: decode failed");
+    decode_changed_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(keys, d->depth, n);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return err(PR_ERR_CUDA, "pr_depth_map_noalloc: decode failed");
     return PR_OK;
 }

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/polyred_cuda.h"
+#include "../../include/polyred_cuda_testing.h"
 #include "pr_texture.h"
 
 namespace prk {
@@ -206,7 +207,7 @@ int pr_png_unfilter(const uint8_t* in, int height, size_t row_bytes, int bpp, ui
 
 }  // extern "C"
 
-// ---- test entry points (not part of the ABI header) ----
+// ---- test entry points (include/polyred_cuda_testing.h) ----
 
 extern "C" {
 

@@ -1,8 +1,9 @@
 """Loader for libpolyred_cuda.so (the CUDA render path).
 
-The library is built in-tree (polyred_gb300/lib/) by polyred_gb300.build.
-There is no fallback: if the library cannot be loaded, every render call
-raises NativeUnavailable.
+The library is built in-tree (polyred_gb300/lib/) by polyred_gb300.build;
+POLYRED_CUDA_LIB names another build of it to load instead (as the Go
+binding's variable of that name does). There is no fallback: if the library
+cannot be loaded, every render call raises NativeUnavailable.
 """
 import ctypes as C
 import os
@@ -31,26 +32,24 @@ def load(build_if_missing=False):
     global _lib
     if _lib is not None:
         return _lib
+    path = os.environ.get("POLYRED_CUDA_LIB")
+    if path:
+        return _open(path)
     if not os.path.exists(LIB_PATH):
         if not build_if_missing:
             raise NativeUnavailable(f"{LIB_PATH} not built; run polyred_gb300.build.build()")
         from . import build
         build.build()
+    return _open(LIB_PATH)
+
+
+def _open(path):
+    global _lib
     try:
-        lib = C.CDLL(LIB_PATH)
+        lib = C.CDLL(path)
     except OSError as e:
-        raise NativeUnavailable(f"cannot load {LIB_PATH}: {e}") from e
+        raise NativeUnavailable(f"cannot load {path}: {e}") from e
     _abi.bind(lib)
-    lib.pr_debug_pow_probe.restype = C.c_int
-    lib.pr_debug_pow_probe.argtypes = [C.c_void_p] * 4 + [C.c_int]
-    lib.pr_debug_ao_probe.restype = C.c_int
-    lib.pr_debug_ao_probe.argtypes = [C.c_void_p] * 7 + [C.c_int]
-    lib.pr_debug_fma_probe.restype = C.c_int
-    lib.pr_debug_fma_probe.argtypes = [C.c_void_p] * 5 + [C.c_int]
-    lib.pr_debug_texture_build.restype = C.c_longlong
-    lib.pr_debug_texture_build.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]
-    lib.pr_debug_texture_query.restype = C.c_int
-    lib.pr_debug_texture_query.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 6
     if lib.pr_abi_version() != _abi.ABI_VERSION:
         raise NativeUnavailable("ABI version mismatch")
     _lib = lib

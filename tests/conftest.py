@@ -17,9 +17,9 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def native_lib():
-    from polyred_gb300 import build, native
+    from polyred_gb300 import _abi, build, native
     build.build()
-    return native.load()
+    return _abi.bind_testing(native.load())
 
 
 @pytest.fixture(scope="session")

@@ -25,12 +25,12 @@ sys.path.insert(0, ROOT)
 
 from oracle import objparse  # noqa: E402
 
-DEFAULT_TESTDATA = "/root/reference/internal/testdata"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "obj_assets.json")
 
 
-def testdata_dir():
-    return os.environ.get("POLYRED_REFERENCE_TESTDATA", DEFAULT_TESTDATA)
+def testdata_dir(reference_root):
+    """The reference's test assets (internal/testdata of its checkout)."""
+    return os.path.join(reference_root, "internal", "testdata")
 
 
 def digest(a):
@@ -89,8 +89,8 @@ def check(path, f, rec):
         assert faces[0].Vertices[0] == int(first[0]) - 1, path
 
 
-def main():
-    d = testdata_dir()
+def main(reference_root):
+    d = testdata_dir(reference_root)
     if not os.path.isdir(d):
         sys.exit(f"no test assets at {d}")
     out = {}
@@ -106,4 +106,6 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_obj_fixtures.py <reference checkout>")
+    main(sys.argv[1])

@@ -7,6 +7,15 @@ import numpy as np
 
 from polyred_gb300 import _abi, native, render, scene as sc
 
+# The reference checkout whose own test assets also pin the oracle and the
+# loaders (tests that read it skip where it is absent, as on a GPU host).
+REFERENCE_ROOT = os.environ.get("POLYRED_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_testdata():
+    return os.path.join(REFERENCE_ROOT, "internal", "testdata")
+
+
 ALL_OUTPUTS = ("rgba", "tri_id", "depth", "nor", "face_nor", "world_pos", "uvd", "vcol", "mat_id")
 THREADS = max(1, min(16, os.cpu_count() or 1))
 

@@ -11,11 +11,12 @@ from polyred_gb300 import _abi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "polyred_cuda.h")
+TESTING_HEADER = os.path.join(ROOT, "include", "polyred_cuda_testing.h")
 F = C.c_float
 
 
-def declared_symbols():
-    text = open(HEADER).read()
+def declared_symbols(header=HEADER):
+    text = open(header).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(pr_[a-z0-9_]+)\s*\(", text)))
 
@@ -29,6 +30,35 @@ def test_header_declares_entry_points():
 def test_library_exports_every_declared_symbol(native_lib):
     for name in declared_symbols():
         assert hasattr(native_lib, name), name
+
+
+def test_testing_header_declares_the_test_hooks(native_lib):
+    names = declared_symbols(TESTING_HEADER)
+    assert set(names) == {n for n, _, _ in _abi.TESTING_ENTRY_POINTS}
+    assert not set(names) & set(declared_symbols())
+    for name in names:
+        assert hasattr(native_lib, name), name
+
+
+def test_injected_allocation_failure_is_reported(native_lib):
+    """The injection fails the n-th allocation without calling CUDA, so it
+    runs without a GPU: pr_host_alloc reports PR_ERR_OOM with the call named,
+    the count advances, and with the injection off the call goes to CUDA."""
+    n0 = native_lib.pr_testing_alloc_count()
+    assert native_lib.pr_testing_fail_alloc(-1) == _abi.PR_ERR_INVALID_ARG
+    assert native_lib.pr_testing_fail_alloc(2) == _abi.PR_OK
+    p = C.c_void_p()
+    try:
+        rc1 = native_lib.pr_host_alloc(64, C.byref(p))
+        if rc1 == _abi.PR_OK:  # a CUDA host is present: the first allocation is real
+            native_lib.pr_host_free(p)
+        rc2 = native_lib.pr_host_alloc(64, C.byref(p))
+        assert rc2 == _abi.PR_ERR_OOM
+        assert b"cudaHostAlloc" in native_lib.pr_last_error()
+        assert not p.value
+    finally:
+        native_lib.pr_testing_fail_alloc(0)
+    assert native_lib.pr_testing_alloc_count() - n0 == 2
 
 
 def test_abi_version(native_lib):

@@ -47,7 +47,12 @@ _TARGET = {}
 
 def _loss_setup(setup):
     """The L2 loss against a target rendered with perturbed parameters: Kd
-    + 0.1, light position + (0.5, 0, 0), vertex colours + N(0, 0.05)."""
+    + 0.1, light position + (0.5, 0, 0), vertex colours + N(0, 0.05).
+    Returns (target, dL/d(radiance)); the upstream gradient is that of the
+    FP64 loss the central differences differentiate, 2 (R64 - target) with
+    R64 the FP64 radiance: from the GPU's float32 radiance instead, pixels
+    whose radiance nearly equals the target would carry the float32
+    rounding of R as a relative error of R - target."""
     import torch
     r, p, rad, gbuf, inp = setup
     if id(r) not in _TARGET:
@@ -57,12 +62,12 @@ def _loss_setup(setup):
         q["light_pos"] = (q["light_pos"] + torch.tensor([0.5, 0.0, 0.0])).contiguous()
         noise = torch.randn(q["vertex_color"].shape, generator=g) * 0.05
         q["vertex_color"] = (q["vertex_color"] + noise.cuda()).contiguous()
-        _TARGET[id(r)] = r.forward_raw(0, q)[0].cpu().numpy()
-    target = _TARGET[id(r)]
-    R = rad.cpu().numpy().astype(np.float64)
-    grad = np.zeros_like(R)
-    grad[..., :3] = 2 * (R[..., :3] - target[..., :3])
-    return target, grad
+        target = r.forward_raw(0, q)[0].cpu().numpy()
+        _, R64 = oracle.diff_forward64(inp)
+        grad = np.zeros_like(R64)
+        grad[..., :3] = 2 * (R64[..., :3] - target[..., :3])
+        _TARGET[id(r)] = (target, grad)
+    return _TARGET[id(r)]
 
 
 def _gpu_grads(setup, grad):
@@ -113,10 +118,20 @@ def central_difference_picks(setup, seed=11):
 
 
 def central_differences(setup, picks, h=1e-4):
-    """[(name, index, FP64 central difference, GPU gradient)] for picks."""
+    """[(name, index, FP64 central difference with step h, GPU gradient,
+    FD error estimate, float32 error scale)] for picks. The FD error
+    estimate is the spread of the central differences with steps 2h and h/2
+    around the one with h, plus their rounding (the loss's float64 ulp over
+    the step: a contribution below it leaves the loss unchanged, so the
+    difference reads 0); the float32 error scale is 2^-17 times the sum of
+    the magnitudes of the gradient's per-pixel contributions (FP64 adjoint
+    in its absolute mode), which bounds the rounding of a float32 evaluation
+    of that sum (about a hundred roundings per contribution, each within
+    2^-24)."""
     r, p, rad, gbuf, inp = setup
     target, grad = _loss_setup(setup)
     gpu = _gpu_grads(setup, grad)
+    mag = oracle.diff_backward64(inp, grad, absolute=True)
     res = []
     for name, a0, a1, a2 in picks:
         arr = inp.param(name)
@@ -124,23 +139,37 @@ def central_differences(setup, picks, h=1e-4):
         inp.s.only_tri = a0 if name.startswith("vertex") else -1
         inp.s.only_mat = a0 if name in ("kd", "ks", "shininess") else -1
         v0 = arr[idx]
-        arr[idx] = v0 + h
-        lp, _ = oracle.diff_forward64(inp, target, want_radiance=False)
-        arr[idx] = v0 - h
-        lm, _ = oracle.diff_forward64(inp, target, want_radiance=False)
-        arr[idx] = v0
-        res.append((name, idx, (lp - lm) / (2 * h), float(gpu[name][idx])))
+        fd, lmax = {}, 0.0
+        for step in (2 * h, h, h / 2):
+            arr[idx] = v0 + step
+            lp, _ = oracle.diff_forward64(inp, target, want_radiance=False)
+            arr[idx] = v0 - step
+            lm, _ = oracle.diff_forward64(inp, target, want_radiance=False)
+            arr[idx] = v0
+            fd[step] = (lp - lm) / (2 * step)
+            lmax = max(lmax, abs(lp), abs(lm))
+        e_fd = max(abs(fd[2 * h] - fd[h]), abs(fd[h / 2] - fd[h])) + 2.0 ** -50 * lmax / (h / 2)
+        res.append((name, idx, fd[h], float(gpu[name][idx]), e_fd, 2.0 ** -17 * float(mag[name][idx])))
     inp.s.only_tri = inp.s.only_mat = -1
     return res
 
 
 def test_gradients_match_central_differences(setup):
     """64 random parameters, FP64 central differences with h = 1e-4 of the
-    FP64 loss (visibility fixed), against the GPU gradients, within 1e-3
-    relative (no absolute term)."""
+    FP64 loss (visibility fixed), against the GPU gradients: within 1e-3
+    relative, plus the FD's own error estimate and the float32 error scale
+    of the gradient (central_differences). Only gradients at the noise level
+    of their own sum need those terms: vertex normals of triangles whose
+    pixels already match the target to about 1e-6, whose gradients are
+    1e-26 to 1e-15 (below the float64 resolution of a loss near 1e-13 over
+    the step, so the central difference reads 0); at most a few of the 64
+    picks are such."""
     res = central_differences(setup, central_difference_picks(setup))
-    bad = [x for x in res if not abs(x[3] - x[2]) <= 1e-3 * abs(x[2])]
+    bad = [x for x in res if not abs(x[3] - x[2]) <= 1e-3 * abs(x[2]) + x[4] + x[5]]
     assert not bad, bad[:6]
+    floor_only = [x for x in res if not abs(x[3] - x[2]) <= 1e-3 * abs(x[2])]
+    assert len(floor_only) <= 6, floor_only
+    assert all(x[0] == "vertex_normal" for x in floor_only), floor_only
 
 
 def test_autograd_contract(setup):

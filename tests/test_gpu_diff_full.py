@@ -46,6 +46,7 @@ def test_full_size_radiance_matches_fp64(setup):
 
 
 def test_full_size_gradients_match_central_differences(setup):
+    """Purely relative: |GPU - FD| <= 1e-3 |FD| for every one of the 64."""
     res = central_differences(setup, central_difference_picks(setup, seed=0x5EED0005))
     bad = [x for x in res if not abs(x[3] - x[2]) <= 1e-3 * abs(x[2])]
     worst = max(abs(x[3] - x[2]) / max(abs(x[2]), 1e-300) for x in res)

@@ -145,8 +145,8 @@ def test_reference_png_assets():
     """The reference's small PNG test assets, when present, decode alike."""
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
-    import make_obj_fixtures as mk
-    d = mk.testdata_dir()
+    from helpers import reference_testdata
+    d = reference_testdata()
     if not os.path.isdir(d):
         pytest.skip("reference assets not present")
     names = [n for n in sorted(os.listdir(d)) if n.endswith(".png") and os.path.getsize(os.path.join(d, n)) < 40000]
@@ -230,8 +230,8 @@ def test_reference_load_image_golden():
     loaded with GammaCorrect(true) equals golden.png pixel for pixel."""
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
-    import make_obj_fixtures as mk
-    d = mk.testdata_dir()
+    from helpers import reference_testdata
+    d = reference_testdata()
     ground, golden = os.path.join(d, "ground.png"), os.path.join(d, "golden.png")
     if not (os.path.exists(ground) and os.path.exists(golden)):
         pytest.skip("reference test assets not present")

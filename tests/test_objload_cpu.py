@@ -274,7 +274,8 @@ def test_reference_assets_match_fixture():
     import json
     sys.path.insert(0, os.path.join(HERE, "golden"))
     import make_obj_fixtures as mk
-    d = mk.testdata_dir()
+    from helpers import reference_testdata
+    d = reference_testdata()
     if not os.path.isdir(d):
         pytest.skip("reference OBJ assets not present")
     with open(os.path.join(HERE, "golden", "obj_assets.json")) as fh:

@@ -123,8 +123,8 @@ def _kat_texture(case):
     if not t["asset"].endswith(".png"):
         pytest.skip(f"{t['asset']}: only PNG images are decoded")
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
-    import make_obj_fixtures as mk
-    path = os.path.join(mk.testdata_dir(), t["asset"])
+    from helpers import reference_testdata
+    path = os.path.join(reference_testdata(), t["asset"])
     if not os.path.exists(path):
         pytest.skip("reference test assets not present")
     from polyred_gb300 import imageload
