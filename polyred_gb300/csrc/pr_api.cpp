@@ -156,6 +156,7 @@ struct SceneBufs {
     HostBuf tables;                        // page-locked staging of the small tables (submitted uploads)
     cudaEvent_t ev_uploaded = nullptr;     // the upload into these buffers has landed
     cudaEvent_t ev_released = nullptr;     // the last frame that read them is past shading
+    cudaEvent_t ev_released_ao = nullptr;  // ... and past listing its AO pixels (stream 3)
     void release() {
         pos.release(); nor.release(); uv.release(); col.release(); mat.release();
         obj_first.release(); tri_flags.release(); obj_model.release(); obj_normal.release();
@@ -164,7 +165,8 @@ struct SceneBufs {
         has_tex = false;
         if (ev_uploaded) cudaEventDestroy(ev_uploaded);
         if (ev_released) cudaEventDestroy(ev_released);
-        ev_uploaded = ev_released = nullptr;
+        if (ev_released_ao) cudaEventDestroy(ev_released_ao);
+        ev_uploaded = ev_released = ev_released_ao = nullptr;
     }
 };
 
@@ -222,6 +224,10 @@ struct Ctx {
     cudaStream_t stream_c = nullptr;
     cudaEvent_t ev_setup = nullptr, ev_clip = nullptr;
     DevBuf<uint2> tasks_c;
+    // AO's march on stream 3 beside attributes and shading: after resolve,
+    // joined before the AO colour scaling
+    cudaEvent_t ev_resolved = nullptr, ev_ao0 = nullptr, ev_ao = nullptr;
+    DevBuf<float> ao_T;
     int n_sms = 1;
 };
 
@@ -503,7 +509,7 @@ void collect_stats(Ctx* c) {
     c->stats.ms_raster = span(c->ev[2], c->ev[3]);
     c->stats.ms_shade = span(c->ev[3], c->ev[4]);
     c->stats.ms_total = span(c->ev[0], c->ev[4]);
-    c->stats.ms_ao = span(c->ev[5], c->ev[4]);
+    c->stats.ms_ao = span(c->ev_ao0, c->ev_ao);  // listing and march, beside shading
     c->stats.n_ao_pixels = c->h_cnt[0].n_ao;
 }
 
@@ -807,6 +813,45 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         KTRY(prk::launch_raster(rc_, c->n_sms * 8, st));
         KTRY(prk::launch_resolve_listing(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p,
                                          c->first_rec.p, c->attr_state.p, c->vis_list.p, st));
+        // AmbientOcclusionShade's march needs only the resolved depths: its
+        // pixels are listed and marched on stream 3 (free after the clipped
+        // raster) while stream 1 writes attributes and shades; the colour
+        // scaling joins after shading.
+        const bool with_ao = out && out->rgba;
+        prk::AoParams ap{};
+        if (with_ao) {
+            if ((rc = c->ao_T.ensure(npx))) return rc;
+            CUDA_TRY(cudaEventRecord(c->ev_resolved, st));
+            CUDA_TRY(cudaStreamWaitEvent(sc, c->ev_resolved, 0));
+            CUDA_TRY(cudaEventRecord(c->ev_ao0, sc));
+            prk::AoListParams lp{};
+            lp.W = W;
+            lp.H = H;
+            lp.win = c->win.p;
+            lp.mat = c->sb.mat.p;
+            lp.obj_first = c->sb.obj_first.p;
+            lp.blk_obj = c->sb.blk_obj.p;
+            lp.obj_matbase = c->sb.obj_matbase.p;
+            lp.n_objects = (uint32_t)c->sb.objects.size();
+            lp.mats = c->sb.dmats.p;
+            lp.n_mats = (uint32_t)c->sb.materials.size();
+            lp.list = c->ao_list.p;
+            lp.cnt = dcnt;
+            KTRY(prk::launch_ao_list(lp, sc));
+            CUDA_TRY(cudaEventRecord(c->sb.ev_released_ao, sc));  // the scene buffers are read no more here
+            ap.W = W;
+            ap.H = H;
+            ap.gamma_on = (f->flags & PR_FRAME_GAMMA) ? 1 : 0;
+            ap.n_dirs = c->n_ao_dirs;
+            ap.ao_half_ulp = prh::ao_classify(c->ao_cos, c->ao_sin, c->n_ao_dirs, W, H, ap.dir_fast, ap.dir_tiny);
+            ap.depth = c->depth_ao.p;
+            ap.list = c->ao_list.p;
+            ap.cnt = dcnt;
+            ap.T = c->ao_T.p;
+            KTRY(prk::launch_ao_T(ap, sc));
+            CUDA_TRY(cudaEventRecord(c->ev_ao, sc));
+            launches += 2;
+        }
         KTRY(prk::launch_attr(mp, c->vis_list.p, st));
         KTRY(prk::launch_nan_cleanup(npx, c->nanseq.p, 0xFFFFFFFFu, c->beaten.p, 0u, dcnt, st));
         CUDA_TRY(cudaEventRecord(c->ev[3], st));
@@ -856,6 +901,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             if ((rc = c->o_msaa.ensure(npx * 4))) return rc;
             sp.rgba = (uchar4*)c->o_msaa.p;  // the framebuffer's colours
         }
+        sp.ao_listed = 1;  // listed by ao_list_kernel on stream 3
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_join, 0));  // the shadow maps are complete
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_d2h, 0));   // a submitted frame's outputs left the staging
         KTRY(prk::launch_shade(sp, st));
@@ -863,20 +909,13 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         CUDA_TRY(cudaEventRecord(c->sb.ev_released, st));  // the scene buffers are read no more
         CUDA_TRY(cudaEventRecord(c->ev[5], st));
         if (sp.rgba) {
-            // AmbientOcclusionShade + gamma for the pixels the shade kernel listed
-            prk::AoParams ap{};
-            ap.W = W;
-            ap.H = H;
-            ap.gamma_on = (f->flags & PR_FRAME_GAMMA) ? 1 : 0;
-            ap.n_dirs = c->n_ao_dirs;
-            ap.ao_half_ulp = prh::ao_classify(c->ao_cos, c->ao_sin, c->n_ao_dirs, W, H, ap.dir_fast, ap.dir_tiny);
-            ap.depth = c->depth_ao.p;
-            ap.list = c->ao_list.p;
-            ap.cnt = dcnt;
+            // AmbientOcclusionShade's colour scaling and gamma of the listed
+            // pixels, once their march (stream 3) and shading are done
+            CUDA_TRY(cudaStreamWaitEvent(st, c->ev_ao, 0));
             ap.rgba = sp.rgba;
             ap.dgb = dh ? dh->dgb : nullptr;
             std::memcpy(ap.gamma, sp.gamma, 256);
-            KTRY(prk::launch_ao(ap, st));
+            KTRY(prk::launch_ao_apply(ap, c->n_sms * 4, st));
             launches += 1;
             if (M > 1) {
                 KTRY(prk::launch_msaa_resize(sp.rgba, W, H, rgba_img, W_img, H_img, st));
@@ -992,7 +1031,11 @@ int pr_create(int device, void** out_ctx) {
         cudaEventCreateWithFlags(&c->sb.ev_uploaded, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->sb.ev_released, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->sb_back.ev_uploaded, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->sb_back.ev_released, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c->sb_back.ev_released, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->sb.ev_released_ao, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->sb_back.ev_released_ao, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_resolved, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&c->ev_ao0) != cudaSuccess || cudaEventCreate(&c->ev_ao) != cudaSuccess) {
         pr_destroy(c);
         return fail(PR_ERR_CUDA, "stream/event creation failed");
     }
@@ -1039,6 +1082,10 @@ int pr_destroy(void* ctx) {
     c->rrec_s.release(); c->tasks_s.release(); c->tasks_c.release();
     if (c->ev_setup) cudaEventDestroy(c->ev_setup);
     if (c->ev_clip) cudaEventDestroy(c->ev_clip);
+    if (c->ev_resolved) cudaEventDestroy(c->ev_resolved);
+    if (c->ev_ao0) cudaEventDestroy(c->ev_ao0);
+    if (c->ev_ao) cudaEventDestroy(c->ev_ao);
+    c->ao_T.release();
     if (c->stream_c) {
         cudaStreamSynchronize(c->stream_c);
         cudaStreamDestroy(c->stream_c);
@@ -1089,6 +1136,7 @@ int pr_frame_submit(void* ctx, const pr_scene_desc* scene, const pr_frame_desc* 
     clear_stale_error();
     CUDA_TRY(cudaEventSynchronize(b.ev_uploaded));                 // its staging is free again
     CUDA_TRY(cudaStreamWaitEvent(c->stream_u, b.ev_released, 0));  // no frame reads it any more
+    CUDA_TRY(cudaStreamWaitEvent(c->stream_u, b.ev_released_ao, 0));
     if ((rc = scene_fill(b, scene, c->stream_u, true))) return rc;
     CUDA_TRY(cudaEventRecord(b.ev_uploaded, c->stream_u));
     std::swap(c->sb, c->sb_back);

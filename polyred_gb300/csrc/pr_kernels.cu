@@ -1316,7 +1316,47 @@ template <bool kTex>
 __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
     const bool pending = shade_one<kTex>(P, x, r);
-    if (P.ao_list) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
+    if (P.ao_list && !P.ao_listed) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
+}
+
+// The shade kernel's AO condition without shading: a covered pixel whose
+// winning triangle's flat material (MaterialID plus its geometry's base, as
+// the setup forms it) exists and has AO. 32 x 8 tiles, one atomic per tile,
+// the order the shade kernel's own append gives.
+__global__ void __launch_bounds__(256) ao_list_kernel(const __grid_constant__ AoListParams P) {
+    __shared__ uint32_t s_cnt[8];
+    __shared__ uint32_t s_base;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint32_t i = (uint32_t)r * (uint32_t)P.W + (uint32_t)x;
+    bool pending = false;
+    if (x < P.W && r < P.H) {
+        const uint32_t seq = P.win[i];
+        if (seq != kNone) {
+            const uint32_t t = seq >> 3;
+            int m = P.mat[t];
+            if (m >= 0) {
+                uint32_t o = P.blk_obj[t >> 7];
+                while (o + 1 < P.n_objects && P.obj_first[o + 1] <= t) o++;
+                m += P.obj_matbase[o];
+                pending = m >= 0 && (uint32_t)m < P.n_mats && (P.mats[m].flags & PR_MAT_AO) != 0u;
+            }
+        }
+    }
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned msk = __ballot_sync(0xffffffffu, pending);
+    if (lane == 0) s_cnt[warp] = (uint32_t)__popc(msk);
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < 8; w++) tot += s_cnt[w];
+        s_base = tot ? atomicAdd(&P.cnt->n_ao, tot) : 0u;
+    }
+    __syncthreads();
+    if (pending) {
+        uint32_t o = s_base + (uint32_t)__popc(msk & ((1u << lane) - 1u));
+        for (int w = 0; w < warp; w++) o += s_cnt[w];
+        P.list[o] = i;
+    }
 }
 
 // ---------------------------------------------------------------- AO
@@ -1555,7 +1595,11 @@ PR_DEV void ao_tables(const AoParams& P, int (*s_off)[kAoTable], float (*s_rlo)[
     }
 }
 
-// One pixel of the AO list.
+PR_DEV void ao_finish(const AoParams& P, uint32_t i, float T);
+
+// One pixel of the AO list: its total T, then (kApply) the colour scaling,
+// or (!kApply) T stored for ao_apply_kernel.
+template <bool kApply>
 PR_DEV void ao_one(const AoParams& P, uint32_t j, const int (*s_off)[kAoTable], const float (*s_rlo)[kAoTable],
                    const float (*s_rhi)[kAoTable]) {
     const int W = P.W, H = P.H;
@@ -1646,6 +1690,15 @@ PR_DEV void ao_one(const AoParams& P, uint32_t j, const int (*s_off)[kAoTable], 
         total = __fadd_rn(total, __fsub_rn(1.57079632679489661923f, ma));  // HalfPi - angle
     }
     const float T = nanpix ? __uint_as_float(0x7fc00000u) : __fdiv_rn(total, 12.5663706143591729539f);
+    if (kApply)
+        ao_finish(P, i, T);
+    else
+        P.T[j] = T;
+}
+
+// material/ao.go:34-37 for pixel i with total T: the colour the shade kernel
+// left (pre-AO, pre-gamma) times float32(Pow(T, 10000)), then gamma.
+PR_DEV void ao_finish(const AoParams& P, uint32_t i, float T) {
     const uchar4 c = P.rgba[i];
     if (P.dgb) {
         // float32(Pow(T, 10000)) as a fixed factor of the differentiable radiance (0 for NaN, as the
@@ -1662,6 +1715,7 @@ PR_DEV void ao_one(const AoParams& P, uint32_t j, const int (*s_off)[kAoTable], 
     P.rgba[i] = make_uchar4(o.x, o.y, o.z, c.w);
 }
 
+template <bool kApply>
 __global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant__ AoParams P) {
     __shared__ __align__(16) int s_off[8][kAoTable];
     __shared__ __align__(16) float s_rlo[8][kAoTable];
@@ -1671,7 +1725,14 @@ __global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant
     ao_tables(P, s_off, s_rlo, s_rhi);
     __syncthreads();
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        ao_one(P, j, s_off, s_rlo, s_rhi);
+        ao_one<kApply>(P, j, s_off, s_rlo, s_rhi);
+}
+
+// The colour scaling of every listed pixel from its stored total.
+__global__ void ao_apply_kernel(const __grid_constant__ AoParams P) {
+    const uint32_t n = P.cnt->n_ao;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        ao_finish(P, P.list[j], P.T[j]);
 }
 
 // Triangle.IsValid (geometry/primitive/triangle.go:63-80) of every input
@@ -1820,7 +1881,7 @@ __global__ void __launch_bounds__(kAoThreads) ao_batch_kernel(const AoParams* vi
             __syncthreads();
             if (c * blockDim.x >= n) break;
             const uint32_t j = c * blockDim.x + threadIdx.x;
-            if (j < n) ao_one(P, j, s_off, s_rlo, s_rhi);
+            if (j < n) ao_one<true>(P, j, s_off, s_rlo, s_rhi);
         }
     }
 }
@@ -2034,13 +2095,24 @@ int launch_msaa_resize(const uchar4* in, int in_w, int in_h, uchar4* out, int w,
     return check(cudaGetLastError());
 }
 
-int launch_ao(const AoParams& p, void* stream) {
+int launch_ao_T(const AoParams& p, void* stream) {
     // One pixel per thread for the largest possible list (every pixel): the
     // block scheduler balances the uneven per-pixel work; blocks past the
     // list's length exit at once.
     const size_t n = (size_t)p.W * p.H;
     if (n == 0) return 0;
-    ao_kernel<<<(unsigned)((n + kAoThreads - 1) / kAoThreads), kAoThreads, 0, (cudaStream_t)stream>>>(p);
+    ao_kernel<false><<<(unsigned)((n + kAoThreads - 1) / kAoThreads), kAoThreads, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_ao_apply(const AoParams& p, int n_blocks, void* stream) {
+    ao_apply_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(p);
+    return check(cudaGetLastError());
+}
+int launch_ao_list(const AoListParams& p, void* stream) {
+    if (p.W <= 0 || p.H <= 0) return 0;
+    dim3 blk(32, 8);
+    dim3 grd((p.W + 31) / 32, (p.H + 7) / 8);
+    ao_list_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
     return check(cudaGetLastError());
 }
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream) {

@@ -162,6 +162,7 @@ struct ShadeParams {
     uchar4* gvcol;
     int32_t* gmat;
     uint32_t* ao_list;          // pixels whose material has AO (null: AO off)
+    int ao_listed;              // 1: ao_list_kernel lists them; shade only leaves their pre-AO colour
     Counters* cnt_w;
     // differentiation only (null otherwise)
     const float* tri_scr;       // [n_tris][12] from the main setup
@@ -184,6 +185,24 @@ struct AoParams {
     int8_t dir_tiny[8];  // 1 / 2: the x / y component lies in (-1/99, 0)
     float ao_half_ulp;   // half an ulp of float32 at max(W, H) + 100
     float4* dgb;         // differentiation only: multiply the G-buffer's factor by the AO factor
+    float* T;            // [list] the AO total of each listed pixel (ao_T_kernel -> ao_apply_kernel)
+};
+
+// The AO pixels of a frame, listed beside shading: every covered pixel whose
+// winning triangle's material has AO (the shade kernel's own condition),
+// appended tile by tile (32 x 8) as the shade kernel would.
+struct AoListParams {
+    int W, H;
+    const uint32_t* win;         // winning seq per pixel (input triangle = seq >> 3)
+    const int32_t* mat;          // [n_tris] Triangle.MaterialID, geometry-local
+    const uint32_t* obj_first;   // [n_objects + 1]
+    const uint32_t* blk_obj;     // [n_tris / 128] object of each 128-triangle block's first triangle
+    const int32_t* obj_matbase;  // [n_objects]
+    uint32_t n_objects;
+    const pr_material* mats;
+    uint32_t n_mats;
+    uint32_t* list;
+    Counters* cnt;               // n_ao
 };
 
 // Differentiable shading (pr_diff.cu)
@@ -242,7 +261,12 @@ int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* s
 int launch_nan_cleanup(size_t n, uint32_t* a, uint32_t va, uint32_t* b, uint32_t vb, const Counters* cnt,
                        void* stream);
 int launch_shade(const ShadeParams& p, void* stream);
-int launch_ao(const AoParams& p, void* stream);
+// AO split in three so that its march overlaps shading: the list (after
+// resolve), the march writing p.T (after the list), and the colour scaling
+// and gamma of the listed pixels (after both the march and shading).
+int launch_ao_list(const AoListParams& p, void* stream);
+int launch_ao_T(const AoParams& p, void* stream);
+int launch_ao_apply(const AoParams& p, int n_blocks, void* stream);
 // passAntialiasing's imageutil.Resize of the n*W x n*H image `in` to W x H
 // (rows top-down, both buffers on the device).
 int launch_msaa_resize(const uchar4* in, int in_w, int in_h, uchar4* out, int w, int h, void* stream);
