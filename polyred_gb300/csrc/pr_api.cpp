@@ -1013,6 +1013,11 @@ int pr_create(int device, void** out_ctx) {
     c->device = device;
     int rc = set_device(c);
     if (rc) { delete c; return rc; }
+    // Stream 3 (clipped raster, then AO's march: the frame's longest chain
+    // after resolve) takes the device's highest priority, so that its blocks
+    // go first and shading and the shadow passes fill the rest.
+    int prio_lo = 0, prio_hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess) prio_hi = 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         return fail(PR_ERR_CUDA, "cudaStreamCreate failed");
@@ -1021,7 +1026,7 @@ int pr_create(int device, void** out_ctx) {
     if (cudaStreamCreateWithFlags(&c->stream_s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->stream_c, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->stream_c, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_setup, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_clip, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream_u, cudaStreamNonBlocking) != cudaSuccess ||
