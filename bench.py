@@ -16,7 +16,8 @@ sRGB gamma. Metric: Mtri/s = input triangles per second of frame time.
   --impl reference  the CPU restatement of the reference renderer (oracle/),
          all host threads, single-worker draw order
 
-Further legs in the same line (each skippable): diff (the adjoint, --no-diff),
+Further legs in the same line (each skippable): small_800x500 (the small
+UV-sphere workload), diff (the adjoint and its 200-step Adam loop, --no-diff),
 soup_4k (10M triangles at 3840x2160, --no-soup), batched (many views in one
 job, --no-batch), msaa_2x and textured_1080p (--no-msaa), obj_ingest
 (loading a 41 MB Wavefront OBJ, --no-obj), cpu_baseline (--no-cpu-baseline).
@@ -484,7 +485,7 @@ def measure_obj(steps=20, n_tori=32, nu=128, nv=64, width=1920, height=1080):
                              "sample": "obj.go restated in pure Python, first 1 MB of the same OBJ text"}}
 
 
-def _resident_frames(s, cam, width, height, steps, msaa=1, shadow_size=SHADOW):
+def _resident_frames(s, cam, width, height, steps, msaa=1, shadow_size=SHADOW, shadow_map=True):
     """ms per resident frame of scene s (CUDA events on the context's stream)."""
     import torch
     from polyred_gb300 import _abi, native, render
@@ -493,9 +494,9 @@ def _resident_frames(s, cam, width, height, steps, msaa=1, shadow_size=SHADOW):
     flat = render.FlatScene(s)
     desc = flat.desc()
     native.check(lib.pr_scene_upload(dev.handle, C.byref(desc)))
-    opts = dict(width=width, height=height, camera=cam, scene=s, perspective=True, shadow_map=True, gamma=True,
+    opts = dict(width=width, height=height, camera=cam, scene=s, perspective=True, shadow_map=shadow_map, gamma=True,
                 background=(0, 0, 0, 0), shadow_size=shadow_size, directional_shadows=True, msaa=msaa)
-    fd = render.FrameDesc(opts, shadow_cams(opts))
+    fd = render.FrameDesc(opts, shadow_cams(opts) if shadow_map else {})
     rgba = torch.empty((height, width, 4), dtype=torch.uint8, device="cuda")
     od = _abi.pr_outputs()
     od.size = C.sizeof(_abi.pr_outputs)
@@ -525,6 +526,37 @@ def measure_msaa(steps=20):
     ms = _resident_frames(s, cam, W, H, steps, msaa=2)
     return {"workload": "sphere field, 1920x1080 image, MSAA 2 (3840x2160 framebuffer)", "n_tris": N_TRIS,
             "ms_per_frame": ms, "value": N_TRIS / (ms / 1e3) / 1e6, "unit": "Mtri/s"}
+
+
+def measure_small(steps=200, width=800, height=500, cpu_baseline=True):
+    """The small CPU-runnable workload: the 64x32 UV sphere (3,968 triangles)
+    on a 2-triangle ground, one point light, ambient 0.1, shadows off, gamma
+    on, 800x500; resident frames, and the oracle on one frame (all host
+    threads)."""
+    from polyred_gb300 import procedural, render
+    s, cam = procedural.small_scene(width, height)
+    n = render.FlatScene(s).n_tris
+    ms = _resident_frames(s, cam, width, height, steps, shadow_size=None, shadow_map=False)
+    res = {"workload": "UV sphere 64x32 on a ground plane, 800x500, no shadows", "n_tris": n,
+           "ms_per_frame": ms, "frames_per_s": 1e3 / ms, "value": n / (ms / 1e3) / 1e6, "unit": "Mtri/s"}
+    if cpu_baseline:
+        import oracle
+        threads = os.cpu_count() or 1
+        flat = render.FlatScene(s)
+        opts = dict(width=width, height=height, camera=cam, scene=s, perspective=True, shadow_map=False, gamma=True,
+                    background=(0, 0, 0, 0), shadow_size=None)
+        fd = render.FrameDesc(opts, {})
+        out = render.Outputs(width, height, ("rgba",))
+        oracle.render(flat.desc(), fd.desc, out.desc, threads=threads)  # warm
+        t0 = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            oracle.render(flat.desc(), fd.desc, out.desc, threads=threads)
+        dt = (time.perf_counter() - t0) / reps
+        res["cpu_baseline"] = {"value": 1.0 / dt, "unit": "frames/s", "cores": threads, "kind": "port",
+                               "sample": "5 frames of the workload (C++ restatement of the Go CPU renderer, "
+                                         "row-band threads)"}
+    return res
 
 
 def measure_textured(steps=50, width=1920, height=1080):
@@ -828,6 +860,10 @@ def main():
             line["soup_4k"] = measure_soup(cpu_baseline=world == 1 and not args.no_cpu_baseline)
         if not args.no_batch:
             line["batched"] = measure_batch(cpu_baseline=world == 1 and not args.no_cpu_baseline)
+        try:
+            line["small_800x500"] = measure_small(cpu_baseline=world == 1 and not args.no_cpu_baseline)
+        except Exception as e:  # the headline line must still print
+            line["small_800x500"] = {"error": f"{type(e).__name__}: {e}"}
         if not args.no_msaa:
             try:
                 line["msaa_2x"] = measure_msaa()
