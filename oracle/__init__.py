@@ -175,9 +175,9 @@ def diff_forward64(inp, target=None, want_radiance=True):
 
 def diff_backward64(inp, grad, absolute=False):
     """Gradients of sum(grad * radiance) in float64, shaped like the
-    parameters; with absolute=True, for each gradient the sum of the
-    magnitudes of its per-pixel contributions instead (the scale of the
-    rounding error of a float32 evaluation of that sum)."""
+    parameters; with absolute=True, for each gradient a majorant of its
+    terms instead (every factor and sum of every pixel's contribution taken
+    in magnitude: the scale of the rounding error of a float32 evaluation)."""
     import numpy as np
     lib = load()
     lib.orc_diff_backward64.restype = None

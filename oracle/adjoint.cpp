@@ -24,9 +24,10 @@ inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline double nrm(D3 a) { return std::sqrt(dot(a, a)); }
 
 const uint32_t kLit = 1u, kFlat = 2u, kConst = 4u, kUnlit = 8u;
-// orc_diff_in.flags: the backward accumulates |v| for each per-pixel
-// contribution v, the sum of the magnitudes that bounds the rounding error of
-// a float32 evaluation of the gradient.
+// orc_diff_in.flags: the backward accumulates majorants instead of the
+// gradients: per pixel its terms with every factor and sum replaced by
+// magnitudes (majorants()), which bound the rounding error of a float32
+// evaluation of the gradient.
 const int32_t kAbs = 1;
 
 }  // namespace
@@ -87,6 +88,69 @@ uint32_t find_obj(const orc_diff_in* in, uint32_t t) {
             hi = mid - 1;
     }
     return lo;
+}
+
+// Per light of one pixel: direction, half vector, intensity, distance and
+// the clamped diffuse and specular terms.
+struct LT { D3 L, H; double I, dist, hlen, nd, nh, ld, ls; };
+
+inline D3 absv(D3 a) { return {std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)}; }
+
+// The absolute mode's contribution of one lit pixel: the backward's terms
+// with every factor replaced by its magnitude and every sum by a sum of
+// magnitudes (the projections of the unit-vector derivatives included), so
+// that it bounds every intermediate a float32 evaluation of the pixel's
+// gradient forms, before any cancellation: the scale of its rounding error.
+void majorants(const orc_diff_in* in, orc_diff_out* out, uint32_t t, int32_t m, double fac, const double* pre,
+               const double* g, const double* col, const double* kd, const double* ks, double s, bool flat, D3 n,
+               double mlen, const float* M, const float* d, const std::vector<LT>& lt) {
+    double ag[3];
+    for (int c = 0; c < 3; c++) ag[c] = (pre[c] > 0.0 && pre[c] < 255.0) ? std::fabs(g[c] * fac) : 0.0;
+    D3 Ld = {0, 0, 0}, Ls = {0, 0, 0};
+    for (int l = 0; l < in->n_lights; l++) {
+        Ld = Ld + (lt[l].ld * lt[l].I) * D3{col[0], col[1], col[2]};
+        Ls = Ls + (lt[l].ls * lt[l].I) * D3{(double)in->lcol[4 * l], (double)in->lcol[4 * l + 1], (double)in->lcol[4 * l + 2]};
+    }
+    const double LdA[3] = {Ld.x, Ld.y, Ld.z}, LsA[3] = {Ls.x, Ls.y, Ls.z};
+    for (int c = 0; c < 3; c++) {
+        if (out->kd) out->kd[3 * m + c] += ag[c] * LdA[c];
+        if (out->ks) out->ks[3 * m + c] += ag[c] * LsA[c];
+    }
+    const double gcol = ag[0] * col[0] + ag[1] * col[1] + ag[2] * col[2];
+    for (int e = 0; e < in->n_amb; e++)
+        if (out->amb) out->amb[e] += gcol;
+    D3 gnA = {0, 0, 0};
+    const D3 nA = absv(n);
+    for (int l = 0; l < in->n_lights; l++) {
+        const LT& q = lt[l];
+        const double A = ag[0] * std::fabs(kd[0]) * col[0] + ag[1] * std::fabs(kd[1]) * col[1] + ag[2] * std::fabs(kd[2]) * col[2];
+        const double B = ag[0] * std::fabs(ks[0]) * in->lcol[4 * l] + ag[1] * std::fabs(ks[1]) * in->lcol[4 * l + 1] +
+                         ag[2] * std::fabs(ks[2]) * in->lcol[4 * l + 2];
+        const double invd = in->ltype[l] == 0 ? 1.0 / q.dist : 1.0;
+        if (out->lint) out->lint[l] += (A * q.ld + B * q.ls) * invd;
+        const double nhc = std::fmin(std::fmax(q.nh, 0.0), 1.0);
+        if (q.ls > 0.0 && nhc < 1.0 && out->shin) out->shin[m] += B * q.I * q.ls * std::fabs(std::log(nhc));
+        const double gnd = (q.nd > 0.0 && q.nd < 1.0) ? A * q.I : 0.0;
+        const double gnh = (q.nh > 0.0 && q.nh < 1.0) ? B * q.I * std::fabs(s) * std::pow(nhc, s - 1.0) : 0.0;
+        const D3 LA = absv(q.L), HA = absv(q.H);
+        gnA = gnA + gnd * LA + gnh * HA;
+        if (in->ltype[l] == 0 && out->lpos) {
+            const D3 gLA = gnd * nA + (gnh / q.hlen) * (nA + std::fabs(q.nh) * HA);
+            const D3 gDA = (1.0 / q.dist) * (gLA + dot(LA, gLA) * LA) + ((A * q.ld + B * q.ls) * q.I / q.dist) * LA;
+            out->lpos[3 * l] += gDA.x;
+            out->lpos[3 * l + 1] += gDA.y;
+            out->lpos[3 * l + 2] += gDA.z;
+        }
+    }
+    if (!flat && out->vnor) {
+        const D3 gmA = (1.0 / mlen) * (gnA + dot(nA, gnA) * nA);
+        for (int k = 0; k < 3; k++) {
+            const D3 gNA = std::fabs((double)d[4 + k]) * gmA;
+            double* gv = out->vnor + 4 * (3 * (size_t)t + k);
+            for (int j = 0; j < 3; j++)
+                gv[j] += std::fabs(M[j]) * gNA.x + std::fabs(M[4 + j]) * gNA.y + std::fabs(M[8 + j]) * gNA.z;
+        }
+    }
 }
 
 // One pixel: radiance R[3]; with g != null also accumulates dL/d(params).
@@ -150,7 +214,6 @@ void pixel(const orc_diff_in* in, size_t i, double R[3], const double* g, orc_di
         for (int c = 0; c < 3; c++) La[c] += in->amb[e] * col[c];
     const D3 Vd = D3{in->cam[0], in->cam[1], in->cam[2]} - x;
     const D3 V = (1.0 / nrm(Vd)) * Vd;
-    struct LT { D3 L, H; double I, dist, hlen, nd, nh, ld, ls; };
     std::vector<LT> lt(in->n_lights);
     for (int l = 0; l < in->n_lights; l++) {
         LT& q = lt[l];
@@ -183,6 +246,10 @@ void pixel(const orc_diff_in* in, size_t i, double R[3], const double* g, orc_di
         R[c] = fac * std::fmin(std::fmax(pre[c], 0.0), 255.0);
     }
     if (!g) return;
+    if (absm) {
+        majorants(in, out, t, m, fac, pre, g, col, kd, ks, s, flat, n, mlen, M, d, lt);
+        return;
+    }
     double gg[3];
     for (int c = 0; c < 3; c++) gg[c] = (pre[c] > 0.0 && pre[c] < 255.0) ? g[c] * fac : 0.0;
     for (int c = 0; c < 3; c++) {

@@ -87,7 +87,60 @@ PR_DEV bool box_contains(const Box& a, V4 v) {
 PR_DEV float ext_w(const SetupParams& P) { return (float)(P.msaa > 1 ? P.W * P.msaa : P.W); }
 PR_DEV float ext_h(const SetupParams& P) { return (float)(P.msaa > 1 ? P.H * P.msaa : P.H); }
 
-PR_DEV bool pixel_box(V4 a, V4 b, V4 c, int W, int H, uint32_t* bx, uint32_t* by, uint32_t* area) {
+// The pixels of the reference's box that the inside test can accept: those
+// whose centre lies within a margin m of the triangle's bounding box; every
+// other pixel fails drawClipped's test bc >= -Epsilon (render/raster.go:491)
+// for certain, so leaving it out changes no fragment.
+//
+// Why. Let S_j (j = 0..2) be the exact cross products of the exact vertex
+// differences with the pixel centre p, S their sum (the exact Sabc), bc_j =
+// S_j / S. If p.x >= max_x + m, then p.x - max_x = sum_j bc_j (x_j - max_x)
+// <= N w_x with N the sum of the negative bc_j and w_x the box width, so
+// some bc_j <= -m / (2 w_x) (at most two are negative): |S_j| >=
+// m |S| / (2 w_x), opposite in sign to S (the same for the other sides and
+// for y). The test's float32 values: each cross product is formed from
+// rounded differences (relative error u = 2^-24 each) as fma64f(vx, wy,
+// -RN(vy wx)), within 3u (|vx wy| + |vy wx|) of its rounded-input value, so
+// within dS = 6u E U of the exact one, E = w_x + w_y bounding every edge's
+// L1 length and U = E + 4 every |p - vertex|_1 over the box (the reference
+// box lies within the bounding box padded by 1.5 px); Sabc within dA = 6u E^2.
+// When L = |Sabc| - dA > 2 dA, the signs hold and the computed b_j =
+// RN(S_j' / Sabc') <= -(|S_j| - dS) / (|S| + dA) (1 - u) < -Epsilon as soon
+// as |S_j| - dS >= 2e-7 (|Sabc| + 2 dA), which m_x = 2 w_x (dS + 2.1e-7
+// (|Sabc| + 2 dA)) / L guarantees. All in upward rounding; degenerate,
+// near-degenerate and non-finite triangles keep the reference box (their
+// NaN and infinite barycentrics can pass the test anywhere in it).
+PR_DEV void tighten_box(V4 a, V4 b, V4 c, float sabc, long long& x0, long long& x1, long long& y0, long long& y1) {
+    const float mnx = fminf(fminf(a.x, b.x), c.x), mxx = fmaxf(fmaxf(a.x, b.x), c.x);
+    const float mny = fminf(fminf(a.y, b.y), c.y), mxy = fmaxf(fmaxf(a.y, b.y), c.y);
+    if (!(isfinite(mnx) && isfinite(mxx) && isfinite(mny) && isfinite(mxy) && isfinite(sabc))) return;
+    const float wx = __fsub_ru(mxx, mnx), wy = __fsub_ru(mxy, mny);
+    const float E = __fadd_ru(wx, wy), U = __fadd_ru(E, 4.0f);
+    const float k6u = 3.6e-7f;  // >= 6 * 2^-24
+    const float dS = __fmul_ru(__fmul_ru(k6u, E), U), dA = __fmul_ru(__fmul_ru(k6u, E), E);
+    const float as = fabsf(sabc);
+    const float L = __fsub_rd(as, dA);
+    if (!(L > __fmul_ru(2.0f, dA)) || !(L > 0.0f)) return;
+    const float q = __fdiv_ru(__fadd_ru(dS, __fmul_ru(2.1e-7f, __fadd_ru(as, __fmul_ru(2.0f, dA)))), L);
+    const float mx = __fmul_ru(__fmul_ru(2.0f, wx), q), my = __fmul_ru(__fmul_ru(2.0f, wy), q);
+    // centres x + 0.5 in [mnx - mx, mxx + mx], rounded outward
+    const float lx = ceilf(__fsub_rd(__fsub_rd(mnx, mx), 0.5f)), hx = floorf(__fsub_ru(__fadd_ru(mxx, mx), 0.5f));
+    const float ly = ceilf(__fsub_rd(__fsub_rd(mny, my), 0.5f)), hy = floorf(__fsub_ru(__fadd_ru(mxy, my), 0.5f));
+    if (!(lx <= hx && ly <= hy)) {  // no pixel centre can pass
+        x0 = 1;
+        x1 = 0;
+        return;
+    }
+    // within the reference box (|coordinates| < 2^16 there): float compares, then exact conversions
+    if (lx > (float)x0) x0 = (long long)lx;
+    if (hx < (float)x1) x1 = (long long)hx;
+    if (ly > (float)y0) y0 = (long long)ly;
+    if (hy < (float)y1) y1 = (long long)hy;
+}
+
+// The reference's pixel box (rounded bounding box padded by one, clamped
+// to the target), narrowed by tighten_box; false: no pixel to test.
+PR_DEV bool pixel_box(V4 a, V4 b, V4 c, float sabc, int W, int H, uint32_t* bx, uint32_t* by, uint32_t* area) {
     Box r = box3(a, b, c);
     long long xmin = go_f2i(__fsub_rn(pround(r.mnx), 1.0f));
     long long xmax = go_f2i(__fadd_rn(pround(r.mxx), 1.0f));
@@ -95,6 +148,8 @@ PR_DEV bool pixel_box(V4 a, V4 b, V4 c, int W, int H, uint32_t* bx, uint32_t* by
     long long ymax = go_f2i(__fadd_rn(pround(r.mxy), 1.0f));
     long long x0 = xmin < 0 ? 0 : xmin, x1 = xmax > W - 1 ? W - 1 : xmax;
     long long y0 = ymin < 0 ? 0 : ymin, y1 = ymax > H - 1 ? H - 1 : ymax;
+    if (x0 > x1 || y0 > y1) return false;
+    tighten_box(a, b, c, sabc, x0, x1, y0, y1);
     if (x0 > x1 || y0 > y1) return false;
     *bx = (uint32_t)x0 | ((uint32_t)x1 << 16);
     *by = (uint32_t)y0 | ((uint32_t)y1 << 16);
@@ -251,7 +306,7 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
     R.sabc = sabc_of(R.v[0], R.v[1], R.v[3], R.v[4], R.v[6], R.v[7]);
     R.seq = seq;
     uint32_t area = 0;
-    if (!pixel_box(v[0].pos, v[1].pos, v[2].pos, P.W, P.H, &R.bx, &R.by, &area)) {
+    if (!pixel_box(v[0].pos, v[1].pos, v[2].pos, R.sabc, P.W, P.H, &R.bx, &R.by, &area)) {
         R.bx = 1u;  // x0 = 1 > x1 = 0: empty
         R.by = 0u;
         area = 0;
@@ -614,7 +669,7 @@ struct __align__(16) SmRec {
     float4 e0;  // (B-A).x, (B-A).y, (C-A).x, (C-A).y
     float4 e1;  // (C-B).x, (C-B).y, RN(1/Sabc) (0: no early reject), Sabc
     float4 zs;  // A.z, B.z, C.z, seq (bits)
-    uint4 bb;   // bbox x0, bbox y0 + the task's first row, bbox width bw, ceil(2^32 / bw)
+    uint4 bb;   // bbox x0, bbox y0 + the task's first row, bbox width bw, ceil(2^32 / bw) (0 for bw = 1)
 };
 
 // A warp's raster scratch: its 32 records, the prefix of their pixel counts,
@@ -631,7 +686,7 @@ struct RasterWarpSm {
 // bbox index t of a record's pixel -> (px, py). t < 2^17 and bw <= 2^14, so
 // t * bw < 2^32 and the multiply-high quotient is exact.
 PR_DEV void rec_pixel(const uint4& bb, uint32_t t, int* px, int* py) {
-    const uint32_t q = __umulhi(t, bb.w);
+    const uint32_t q = bb.w ? __umulhi(t, bb.w) : t;  // ceil(2^32 / 1) does not fit: one column, row t
     *px = (int)(bb.x + (t - q * bb.z));
     *py = (int)(bb.y + q);
 }
@@ -739,7 +794,7 @@ PR_DEV void raster_warp(const RasterParams& P, uint32_t base, uint32_t n_tasks, 
             if (k0 < area) cnt = (int)min(area - k0, 1u << P.task_shift);
             const uint32_t qy0 = k0 / bw;  // one division per task
             qx0 = k0 - qy0 * bw;
-            s.bb = make_uint4(x0, y0 + qy0, bw, 0xFFFFFFFFu / bw + 1u);
+            s.bb = make_uint4(x0, y0 + qy0, bw, bw > 1u ? 0xFFFFFFFFu / bw + 1u : 0u);
         }
     }
     int incl = cnt;

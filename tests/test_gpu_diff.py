@@ -123,10 +123,11 @@ def central_differences(setup, picks, h=1e-4):
     estimate is the spread of the central differences with steps 2h and h/2
     around the one with h, plus their rounding (the loss's float64 ulp over
     the step: a contribution below it leaves the loss unchanged, so the
-    difference reads 0); the float32 error scale is 2^-17 times the sum of
-    the magnitudes of the gradient's per-pixel contributions (FP64 adjoint
-    in its absolute mode), which bounds the rounding of a float32 evaluation
-    of that sum (about a hundred roundings per contribution, each within
+    difference reads 0); the float32 error scale is 2^-17 times a majorant
+    of the gradient's terms (the FP64 adjoint in its absolute mode: every
+    factor and sum of every pixel's contribution in magnitude, projections of
+    the unit-vector derivatives included), which bounds the rounding of a
+    float32 evaluation (about a hundred roundings per term, each within
     2^-24)."""
     r, p, rad, gbuf, inp = setup
     target, grad = _loss_setup(setup)
@@ -159,11 +160,13 @@ def test_gradients_match_central_differences(setup):
     FP64 loss (visibility fixed), against the GPU gradients: within 1e-3
     relative, plus the FD's own error estimate and the float32 error scale
     of the gradient (central_differences). Only gradients at the noise level
-    of their own sum need those terms: vertex normals of triangles whose
+    of their own terms need those terms: vertex normals of triangles whose
     pixels already match the target to about 1e-6, whose gradients are
     1e-26 to 1e-15 (below the float64 resolution of a loss near 1e-13 over
-    the step, so the central difference reads 0); at most a few of the 64
-    picks are such."""
+    the step, so the central difference reads 0, or a derivative that
+    vanishes exactly, the perturbation lying along the unit normal, where
+    both adjoints return their rounding); at most a few of the 64 picks are
+    such."""
     res = central_differences(setup, central_difference_picks(setup))
     bad = [x for x in res if not abs(x[3] - x[2]) <= 1e-3 * abs(x[2]) + x[4] + x[5]]
     assert not bad, bad[:6]
