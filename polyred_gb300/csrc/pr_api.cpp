@@ -359,7 +359,8 @@ int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool stage
     if ((rc = upload(b.dmats, t_mats, nm, false, st))) return rc;
     if ((rc = upload(b.blk_obj, t_blk, blk.size(), false, st))) return rc;
     if ((rc = b.tri_flags.ensure(std::max<uint32_t>(n, 1)))) return rc;
-    KTRY(prk::launch_tri_flags(b.pos.p, n, b.tri_flags.p, st));
+    KTRY(prk::launch_tri_flags(b.pos.p, n, b.tri_flags.p, b.mat.p, b.obj_first.p, b.blk_obj.p, b.obj_matbase.p, no,
+                               b.dmats.p, nm, st));
     // image textures: NewTexture's levels built here, once per upload
     b.has_tex = false;
     if (scene_has_images(s)) {
@@ -828,13 +829,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             lp.W = W;
             lp.H = H;
             lp.win = c->win.p;
-            lp.mat = c->sb.mat.p;
-            lp.obj_first = c->sb.obj_first.p;
-            lp.blk_obj = c->sb.blk_obj.p;
-            lp.obj_matbase = c->sb.obj_matbase.p;
-            lp.n_objects = (uint32_t)c->sb.objects.size();
-            lp.mats = c->sb.dmats.p;
-            lp.n_mats = (uint32_t)c->sb.materials.size();
+            lp.tri_flags = c->sb.tri_flags.p;
             lp.list = c->ao_list.p;
             lp.cnt = dcnt;
             KTRY(prk::launch_ao_list(lp, sc));

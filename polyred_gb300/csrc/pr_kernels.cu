@@ -290,7 +290,8 @@ PR_DEV void write_attr(const SetupParams& P, uint32_t ridx, const SubVtx* v, con
 }
 
 // Build and store the records of one sub-triangle; returns its pixel area
-// (0 = nothing to raster) and writes its bbox words. With P.defer_attr the
+// (0 = nothing to raster, and then nothing is stored) and writes its bbox
+// words. With P.defer_attr the
 // attribute record is left to attr_kernel, which writes it only for records
 // that win a pixel.
 PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, const SubVtx* v, const float* recipw,
@@ -306,11 +307,9 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
     R.sabc = sabc_of(R.v[0], R.v[1], R.v[3], R.v[4], R.v[6], R.v[7]);
     R.seq = seq;
     uint32_t area = 0;
-    if (!pixel_box(v[0].pos, v[1].pos, v[2].pos, R.sabc, P.W, P.H, &R.bx, &R.by, &area)) {
-        R.bx = 1u;  // x0 = 1 > x1 = 0: empty
-        R.by = 0u;
-        area = 0;
-    }
+    // no pixel to test: no task will name the record, no pixel can pick it
+    // as its winner, so nothing reads it
+    if (!pixel_box(v[0].pos, v[1].pos, v[2].pos, R.sabc, P.W, P.H, &R.bx, &R.by, &area)) return 0;
     const float4* rs = reinterpret_cast<const float4*>(&R);
     float4* rd = reinterpret_cast<float4*>(P.rrec + ridx);
 #pragma unroll
@@ -449,7 +448,7 @@ PR_DEV uint32_t object_trans(const SetupParams& P, const ObjCache* C, uint32_t t
 
 // Triangle.IsValid of triangle t (from the flags the scene upload computed).
 PR_DEV bool tri_valid_of(const SetupParams& P, uint32_t t, const V4* p) {
-    if (P.tri_flags) return P.tri_flags[t] != 0;
+    if (P.tri_flags) return (P.tri_flags[t] & kTriValid) != 0;
     return tri_is_valid(p[0], p[1], p[2]);
 }
 
@@ -1386,16 +1385,7 @@ __global__ void __launch_bounds__(256) ao_list_kernel(const __grid_constant__ Ao
     bool pending = false;
     if (x < P.W && r < P.H) {
         const uint32_t seq = P.win[i];
-        if (seq != kNone) {
-            const uint32_t t = seq >> 3;
-            int m = P.mat[t];
-            if (m >= 0) {
-                uint32_t o = P.blk_obj[t >> 7];
-                while (o + 1 < P.n_objects && P.obj_first[o + 1] <= t) o++;
-                m += P.obj_matbase[o];
-                pending = m >= 0 && (uint32_t)m < P.n_mats && (P.mats[m].flags & PR_MAT_AO) != 0u;
-            }
-        }
+        pending = seq != kNone && (P.tri_flags[seq >> 3] & kTriAO) != 0;
     }
     const int tid = threadIdx.x + threadIdx.y * blockDim.x, warp = tid >> 5, lane = tid & 31;
     const unsigned msk = __ballot_sync(0xffffffffu, pending);
@@ -1792,10 +1782,21 @@ __global__ void ao_apply_kernel(const __grid_constant__ AoParams P) {
 
 // Triangle.IsValid (geometry/primitive/triangle.go:63-80) of every input
 // triangle, once per scene upload: it depends on model-space positions only.
-__global__ void tri_flags_kernel(const float4* pos, uint32_t n, uint8_t* flags) {
+__global__ void tri_flags_kernel(const float4* pos, uint32_t n, uint8_t* flags, const int32_t* mat,
+                                 const uint32_t* obj_first, const uint32_t* blk_obj, const int32_t* obj_matbase,
+                                 uint32_t n_objects, const pr_material* mats, uint32_t n_mats) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    flags[t] = tri_is_valid(ld4(pos[3 * t]), ld4(pos[3 * t + 1]), ld4(pos[3 * t + 2])) ? 1 : 0;
+    uint8_t f = tri_is_valid(ld4(pos[3 * t]), ld4(pos[3 * t + 1]), ld4(pos[3 * t + 2])) ? kTriValid : 0;
+    // the flat material of the triangle's fragments (MaterialID plus its geometry's base) has AO
+    int m = mat[t];
+    if (m >= 0) {
+        uint32_t o = blk_obj[t >> 7];
+        while (o + 1 < n_objects && obj_first[o + 1] <= t) o++;
+        m += obj_matbase[o];
+        if (m >= 0 && (uint32_t)m < n_mats && (mats[m].flags & PR_MAT_AO)) f |= kTriAO;
+    }
+    flags[t] = f;
 }
 
 // ---------------------------------------------------------------- batches
@@ -2036,9 +2037,12 @@ int launch_shade(const ShadeParams& p, void* stream) {
         shade_kernel<false><<<grd, blk, 0, (cudaStream_t)stream>>>(p);
     return check(cudaGetLastError());
 }
-int launch_tri_flags(const float4* pos, uint32_t n, uint8_t* flags, void* stream) {
+int launch_tri_flags(const float4* pos, uint32_t n, uint8_t* flags, const int32_t* mat, const uint32_t* obj_first,
+                     const uint32_t* blk_obj, const int32_t* obj_matbase, uint32_t n_objects, const pr_material* mats,
+                     uint32_t n_mats, void* stream) {
     if (n == 0) return 0;
-    tri_flags_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(pos, n, flags);
+    tri_flags_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(pos, n, flags, mat, obj_first, blk_obj,
+                                                                          obj_matbase, n_objects, mats, n_mats);
     return check(cudaGetLastError());
 }
 int launch_setup_shadow_batch(const SetupParams* jobs, const uint32_t* blk, int n_jobs, uint32_t n_blocks, void* stream) {

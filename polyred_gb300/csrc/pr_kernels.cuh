@@ -21,6 +21,9 @@ constexpr int kNumCounters = kMaxLights + 2;
 constexpr int kMaxAmbient = 16;
 constexpr uint32_t kTaskShift = 5;  // a raster task is a 2^kTaskShift-pixel chunk of a bbox (default)
 constexpr uint32_t kNone = 0xFFFFFFFFu;
+// Per-triangle flags built at scene upload (tri_flags_kernel)
+constexpr uint8_t kTriValid = 1u;  // Triangle.IsValid
+constexpr uint8_t kTriAO = 2u;     // its fragments' material has AO (AmbientOcclusionShade runs on them)
 
 // Raster record: what the coverage/depth test of one (sub-)triangle needs.
 // 16 words = 64 bytes, read with four 16-byte loads (16-byte aligned so a
@@ -194,13 +197,7 @@ struct AoParams {
 struct AoListParams {
     int W, H;
     const uint32_t* win;         // winning seq per pixel (input triangle = seq >> 3)
-    const int32_t* mat;          // [n_tris] Triangle.MaterialID, geometry-local
-    const uint32_t* obj_first;   // [n_objects + 1]
-    const uint32_t* blk_obj;     // [n_tris / 128] object of each 128-triangle block's first triangle
-    const int32_t* obj_matbase;  // [n_objects]
-    uint32_t n_objects;
-    const pr_material* mats;
-    uint32_t n_mats;
+    const uint8_t* tri_flags;    // [n_tris] kTriAO: the triangle's material has AO
     uint32_t* list;
     Counters* cnt;               // n_ao
 };
@@ -298,7 +295,10 @@ int launch_shade_batch(const ShadeParams* views, const uint32_t* blk, int n_view
 int launch_ao_batch(const AoParams* views, int n_views, uint32_t* chunk_ctr, int n_blocks, void* stream);
 int launch_col_to_float(const uchar4* col, float4* out, size_t n, void* stream);
 int launch_fill_u32(uint32_t* p, uint32_t v, size_t n, void* stream);
-int launch_tri_flags(const float4* pos, uint32_t n, uint8_t* flags, void* stream);
+// Triangle.IsValid (kTriValid) and the AO flag of each triangle's material (kTriAO).
+int launch_tri_flags(const float4* pos, uint32_t n, uint8_t* flags, const int32_t* mat, const uint32_t* obj_first,
+                     const uint32_t* blk_obj, const int32_t* obj_matbase, uint32_t n_objects, const pr_material* mats,
+                     uint32_t n_mats, void* stream);
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream);
 int launch_decode_shadow(const uint32_t* smap, float* out, size_t n, void* stream);
 int launch_pow_probe(const float* x, const float* y, float* fast, float* ref, int n, void* stream);
