@@ -26,6 +26,12 @@ int     pr_testing_fail_alloc(int64_t n);
 /* Allocation attempts (device and page-locked) since the library loaded. */
 int64_t pr_testing_alloc_count(void);
 
+/* The AO march directions (cos, sin: 8 floats each) and, for a W x H frame,
+ * how the device marches each (host only, no device): fast[k] 1 when its
+ * tap offset table is exact, tiny[k] the component (1 = x, 2 = y) that lies
+ * in (-1/99, 0). Returns the number of directions or a negative status. */
+int pr_debug_ao_dirs(int W, int H, float* cosv, float* sinv, int8_t* fast, int8_t* tiny);
+
 /* Device arithmetic probes (one thread per element, n device-resident
  * elements; synchronous): */
 /* the shade kernel's float32 Pow beside the float64 algorithm */

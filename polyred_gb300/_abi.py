@@ -253,6 +253,7 @@ ENTRY_POINTS = [
 TESTING_ENTRY_POINTS = [
     ("pr_testing_fail_alloc", C.c_int, [C.c_int64]),
     ("pr_testing_alloc_count", C.c_int64, []),
+    ("pr_debug_ao_dirs", C.c_int, [C.c_int, C.c_int] + [VP] * 4),
     ("pr_debug_pow_probe", C.c_int, [VP] * 4 + [C.c_int]),
     ("pr_debug_ao_probe", C.c_int, [VP] * 7 + [C.c_int]),
     ("pr_debug_fma_probe", C.c_int, [VP] * 5 + [C.c_int]),

@@ -1270,6 +1270,15 @@ int pr_testing_fail_alloc(int64_t n) {
 
 int64_t pr_testing_alloc_count(void) { return g_alloc_count.load(); }
 
+int pr_debug_ao_dirs(int W, int H, float* cosv, float* sinv, int8_t* fast, int8_t* tiny) {
+    if (!cosv || !sinv || !fast || !tiny) return fail(PR_ERR_INVALID_ARG, "pr_debug_ao_dirs: NULL output");
+    if (W <= 0 || H <= 0) return fail(PR_ERR_INVALID_ARG, "pr_debug_ao_dirs: bad frame size");
+    int n = 0;
+    prh::ao_directions(cosv, sinv, &n);
+    prh::ao_classify(cosv, sinv, n, W, H, fast, tiny);
+    return n;
+}
+
 int pr_host_free(void* ptr) {
     if (!ptr) return fail(PR_ERR_INVALID_ARG, "ptr is NULL");
     cudaError_t e = cudaFreeHost(ptr);
