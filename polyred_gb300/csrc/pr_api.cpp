@@ -802,6 +802,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         rc_.tasks = c->tasks_c.p;
         rc_.cnt = dclip;
         rc_.take = &dclip->take[0];
+        rc_.grab = 32;  // a short list (the frame's clipped triangles): spread it over warps
         KTRY(prk::launch_raster(rc_, c->n_sms * 8, sc));
         CUDA_TRY(cudaEventRecord(c->ev_clip, sc));
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));

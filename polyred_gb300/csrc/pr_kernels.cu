@@ -593,10 +593,63 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
     }
     emit_tasks_warp(P, ridxs, areas, nw);
 }
+
+// clip_one with the fan spread over lanes: a group of kClipLanes lanes takes
+// entry j, every lane of it clips the triangle (the same arithmetic, so the
+// same polygon), and lane `sub` interpolates and writes sub-triangle sub
+// alone. The group's lanes reserve their records in lane order, so its
+// sub-triangles keep consecutive records from first_rec[t]. Each record is
+// the one clip_one writes; only the chain of one lane gets shorter (a
+// frame's few clipped triangles otherwise run as a few long serial threads).
+constexpr int kClipLanes = 8;  // >= the most sub-triangles of a clipped triangle (9 vertices: 7)
+PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint32_t j, uint32_t n, uint32_t sub) {
+    SubVtx v[3];
+    float recipw[3];
+    int matid = -1;
+    bool contained = false;
+    uint32_t t = 0;
+    int nc = 0;
+    V4 clips[10];
+    if (j < n) {
+        t = clip_list[j];
+        transform_main(P, nullptr, t, v, recipw, &matid, &contained);
+        V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
+        nc = sutherland_hodgman(in3, ext_w(P), ext_h(P), clips);
+        if (nc < 0) {
+            atomicOr(&P.cnt->overflow, 4u);
+            nc = 0;
+        }
+    }
+    __syncwarp();
+    const bool mine = (int)sub < nc - 2;
+    uint32_t tot;
+    Counters* crec = P.cnt_rec ? P.cnt_rec : P.cnt;
+    uint32_t ridx = warp_reserve(&crec->n_rec, mine ? 1u : 0u, &tot);
+    uint32_t area = 0;
+    int nw = 0;
+    if (mine) {
+        if (ridx >= P.cap_rec) {
+            atomicOr(&P.cnt->overflow, 1u);
+            atomicMax(&P.cnt->need_rec, ridx + 1u);
+        } else {
+            if (sub == 0) P.first_rec[t] = ridx;
+            const float psabc = sabc_of(v[0].pos.x, v[0].pos.y, v[1].pos.x, v[1].pos.y, v[2].pos.x, v[2].pos.y);
+            SubVtx s[3];
+            s[0] = clip_vertex(clips[0], v, psabc);
+            s[1] = clip_vertex(clips[sub + 1], v, psabc);
+            s[2] = clip_vertex(clips[sub + 2], v, psabc);
+            area = write_sub(P, ridx, t * 8u + sub, s, recipw, matid);
+            nw = 1;
+        }
+    }
+    emit_tasks_warp(P, &ridx, &area, nw);
+}
 __global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ SetupParams P, const uint32_t* clip_list) {
     const uint32_t n = (P.cnt_rec ? P.cnt_rec : P.cnt)->n_clipped;
-    // grid-stride over the list (uniform per block, so every warp calls clip_one whole)
-    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) clip_one(P, clip_list, b + threadIdx.x, n);
+    constexpr uint32_t kPerBlock = 128 / kClipLanes;
+    // grid-stride over the list (uniform per block, so every warp calls clip_one_group whole)
+    for (uint32_t b = blockIdx.x * kPerBlock; b < n; b += gridDim.x * kPerBlock)
+        clip_one_group(P, clip_list, b + threadIdx.x / kClipLanes, n, threadIdx.x % kClipLanes);
 }
 
 // passShadows / drawDepth for one input triangle (render/shadow.go:137-192)
@@ -851,13 +904,15 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
     if (P.take) {
         // Dynamic: a task's cost is its bbox chunk, and consecutive tasks of
         // one object tend to be alike, so a static stride leaves a tail.
-        // four 32-task batches per atomic: one counter serves every warp of the pass
+        // P.grab tasks (four 32-task batches on long lists) per atomic: one
+        // counter serves every warp of the pass
+        const uint32_t grab = P.grab;
         for (;;) {
             uint32_t base = 0;
-            if ((threadIdx.x & 31) == 0) base = atomicAdd(P.take, 128u);
+            if ((threadIdx.x & 31) == 0) base = atomicAdd(P.take, grab);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= n_tasks) break;
-            const uint32_t end = min(base + 128u, n_tasks);
+            const uint32_t end = min(base + grab, n_tasks);
             for (uint32_t b = base; b < end; b += 32u) raster_warp(P, b, n_tasks, s_w[warp]);
         }
         return;
@@ -2001,7 +2056,7 @@ int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uin
 int launch_clip(const SetupParams& p, const uint32_t* clip_list, void* stream) {
     if (p.n_tris == 0) return 0;
     // the list's length is known only on the device: a few blocks per SM stride over it
-    const unsigned nb = std::min((p.n_tris + 127) / 128, (unsigned)sm_count() * 4u);
+    const unsigned nb = std::min((p.n_tris + 15) / 16, (unsigned)sm_count() * 4u);
     clip_kernel<<<nb, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
     return check(cudaGetLastError());
 }

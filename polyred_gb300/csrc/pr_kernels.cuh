@@ -127,8 +127,9 @@ struct RasterParams {
     uint32_t* smap;            // shadow: orderable depth keys, index x + y*W
     uint32_t* lastnan;         // shadow: 1 + max seq of NaN-depth fragments, 0 if none
     uint32_t task_shift = kTaskShift;  // as the setup that wrote the tasks
-    uint32_t* take = nullptr;          // zeroed work-queue head (warps take 32 tasks at a time), or
+    uint32_t* take = nullptr;          // zeroed work-queue head (warps take grab tasks at a time), or
                                        // null: a static stride over the tasks
+    uint32_t grab = 128;               // tasks per queue grab, a multiple of 32 (short lists: 32)
 };
 
 struct ShadeParams {
