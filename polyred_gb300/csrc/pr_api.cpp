@@ -156,7 +156,7 @@ struct SceneBufs {
     HostBuf tables;                        // page-locked staging of the small tables (submitted uploads)
     cudaEvent_t ev_uploaded = nullptr;     // the upload into these buffers has landed
     cudaEvent_t ev_released = nullptr;     // the last frame that read them is past shading
-    cudaEvent_t ev_released_ao = nullptr;  // ... and past listing its AO pixels (stream 3)
+    cudaEvent_t ev_released_ao = nullptr;  // ... and past the frame's AO stream work (stream 3)
     void release() {
         pos.release(); nor.release(); uv.release(); col.release(); mat.release();
         obj_first.release(); tri_flags.release(); obj_model.release(); obj_normal.release();
@@ -510,7 +510,7 @@ void collect_stats(Ctx* c) {
     c->stats.ms_raster = span(c->ev[2], c->ev[3]);
     c->stats.ms_shade = span(c->ev[3], c->ev[4]);
     c->stats.ms_total = span(c->ev[0], c->ev[4]);
-    c->stats.ms_ao = span(c->ev_ao0, c->ev_ao);  // listing and march, beside shading
+    c->stats.ms_ao = span(c->ev_ao0, c->ev_ao);  // the march, beside shading
     c->stats.n_ao_pixels = c->h_cnt[0].n_ao;
 }
 
@@ -813,28 +813,21 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         rc_.take = &dclip->take[1];
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
         KTRY(prk::launch_raster(rc_, c->n_sms * 8, st));
-        KTRY(prk::launch_resolve_listing(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p,
-                                         c->first_rec.p, c->attr_state.p, c->vis_list.p, st));
-        // AmbientOcclusionShade's march needs only the resolved depths: its
-        // pixels are listed and marched on stream 3 (free after the clipped
-        // raster) while stream 1 writes attributes and shades; the colour
-        // scaling joins after shading.
+        // AmbientOcclusionShade's march needs only the resolved depths: resolve
+        // lists its pixels, and they are marched on stream 3 (free after the
+        // clipped raster) while stream 1 writes attributes and shades; the
+        // colour scaling joins after shading.
         const bool with_ao = out && out->rgba;
+        if (with_ao && (rc = c->ao_T.ensure(npx))) return rc;
+        KTRY(prk::launch_resolve_listing(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p,
+                                         c->first_rec.p, c->attr_state.p, c->vis_list.p, c->sb.tri_flags.p,
+                                         with_ao ? c->ao_list.p : nullptr, st));
         prk::AoParams ap{};
         if (with_ao) {
-            if ((rc = c->ao_T.ensure(npx))) return rc;
             CUDA_TRY(cudaEventRecord(c->ev_resolved, st));
             CUDA_TRY(cudaStreamWaitEvent(sc, c->ev_resolved, 0));
             CUDA_TRY(cudaEventRecord(c->ev_ao0, sc));
-            prk::AoListParams lp{};
-            lp.W = W;
-            lp.H = H;
-            lp.win = c->win.p;
-            lp.tri_flags = c->sb.tri_flags.p;
-            lp.list = c->ao_list.p;
-            lp.cnt = dcnt;
-            KTRY(prk::launch_ao_list(lp, sc));
-            CUDA_TRY(cudaEventRecord(c->sb.ev_released_ao, sc));  // the scene buffers are read no more here
+            CUDA_TRY(cudaEventRecord(c->sb.ev_released_ao, sc));  // stream 3 reads no scene buffer
             ap.W = W;
             ap.H = H;
             ap.gamma_on = (f->flags & PR_FRAME_GAMMA) ? 1 : 0;
@@ -846,7 +839,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             ap.T = c->ao_T.p;
             KTRY(prk::launch_ao_T(ap, sc));
             CUDA_TRY(cudaEventRecord(c->ev_ao, sc));
-            launches += 2;
+            launches += 1;
         }
         KTRY(prk::launch_attr(mp, c->vis_list.p, st));
         KTRY(prk::launch_nan_cleanup(npx, c->nanseq.p, 0xFFFFFFFFu, c->beaten.p, 0u, dcnt, st));
@@ -897,7 +890,7 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             if ((rc = c->o_msaa.ensure(npx * 4))) return rc;
             sp.rgba = (uchar4*)c->o_msaa.p;  // the framebuffer's colours
         }
-        sp.ao_listed = 1;  // listed by ao_list_kernel on stream 3
+        sp.ao_listed = 1;  // listed by resolve
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_join, 0));  // the shadow maps are complete
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_d2h, 0));   // a submitted frame's outputs left the staging
         KTRY(prk::launch_shade(sp, st));

@@ -938,40 +938,57 @@ PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint
     depth_ao[i] = d;
 }
 
-// Resolve (resolve_one) that also lists the winners' deferred attribute records:
-// the first pixel to find its record pending (1 -> 2) appends it.
-__global__ void resolve_listing_kernel(int W, int H, const unsigned long long* keys, const uint32_t* nanseq,
-                                       const uint32_t* beaten, Counters* cnt, uint32_t* win, float* depth_ao,
-                                       const uint32_t* first_rec, uint32_t* attr_state, uint32_t* vis) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    resolve_one(W, H, keys, nanseq, beaten, cnt, win, depth_ao, i);
-    bool want = false;
+// Resolve (resolve_one) that also lists the winners' deferred attribute
+// records (the first pixel to find its record pending, 1 -> 2, appends it)
+// and, with ao_list, the frame's AO pixels: every covered pixel whose winning
+// triangle's material has AO (tri_flags kTriAO; AmbientOcclusionShade's own
+// condition, material/ao.go:22), appended tile by tile (32 x 8 blocks, warps
+// in order) for the march's locality. One atomic per block and list.
+__global__ void __launch_bounds__(256) resolve_listing_kernel(int W, int H, const unsigned long long* keys,
+                                                              const uint32_t* nanseq, const uint32_t* beaten,
+                                                              Counters* cnt, uint32_t* win, float* depth_ao,
+                                                              const uint32_t* first_rec, uint32_t* attr_state,
+                                                              uint32_t* vis, const uint8_t* tri_flags,
+                                                              uint32_t* ao_list) {
+    const int x = blockIdx.x * 32 + threadIdx.x, r = blockIdx.y * 8 + threadIdx.y;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    bool want = false, ao = false;
     uint32_t ridx = 0;
-    if (i < (size_t)W * H) {
+    const size_t i = (size_t)r * W + x;
+    if (x < W && r < H) {
+        resolve_one(W, H, keys, nanseq, beaten, cnt, win, depth_ao, i);
         const uint32_t w = win[i];
         if (w != kNone) {
             ridx = first_rec[w >> 3] + (w & 7u);
             // most pixels find their record listed already: a plain read first
             want = attr_state[ridx] == 1u && atomicCAS(&attr_state[ridx], 1u, 2u) == 1u;
+            ao = ao_list && (tri_flags[w >> 3] & kTriAO) != 0;
         }
     }
-    // one atomic per block on the list's counter (256 threads, every one reaches here)
-    __shared__ uint32_t s_cnt[8];
-    __shared__ uint32_t s_base;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned m = __ballot_sync(0xffffffffu, want);
-    if (lane == 0) s_cnt[warp] = (uint32_t)__popc(m);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tot = 0;
-        for (int w = 0; w < 8; w++) tot += s_cnt[w];
-        s_base = tot ? atomicAdd(&cnt->n_vis, tot) : 0u;
+    __shared__ uint32_t s_cnt[2][8];
+    __shared__ uint32_t s_base[2];
+    const unsigned m = __ballot_sync(0xffffffffu, want), ma = __ballot_sync(0xffffffffu, ao);
+    if (lane == 0) {
+        s_cnt[0][warp] = (uint32_t)__popc(m);
+        s_cnt[1][warp] = (uint32_t)__popc(ma);
     }
     __syncthreads();
+    if (warp == 0 && lane < 2) {
+        uint32_t tot = 0;
+        for (int q = 0; q < 8; q++) tot += s_cnt[lane][q];
+        s_base[lane] = tot ? atomicAdd(lane ? &cnt->n_ao : &cnt->n_vis, tot) : 0u;
+    }
+    __syncthreads();
+    const uint32_t below = (1u << lane) - 1u;
     if (want) {
-        uint32_t o = s_base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-        for (int w = 0; w < warp; w++) o += s_cnt[w];
+        uint32_t o = s_base[0] + (uint32_t)__popc(m & below);
+        for (int q = 0; q < warp; q++) o += s_cnt[0][q];
         vis[o] = ridx;
+    }
+    if (ao) {
+        uint32_t o = s_base[1] + (uint32_t)__popc(ma & below);
+        for (int q = 0; q < warp; q++) o += s_cnt[1][q];
+        ao_list[o] = (uint32_t)i;
     }
 }
 
@@ -1426,37 +1443,6 @@ __global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ Shad
     const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
     const bool pending = shade_one<kTex>(P, x, r);
     if (P.ao_list && !P.ao_listed) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
-}
-
-// The shade kernel's AO condition without shading: a covered pixel whose
-// winning triangle's flat material (MaterialID plus its geometry's base, as
-// the setup forms it) exists and has AO. 32 x 8 tiles, one atomic per tile,
-// the order the shade kernel's own append gives.
-__global__ void __launch_bounds__(256) ao_list_kernel(const __grid_constant__ AoListParams P) {
-    __shared__ uint32_t s_cnt[8];
-    __shared__ uint32_t s_base;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
-    const uint32_t i = (uint32_t)r * (uint32_t)P.W + (uint32_t)x;
-    bool pending = false;
-    if (x < P.W && r < P.H) {
-        const uint32_t seq = P.win[i];
-        pending = seq != kNone && (P.tri_flags[seq >> 3] & kTriAO) != 0;
-    }
-    const int tid = threadIdx.x + threadIdx.y * blockDim.x, warp = tid >> 5, lane = tid & 31;
-    const unsigned msk = __ballot_sync(0xffffffffu, pending);
-    if (lane == 0) s_cnt[warp] = (uint32_t)__popc(msk);
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t tot = 0;
-        for (int w = 0; w < 8; w++) tot += s_cnt[w];
-        s_base = tot ? atomicAdd(&P.cnt->n_ao, tot) : 0u;
-    }
-    __syncthreads();
-    if (pending) {
-        uint32_t o = s_base + (uint32_t)__popc(msk & ((1u << lane) - 1u));
-        for (int w = 0; w < warp; w++) o += s_cnt[w];
-        P.list[o] = i;
-    }
 }
 
 // ---------------------------------------------------------------- AO
@@ -2036,10 +2022,12 @@ int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stre
 }
 int launch_resolve_listing(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
                            Counters* cnt, uint32_t* win, float* depth_ao, const uint32_t* first_rec,
-                           uint32_t* attr_state, uint32_t* vis, void* stream) {
-    size_t n = (size_t)W * H;
-    resolve_listing_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        W, H, keys, nanseq, beaten, cnt, win, depth_ao, first_rec, attr_state, vis);
+                           uint32_t* attr_state, uint32_t* vis, const uint8_t* tri_flags, uint32_t* ao_list,
+                           void* stream) {
+    if (W <= 0 || H <= 0) return 0;
+    const dim3 blk(32, 8), grd((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
+    resolve_listing_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(W, H, keys, nanseq, beaten, cnt, win, depth_ao,
+                                                                 first_rec, attr_state, vis, tri_flags, ao_list);
     return check(cudaGetLastError());
 }
 int launch_attr(const SetupParams& p, const uint32_t* vis, void* stream) {
@@ -2220,13 +2208,6 @@ int launch_ao_T(const AoParams& p, void* stream) {
 }
 int launch_ao_apply(const AoParams& p, int n_blocks, void* stream) {
     ao_apply_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(p);
-    return check(cudaGetLastError());
-}
-int launch_ao_list(const AoListParams& p, void* stream) {
-    if (p.W <= 0 || p.H <= 0) return 0;
-    dim3 blk(32, 8);
-    dim3 grd((p.W + 31) / 32, (p.H + 7) / 8);
-    ao_list_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(p);
     return check(cudaGetLastError());
 }
 int set_ao_tables(const float* cosv, const float* sinv, int n, void* stream) {

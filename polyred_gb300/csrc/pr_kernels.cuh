@@ -166,7 +166,7 @@ struct ShadeParams {
     uchar4* gvcol;
     int32_t* gmat;
     uint32_t* ao_list;          // pixels whose material has AO (null: AO off)
-    int ao_listed;              // 1: ao_list_kernel lists them; shade only leaves their pre-AO colour
+    int ao_listed;              // 1: resolve lists them; shade only leaves their pre-AO colour
     Counters* cnt_w;
     // differentiation only (null otherwise)
     const float* tri_scr;       // [n_tris][12] from the main setup
@@ -192,16 +192,6 @@ struct AoParams {
     float* T;            // [list] the AO total of each listed pixel (ao_T_kernel -> ao_apply_kernel)
 };
 
-// The AO pixels of a frame, listed beside shading: every covered pixel whose
-// winning triangle's material has AO (the shade kernel's own condition),
-// appended tile by tile (32 x 8) as the shade kernel would.
-struct AoListParams {
-    int W, H;
-    const uint32_t* win;         // winning seq per pixel (input triangle = seq >> 3)
-    const uint8_t* tri_flags;    // [n_tris] kTriAO: the triangle's material has AO
-    uint32_t* list;
-    Counters* cnt;               // n_ao
-};
 
 // Differentiable shading (pr_diff.cu)
 constexpr int kDiffMaxMats = 256;
@@ -245,10 +235,13 @@ struct PassMats {
 int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uint32_t n_objects, float* out,
                      void* stream);
 // Resolve that also lists, once each, the winning records whose attributes
-// were deferred (attr_state 1 -> 2) in vis (count in cnt->n_vis).
+// were deferred (attr_state 1 -> 2) in vis (count in cnt->n_vis) and, with
+// ao_list, the pixels whose winner's material has AO (tri_flags kTriAO) in
+// ao_list (count in cnt->n_ao), tile by tile (32 x 8).
 int launch_resolve_listing(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
                            Counters* cnt, uint32_t* win, float* depth_ao, const uint32_t* first_rec,
-                           uint32_t* attr_state, uint32_t* vis, void* stream);
+                           uint32_t* attr_state, uint32_t* vis, const uint8_t* tri_flags, uint32_t* ao_list,
+                           void* stream);
 // The attribute records of the records resolve listed (P: the main view's setup parameters).
 int launch_attr(const SetupParams& p, const uint32_t* vis, void* stream);
 int launch_setup_shadow(const SetupParams& p, void* stream);
@@ -259,10 +252,9 @@ int launch_shadow_fixup_reset(int W, int H, const uint32_t* lastnan, uint32_t* s
 int launch_nan_cleanup(size_t n, uint32_t* a, uint32_t va, uint32_t* b, uint32_t vb, const Counters* cnt,
                        void* stream);
 int launch_shade(const ShadeParams& p, void* stream);
-// AO split in three so that its march overlaps shading: the list (after
-// resolve), the march writing p.T (after the list), and the colour scaling
-// and gamma of the listed pixels (after both the march and shading).
-int launch_ao_list(const AoListParams& p, void* stream);
+// AO split so that its march overlaps shading: the list (made by resolve),
+// the march writing p.T (after resolve), and the colour scaling and gamma
+// of the listed pixels (after both the march and shading).
 int launch_ao_T(const AoParams& p, void* stream);
 int launch_ao_apply(const AoParams& p, int n_blocks, void* stream);
 // passAntialiasing's imageutil.Resize of the n*W x n*H image `in` to W x H
