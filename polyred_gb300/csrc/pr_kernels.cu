@@ -904,9 +904,10 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
     if (P.take) {
         // Dynamic: a task's cost is its bbox chunk, and consecutive tasks of
         // one object tend to be alike, so a static stride leaves a tail.
-        // P.grab tasks (four 32-task batches on long lists) per atomic: one
-        // counter serves every warp of the pass
-        const uint32_t grab = P.grab;
+        // P.grab tasks per atomic (one counter serves every warp of the
+        // pass): four 32-task batches on long lists, two on shorter ones,
+        // where larger grabs would leave warps without work
+        const uint32_t grab = P.grab ? P.grab : (n_tasks < gridDim.x * kRasterWarps * 256u ? 64u : 128u);
         for (;;) {
             uint32_t base = 0;
             if ((threadIdx.x & 31) == 0) base = atomicAdd(P.take, grab);

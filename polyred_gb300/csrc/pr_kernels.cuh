@@ -129,7 +129,8 @@ struct RasterParams {
     uint32_t task_shift = kTaskShift;  // as the setup that wrote the tasks
     uint32_t* take = nullptr;          // zeroed work-queue head (warps take grab tasks at a time), or
                                        // null: a static stride over the tasks
-    uint32_t grab = 128;               // tasks per queue grab, a multiple of 32 (short lists: 32)
+    uint32_t grab = 0;                 // tasks per queue grab, a multiple of 32; 0: from the task count
+                                       // (64 below 256 tasks per warp of the grid, else 128)
 };
 
 struct ShadeParams {
