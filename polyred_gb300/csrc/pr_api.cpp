@@ -807,12 +807,14 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         CUDA_TRY(cudaEventRecord(c->ev_clip, sc));
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
         CUDA_TRY(cudaStreamWaitEvent(st, c->ev_clip, 0));
+        // the NaN fix-up of both lists in one launch (it returns at once
+        // without a NaN fragment)
         rp.mode = prk::kMainFixup;
-        rc_.mode = prk::kMainFixup;
         rp.take = &dcnt[0].take[1];
-        rc_.take = &dclip->take[1];
+        rp.tasks2 = c->tasks_c.p;
+        rp.cnt2 = dclip;
+        rp.take2 = &dclip->take[1];
         KTRY(prk::launch_raster(rp, c->n_sms * 8, st));
-        KTRY(prk::launch_raster(rc_, c->n_sms * 8, st));
         // AmbientOcclusionShade's march needs only the resolved depths: resolve
         // lists its pixels, and they are marched on stream 3 (free after the
         // clipped raster) while stream 1 writes attributes and shades; the
@@ -842,9 +844,8 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
             launches += 1;
         }
         KTRY(prk::launch_attr(mp, c->vis_list.p, st));
-        KTRY(prk::launch_nan_cleanup(npx, c->nanseq.p, 0xFFFFFFFFu, c->beaten.p, 0u, dcnt, st));
         CUDA_TRY(cudaEventRecord(c->ev[3], st));
-        launches += 9;
+        launches += 7;
 
         // ---- deferred shading + gamma (render/raster.go:275-378) ----
         std::unique_ptr<prk::ShadeParams> sp_owner(new (std::nothrow) prk::ShadeParams());

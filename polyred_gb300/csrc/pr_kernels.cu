@@ -820,13 +820,13 @@ PR_DEV void raster_pixel(const RasterParams& P, const RasterWarpSm& S, uint32_t 
 
 // Tasks [base, base + 32) of one pass, one per lane, pixels spread over the
 // warp by a prefix scan of their counts.
-PR_DEV void raster_warp(const RasterParams& P, uint32_t base, uint32_t n_tasks, RasterWarpSm& S) {
+PR_DEV void raster_warp(const RasterParams& P, const uint2* tasks, uint32_t base, uint32_t n_tasks, RasterWarpSm& S) {
     const int lane = threadIdx.x & 31;
     uint32_t ti = base + lane;
     int cnt = 0;
     uint32_t qx0 = 0;
     if (ti < n_tasks) {
-        uint2 tk = P.tasks[ti];
+        uint2 tk = tasks[ti];
         const float4* rp = reinterpret_cast<const float4*>(P.rrec + tk.x);
         const float4 q0 = rp[0], q1 = rp[1], q2 = rp[2], q3 = rp[3];
         // record: A.xyz, B.xyz, C.xyz, Sabc, packed bbox x and y ranges, seq
@@ -907,19 +907,23 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
         // P.grab tasks per atomic (one counter serves every warp of the
         // pass): four 32-task batches on long lists, two on shorter ones,
         // where larger grabs would leave warps without work
-        const uint32_t grab = P.grab ? P.grab : (n_tasks < gridDim.x * kRasterWarps * 256u ? 64u : 128u);
-        for (;;) {
-            uint32_t base = 0;
-            if ((threadIdx.x & 31) == 0) base = atomicAdd(P.take, grab);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base >= n_tasks) break;
-            const uint32_t end = min(base + grab, n_tasks);
-            for (uint32_t b = base; b < end; b += 32u) raster_warp(P, b, n_tasks, s_w[warp]);
-        }
+        auto drain = [&](const uint2* tasks, uint32_t* take, uint32_t n) {
+            const uint32_t grab = P.grab ? P.grab : (n < gridDim.x * kRasterWarps * 256u ? 64u : 128u);
+            for (;;) {
+                uint32_t base = 0;
+                if ((threadIdx.x & 31) == 0) base = atomicAdd(take, grab);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base >= n) break;
+                const uint32_t end = min(base + grab, n);
+                for (uint32_t b = base; b < end; b += 32u) raster_warp(P, tasks, b, n, s_w[warp]);
+            }
+        };
+        drain(P.tasks, P.take, n_tasks);
+        if (P.tasks2 && !P.cnt2->overflow) drain(P.tasks2, P.take2, P.cnt2->n_tasks);
         return;
     }
     const uint32_t gw = blockIdx.x * kRasterWarps + warp, nw = gridDim.x * kRasterWarps;
-    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) raster_warp(P, base, n_tasks, s_w[warp]);
+    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) raster_warp(P, P.tasks, base, n_tasks, s_w[warp]);
 }
 
 PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
@@ -946,7 +950,7 @@ PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint
 // condition, material/ao.go:22), appended tile by tile (32 x 8 blocks, warps
 // in order) for the march's locality. One atomic per block and list.
 __global__ void __launch_bounds__(256) resolve_listing_kernel(int W, int H, const unsigned long long* keys,
-                                                              const uint32_t* nanseq, const uint32_t* beaten,
+                                                              uint32_t* nanseq, uint32_t* beaten,
                                                               Counters* cnt, uint32_t* win, float* depth_ao,
                                                               const uint32_t* first_rec, uint32_t* attr_state,
                                                               uint32_t* vis, const uint8_t* tri_flags,
@@ -958,6 +962,11 @@ __global__ void __launch_bounds__(256) resolve_listing_kernel(int W, int H, cons
     const size_t i = (size_t)r * W + x;
     if (x < W && r < H) {
         resolve_one(W, H, keys, nanseq, beaten, cnt, win, depth_ao, i);
+        // the NaN bookkeeping back to its rest state (resolve reads it last)
+        if (cnt->nan_flag && nanseq[i] != kNone) {
+            nanseq[i] = kNone;
+            beaten[i] = 0u;
+        }
         const uint32_t w = win[i];
         if (w != kNone) {
             ridx = first_rec[w >> 3] + (w & 7u);
@@ -1928,7 +1937,7 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_batch_kernel(const R
         if (it >= total) break;
         const int j = job_of(items, n_jobs, it);
         const RasterParams& P = jobs[j];
-        raster_warp(P, (it - items[j]) * 32u, P.cnt->n_tasks, s_w[warp]);
+        raster_warp(P, P.tasks, (it - items[j]) * 32u, P.cnt->n_tasks, s_w[warp]);
     }
 }
 
@@ -2021,7 +2030,7 @@ int launch_setup_main_only(const SetupParams& p, uint32_t* clip_list, void* stre
     setup_main_kernel<<<(p.n_tris + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p, clip_list);
     return check(cudaGetLastError());
 }
-int launch_resolve_listing(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
+int launch_resolve_listing(int W, int H, const unsigned long long* keys, uint32_t* nanseq, uint32_t* beaten,
                            Counters* cnt, uint32_t* win, float* depth_ao, const uint32_t* first_rec,
                            uint32_t* attr_state, uint32_t* vis, const uint8_t* tri_flags, uint32_t* ao_list,
                            void* stream) {

@@ -131,6 +131,12 @@ struct RasterParams {
                                        // null: a static stride over the tasks
     uint32_t grab = 0;                 // tasks per queue grab, a multiple of 32; 0: from the task count
                                        // (64 below 256 tasks per warp of the grid, else 128)
+    // a second task list drained after the first (its own counters and
+    // queue head, the same records): the NaN fix-up of the main and the
+    // clipped lists in one launch
+    const uint2* tasks2 = nullptr;
+    const Counters* cnt2 = nullptr;
+    uint32_t* take2 = nullptr;
 };
 
 struct ShadeParams {
@@ -236,10 +242,12 @@ struct PassMats {
 int launch_obj_trans(const PassMats& pm, int n_pass, const float* obj_model, uint32_t n_objects, float* out,
                      void* stream);
 // Resolve that also lists, once each, the winning records whose attributes
-// were deferred (attr_state 1 -> 2) in vis (count in cnt->n_vis) and, with
+// were deferred (attr_state 1 -> 2) in vis (count in cnt->n_vis), puts the
+// NaN bookkeeping (nanseq, beaten) back to kNone / 0 after a frame that used
+// it, and, with
 // ao_list, the pixels whose winner's material has AO (tri_flags kTriAO) in
 // ao_list (count in cnt->n_ao), tile by tile (32 x 8).
-int launch_resolve_listing(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
+int launch_resolve_listing(int W, int H, const unsigned long long* keys, uint32_t* nanseq, uint32_t* beaten,
                            Counters* cnt, uint32_t* win, float* depth_ao, const uint32_t* first_rec,
                            uint32_t* attr_state, uint32_t* vis, const uint8_t* tri_flags, uint32_t* ao_list,
                            void* stream);
