@@ -53,8 +53,11 @@ static __device__ __noinline__ float fma64f_slow(float a, float b, float c) {
 PR_DEV float fma64f_try(float a, float b, float c, bool& bad) {
     const float r1 = __fmaf_rn(a, b, c);
     // a zero first factor (a matrix entry, usually warp-uniform): s = c + (+-0)
-    // rounds to c in both precisions
-    if (a == 0.0f) return r1;
+    // rounds to c in both precisions; a zero addend (the w terms of direction
+    // vectors, usually warp-uniform): the product of two floats is exact in
+    // float64, so s = ab + (+-0) is rounded once, to r1, with the same sign
+    // of zero
+    if (a == 0.0f || c == 0.0f) return r1;
     const float p = __fmul_rn(a, b);
     const float q = __fmaf_rn(a, b, -p);
     const float sg = __fadd_rn(p, c);

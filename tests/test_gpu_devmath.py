@@ -64,6 +64,8 @@ def test_fma64f_matches_fp64(native_lib):
         tuple(sm),
         _bits(n, 3, 0, 256),    # every exponent: subnormals, zeros, infinities, NaNs
         _bits(n, 4, 90, 170),
+        # zero addends of either sign (the shortcut for c = +-0): every exponent of a and b
+        _bits(n, 5, 0, 256)[:2] + (np.where(g.integers(0, 2, n) == 1, np.float32(0.0), np.float32(-0.0)),),
     ]
     for a, b, c in sets:
         ta, tb, tc = (torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (a, b, c))
