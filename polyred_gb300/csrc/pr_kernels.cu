@@ -733,7 +733,35 @@ struct RasterWarpSm {
     int start[32];    // first warp pixel of each task
     uint32_t tq[32];  // the task's first bbox index minus start (mod 2^32)
     uint32_t q[64];   // (slot << 27) | bbox index t (t < 2^17)
+    uint32_t zk[32];  // early depth test: key of a bound on the record's depths (kNoEarlyZ: none)
 };
+
+// Early depth test. Visibility keeps the largest key per texel or pixel, so
+// a fragment whose key cannot exceed the value already there changes
+// nothing (values only grow during a pass). For a triangle with finite
+// vertex depths Zi, a covered pixel (every computed barycentric b >=
+// -Epsilon) gets z = RN(RN(RN(b0 Z0) + RN(b1 Z1)) + RN(b2 Z2)) with
+// |sum b - 1| <= eta = (dA + 3 dS) / |Sabc| + 3u (1.06) (the sub-areas' and
+// Sabc's rounding, as in tighten_box, and the divisions'), so z <= max Zi +
+// M (eta + 6 Epsilon + 8u), M = max |Zi|, while eta <= 0.05 (b <= 1.06). The
+// raster skips, before the exact test, every pixel whose current value is
+// at least that bound's key (a stale read is only smaller: still sound).
+constexpr uint32_t kNoEarlyZ = 0xFFFFFFFFu;  // no depth key reaches it (NaN depths take the NaN path)
+PR_DEV uint32_t early_z_key(float ax, float ay, float bx, float by, float cx, float cy, float sabc, float4 zs) {
+    const float z0 = zs.x, z1 = zs.y, z2 = zs.z;
+    if (!(isfinite(z0) && isfinite(z1) && isfinite(z2) && isfinite(sabc) && sabc != 0.0f)) return kNoEarlyZ;
+    const float mnx = fminf(fminf(ax, bx), cx), mxx = fmaxf(fmaxf(ax, bx), cx);
+    const float mny = fminf(fminf(ay, by), cy), mxy = fmaxf(fmaxf(ay, by), cy);
+    const float E = __fadd_ru(__fsub_ru(mxx, mnx), __fsub_ru(mxy, mny)), U = __fadd_ru(E, 4.0f);
+    const float k6u = 3.6e-7f;  // >= 6 * 2^-24
+    const float dS = __fmul_ru(__fmul_ru(k6u, E), U), dA = __fmul_ru(__fmul_ru(k6u, E), E);
+    const float eta = __fdiv_ru(__fadd_ru(dA, __fmul_ru(3.0f, dS)), fabsf(sabc));
+    if (!(eta <= 0.05f)) return kNoEarlyZ;
+    const float M = fmaxf(fmaxf(fabsf(z0), fabsf(z1)), fabsf(z2));
+    // 3u (1.06) + 6 Epsilon + 8u < 1.3e-6
+    const float zb = __fadd_ru(fmaxf(fmaxf(z0, z1), z2), __fmul_ru(M, __fadd_ru(eta, 1.5e-6f)));
+    return isfinite(zb) ? fkey(zb) : kNoEarlyZ;
+}
 
 // bbox index t of a record's pixel -> (px, py). t < 2^17 and bw <= 2^14, so
 // t * bw < 2^32 and the multiply-high quotient is exact.
@@ -820,7 +848,8 @@ PR_DEV void raster_pixel(const RasterParams& P, const RasterWarpSm& S, uint32_t 
 
 // Tasks [base, base + 32) of one pass, one per lane, pixels spread over the
 // warp by a prefix scan of their counts.
-PR_DEV void raster_warp(const RasterParams& P, const uint2* tasks, uint32_t base, uint32_t n_tasks, RasterWarpSm& S) {
+PR_DEV void raster_warp(const RasterParams& P, const uint2* tasks, uint32_t base, uint32_t n_tasks, RasterWarpSm& S,
+                        bool early_z) {
     const int lane = threadIdx.x & 31;
     uint32_t ti = base + lane;
     int cnt = 0;
@@ -840,6 +869,8 @@ PR_DEV void raster_warp(const RasterParams& P, const uint2* tasks, uint32_t base
         const float inv = (as >= 1e-30f && as <= 1e30f) ? __frcp_rn(sabc) : 0.0f;
         s.e1 = make_float4(__fsub_rn(cx, bx), __fsub_rn(cy, by), inv, sabc);
         s.zs = make_float4(q0.z, q1.y, q2.x, q3.x);
+        S.zk[lane] = (early_z && (P.mode == kMain || P.mode == kShadow)) ? early_z_key(ax, ay, bx, by, cx, cy, sabc, s.zs)
+                                                                          : kNoEarlyZ;
         if (x0 <= x1 && y0 <= y1) {
             const uint32_t bw = x1 - x0 + 1, area = bw * (y1 - y0 + 1);
             const uint32_t k0 = tk.y << P.task_shift;
@@ -875,6 +906,14 @@ PR_DEV void raster_warp(const RasterParams& P, const uint2* tasks, uint32_t base
             int px, py;
             rec_pixel(r.bb, t, &px, &py);
             keep = !pixel_rejected(r, px, py);
+            const uint32_t zk = S.zk[j];
+            if (keep && zk != kNoEarlyZ) {
+                if (P.mode == kShadow)
+                    keep = __ldcg(P.smap + ((size_t)px + (size_t)py * P.W)) < zk;
+                else
+                    keep = __ldcg(P.keys + ((size_t)(P.H - 1 - py) * P.W + px)) <
+                           (((unsigned long long)zk << 32) | 0xFFFFFFFFull);
+            }
             ent = ((uint32_t)j << 27) | t;
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -892,7 +931,7 @@ PR_DEV void raster_warp(const RasterParams& P, const uint2* tasks, uint32_t base
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_constant__ RasterParams P) {
+__global__ void __launch_bounds__(kRasterWarps * 32, 6) raster_kernel(const __grid_constant__ RasterParams P) {
     __shared__ RasterWarpSm s_w[kRasterWarps];
     const Counters* c = P.cnt;
     if (P.mode == kMainFixup || P.mode == kShadowFixup) {
@@ -907,15 +946,19 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
         // P.grab tasks per atomic (one counter serves every warp of the
         // pass): four 32-task batches on long lists, two on shorter ones,
         // where larger grabs would leave warps without work
+        // The early depth test pays on passes with many fragments per pixel;
+        // on short lists its extra read only lengthens each warp's chain.
         auto drain = [&](const uint2* tasks, uint32_t* take, uint32_t n) {
-            const uint32_t grab = P.grab ? P.grab : (n < gridDim.x * kRasterWarps * 256u ? 64u : 128u);
+            const uint32_t nw = gridDim.x * kRasterWarps;
+            const uint32_t grab = P.grab ? P.grab : (n < nw * 256u ? 64u : 128u);
+            const bool early_z = n >= nw * 32u;
             for (;;) {
                 uint32_t base = 0;
                 if ((threadIdx.x & 31) == 0) base = atomicAdd(take, grab);
                 base = __shfl_sync(0xffffffffu, base, 0);
                 if (base >= n) break;
                 const uint32_t end = min(base + grab, n);
-                for (uint32_t b = base; b < end; b += 32u) raster_warp(P, tasks, b, n, s_w[warp]);
+                for (uint32_t b = base; b < end; b += 32u) raster_warp(P, tasks, b, n, s_w[warp], early_z);
             }
         };
         drain(P.tasks, P.take, n_tasks);
@@ -923,7 +966,8 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_kernel(const __grid_
         return;
     }
     const uint32_t gw = blockIdx.x * kRasterWarps + warp, nw = gridDim.x * kRasterWarps;
-    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u) raster_warp(P, P.tasks, base, n_tasks, s_w[warp]);
+    for (uint32_t base = gw * 32u; base < n_tasks; base += nw * 32u)
+        raster_warp(P, P.tasks, base, n_tasks, s_w[warp], n_tasks >= nw * 32u);
 }
 
 PR_DEV void resolve_one(int W, int H, const unsigned long long* keys, const uint32_t* nanseq, const uint32_t* beaten,
@@ -1925,7 +1969,7 @@ __global__ void __launch_bounds__(1024) batch_scan_kernel(const RasterParams* jo
 
 // Persistent raster over every pass of a batch: each warp takes the next
 // (pass, warp batch) item from the global queue.
-__global__ void __launch_bounds__(kRasterWarps * 32) raster_batch_kernel(const RasterParams* jobs, const uint32_t* items,
+__global__ void __launch_bounds__(kRasterWarps * 32, 6) raster_batch_kernel(const RasterParams* jobs, const uint32_t* items,
                                                                          int n_jobs, uint32_t* queue) {
     __shared__ RasterWarpSm s_w[kRasterWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1937,7 +1981,7 @@ __global__ void __launch_bounds__(kRasterWarps * 32) raster_batch_kernel(const R
         if (it >= total) break;
         const int j = job_of(items, n_jobs, it);
         const RasterParams& P = jobs[j];
-        raster_warp(P, P.tasks, (it - items[j]) * 32u, P.cnt->n_tasks, s_w[warp]);
+        raster_warp(P, P.tasks, (it - items[j]) * 32u, P.cnt->n_tasks, s_w[warp], true);
     }
 }
 
