@@ -153,6 +153,7 @@ struct SceneBufs {
     DevBuf<prt::TexDesc> tex;
     DevBuf<int32_t> mat_tex;               // [n_materials] texture of each material, -1: uniform
     bool has_tex = false;
+    bool has_ao = false;                   // a material has ambient occlusion
     HostBuf tables;                        // page-locked staging of the small tables (submitted uploads)
     cudaEvent_t ev_uploaded = nullptr;     // the upload into these buffers has landed
     cudaEvent_t ev_released = nullptr;     // the last frame that read them is past shading
@@ -162,7 +163,7 @@ struct SceneBufs {
         obj_first.release(); tri_flags.release(); obj_model.release(); obj_normal.release();
         obj_matbase.release(); dmats.release(); blk_obj.release(); tables.release();
         texels.release(); tex.release(); mat_tex.release();
-        has_tex = false;
+        has_tex = has_ao = false;
         if (ev_uploaded) cudaEventDestroy(ev_uploaded);
         if (ev_released) cudaEventDestroy(ev_released);
         if (ev_released_ao) cudaEventDestroy(ev_released_ao);
@@ -227,6 +228,7 @@ struct Ctx {
     // AO's march on stream 3 beside attributes and shading: after resolve,
     // joined before the AO colour scaling
     cudaEvent_t ev_resolved = nullptr, ev_ao0 = nullptr, ev_ao = nullptr;
+    bool ao_marched = false;  // the last frame ran the AO march (ev_ao0, ev_ao hold it)
     DevBuf<float> ao_T;
     int n_sms = 1;
 };
@@ -390,6 +392,8 @@ int scene_fill(SceneBufs& b, const pr_scene_desc* s, cudaStream_t st, bool stage
     }
     b.objects.assign(s->objects, s->objects + no);
     b.materials.assign(s->materials, s->materials + nm);
+    b.has_ao = false;
+    for (uint32_t m = 0; m < nm; m++) b.has_ao |= (s->materials[m].flags & PR_MAT_AO) != 0;
     b.n_tris = n;
     return PR_OK;
 }
@@ -510,7 +514,7 @@ void collect_stats(Ctx* c) {
     c->stats.ms_raster = span(c->ev[2], c->ev[3]);
     c->stats.ms_shade = span(c->ev[3], c->ev[4]);
     c->stats.ms_total = span(c->ev[0], c->ev[4]);
-    c->stats.ms_ao = span(c->ev_ao0, c->ev_ao);  // the march, beside shading
+    c->stats.ms_ao = c->ao_marched ? span(c->ev_ao0, c->ev_ao) : 0.0f;  // the march, beside shading
     c->stats.n_ao_pixels = c->h_cnt[0].n_ao;
 }
 
@@ -818,8 +822,10 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         // AmbientOcclusionShade's march needs only the resolved depths: resolve
         // lists its pixels, and they are marched on stream 3 (free after the
         // clipped raster) while stream 1 writes attributes and shades; the
-        // colour scaling joins after shading.
-        const bool with_ao = out && out->rgba;
+        // colour scaling joins after shading. A scene without an AO material
+        // lists no pixel, and both launches are left out.
+        const bool with_ao = out && out->rgba && c->sb.has_ao;
+        c->ao_marched = with_ao;
         if (with_ao && (rc = c->ao_T.ensure(npx))) return rc;
         KTRY(prk::launch_resolve_listing(W, H, c->keys.p, c->nanseq.p, c->beaten.p, dcnt, c->win.p, c->depth_ao.p,
                                          c->first_rec.p, c->attr_state.p, c->vis_list.p, c->sb.tri_flags.p,
@@ -899,14 +905,16 @@ int render_impl(Ctx* c, const pr_frame_desc* f, pr_outputs* out, bool sync, cons
         CUDA_TRY(cudaEventRecord(c->sb.ev_released, st));  // the scene buffers are read no more
         CUDA_TRY(cudaEventRecord(c->ev[5], st));
         if (sp.rgba) {
-            // AmbientOcclusionShade's colour scaling and gamma of the listed
-            // pixels, once their march (stream 3) and shading are done
-            CUDA_TRY(cudaStreamWaitEvent(st, c->ev_ao, 0));
-            ap.rgba = sp.rgba;
-            ap.dgb = dh ? dh->dgb : nullptr;
-            std::memcpy(ap.gamma, sp.gamma, 256);
-            KTRY(prk::launch_ao_apply(ap, c->n_sms * 4, st));
-            launches += 1;
+            if (with_ao) {
+                // AmbientOcclusionShade's colour scaling and gamma of the listed
+                // pixels, once their march (stream 3) and shading are done
+                CUDA_TRY(cudaStreamWaitEvent(st, c->ev_ao, 0));
+                ap.rgba = sp.rgba;
+                ap.dgb = dh ? dh->dgb : nullptr;
+                std::memcpy(ap.gamma, sp.gamma, 256);
+                KTRY(prk::launch_ao_apply(ap, c->n_sms * 4, st));
+                launches += 1;
+            }
             if (M > 1) {
                 KTRY(prk::launch_msaa_resize(sp.rgba, W, H, rgba_img, W_img, H_img, st));
                 launches += 1;

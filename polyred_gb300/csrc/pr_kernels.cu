@@ -362,20 +362,34 @@ PR_DEV uint32_t warp_reserve(uint32_t* counter, uint32_t n, uint32_t* total) {
 PR_DEV uint32_t n_tasks_of(uint32_t area, uint32_t shift) { return (area + (1u << shift) - 1u) >> shift; }
 
 // Write the raster tasks of up to 8 records (areas given); all lanes call.
+// A lane with one record of more than kWarpEmit tasks (a large triangle:
+// thousands of tasks for a ground plane) leaves their writing to the whole
+// warp, which would otherwise wait on that lane's serial stores.
+constexpr uint32_t kWarpEmit = 8;
 PR_DEV void emit_tasks_warp(const SetupParams& P, const uint32_t* ridx, const uint32_t* area, int n) {
     uint32_t mine = 0;
     for (int i = 0; i < n; i++) mine += n_tasks_of(area[i], P.task_shift);
     uint32_t tot;
     uint32_t o = warp_reserve(&P.cnt->n_tasks, mine, &tot);
-    if (mine == 0) return;
-    if (o + mine > P.cap_tasks) {
+    if (tot == 0) return;  // warp-uniform
+    const bool fits = o + mine <= P.cap_tasks;
+    if (mine != 0 && !fits) {
         atomicOr(&P.cnt->overflow, 2u);
         atomicMax(&P.cnt->need_tasks, o + mine);
-        return;
     }
-    for (int i = 0; i < n; i++) {
-        uint32_t nt = n_tasks_of(area[i], P.task_shift);
-        for (uint32_t c = 0; c < nt; c++) P.tasks[o++] = make_uint2(ridx[i], c);
+    const bool shared = fits && n == 1 && mine > kWarpEmit;
+    if (fits && !shared) {
+        for (int i = 0; i < n; i++) {
+            uint32_t nt = n_tasks_of(area[i], P.task_shift);
+            for (uint32_t c = 0; c < nt; c++) P.tasks[o++] = make_uint2(ridx[i], c);
+        }
+    }
+    const uint32_t r0 = n > 0 ? ridx[0] : 0u;
+    for (unsigned big = __ballot_sync(0xffffffffu, shared); big; big &= big - 1u) {
+        const int l = __ffs(big) - 1;
+        const uint32_t lo = __shfl_sync(0xffffffffu, o, l), ln = __shfl_sync(0xffffffffu, mine, l);
+        const uint32_t lr = __shfl_sync(0xffffffffu, r0, l);
+        for (uint32_t c = lane_id(); c < ln; c += 32u) P.tasks[lo + c] = make_uint2(lr, c);
     }
 }
 
@@ -931,6 +945,7 @@ PR_DEV void raster_warp(const RasterParams& P, const uint2* tasks, uint32_t base
     __syncwarp();
 }
 
+constexpr uint32_t kSpreadShare = 33;  // lists with fewer tasks per warp than this (and than grab) are spread
 __global__ void __launch_bounds__(kRasterWarps * 32, 6) raster_kernel(const __grid_constant__ RasterParams P) {
     __shared__ RasterWarpSm s_w[kRasterWarps];
     const Counters* c = P.cnt;
@@ -948,17 +963,30 @@ __global__ void __launch_bounds__(kRasterWarps * 32, 6) raster_kernel(const __gr
         // where larger grabs would leave warps without work
         // The early depth test pays on passes with many fragments per pixel;
         // on short lists its extra read only lengthens each warp's chain.
+        // A list of fewer than grab tasks per warp (a small frame: a few
+        // thousand tasks, mostly from one or two large triangles) is spread
+        // over every warp instead, down to one task each, by warp index: the
+        // pass then lasts one or two small batches rather than grab tasks in
+        // a few warps, and no warp waits on the counter. Its batches being
+        // small, a block that becomes resident late adds little.
         auto drain = [&](const uint2* tasks, uint32_t* take, uint32_t n) {
             const uint32_t nw = gridDim.x * kRasterWarps;
             const uint32_t grab = P.grab ? P.grab : (n < nw * 256u ? 64u : 128u);
             const bool early_z = n >= nw * 32u;
+            if (n / nw < min(grab, kSpreadShare)) {
+                // spread: batches of max(n / nw, 1) tasks by warp index, at most two per warp
+                const uint32_t g = max(n / nw, 1u);
+                for (uint32_t base = (blockIdx.x * kRasterWarps + (uint32_t)warp) * g; base < n; base += nw * g)
+                    raster_warp(P, tasks, base, min(base + g, n), s_w[warp], early_z);  // g <= 32
+                return;
+            }
             for (;;) {
                 uint32_t base = 0;
                 if ((threadIdx.x & 31) == 0) base = atomicAdd(take, grab);
                 base = __shfl_sync(0xffffffffu, base, 0);
                 if (base >= n) break;
                 const uint32_t end = min(base + grab, n);
-                for (uint32_t b = base; b < end; b += 32u) raster_warp(P, tasks, b, n, s_w[warp], early_z);
+                for (uint32_t b = base; b < end; b += 32u) raster_warp(P, tasks, b, end, s_w[warp], early_z);
             }
         };
         drain(P.tasks, P.take, n_tasks);

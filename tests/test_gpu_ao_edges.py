@@ -20,9 +20,9 @@ def _ao_material():
                          shininess=32, ambient_occlusion=True)
 
 
-def _scene(W, H, eye, seed=0xA0E5, n=40):
+def _scene(W, H, eye, seed=0xA0E5, n=40, m=None):
     """A ground plane in front of the camera and spheres of several sizes."""
-    m = _ao_material()
+    m = _ao_material() if m is None else m
     objs = [sc.Geometry(procedural.ground_plane(30.0, -1.0, material_id=0), m).translate(0.0, 0.0, -14.0)]
     rng = np.random.default_rng(seed)
     for _ in range(n):
@@ -60,3 +60,25 @@ def test_grazing_and_steep_views_with_ao(device, eye):
     W, H = 256, 160
     s, cam = _scene(W, H, eye)
     _frame(device, s, cam, W, H, 0.3)
+
+
+def test_scene_without_ao_material_skips_the_march(device):
+    """A scene none of whose materials has AO lists no pixel: the march and
+    the colour scaling are left out (two launches fewer) and the frame stays
+    bit-exact; uploading an AO scene into the same context brings them back."""
+    W, H = 160, 120
+    s_ao, cam = _scene(W, H, (5.0, 1.0, 4.0), n=12)
+    plain = sc.BlinnPhong(diffuse=sc.color_from_value(0.8, 0.3, 0.2, 1.0),
+                          specular=sc.color_from_value(0.5, 0.5, 0.5, 1.0), shininess=32)
+    s_plain, _ = _scene(W, H, (5.0, 1.0, 4.0), n=12, m=plain)
+    stats = []
+    for s in (s_ao, s_plain, s_ao):
+        p = Pair(device, options(s, cam, W, H))
+        gpu, cpu = p.frame()
+        assert_bitexact(gpu, cpu)
+        stats.append(p.stats)
+    assert stats[0]["n_ao_pixels"] > 0 and stats[0]["ms_ao"] > 0
+    assert stats[1]["n_ao_pixels"] == 0 and stats[1]["ms_ao"] == 0
+    assert stats[1]["n_kernel_launches"] == stats[0]["n_kernel_launches"] - 2
+    assert stats[2]["n_ao_pixels"] == stats[0]["n_ao_pixels"]
+    assert stats[2]["n_kernel_launches"] == stats[0]["n_kernel_launches"]
