@@ -259,10 +259,16 @@ PR_DEV int sutherland_hodgman(const V4* in3, float w, float h, V4* out) {
 // does not.
 __device__ __noinline__ V4 apply4_outline(V4 v, const float* m) { return apply4(v, m); }
 
-// Build and store the records of one sub-triangle; returns its pixel area
-// (0 = nothing to raster) and writes its bbox words.
+// A screen-space vertex back in world space (render/raster.go:467-469).
+PR_DEV V4 world_of(const SetupParams& P, V4 pos) {
+    return apply4_outline(apply4_outline(apply4_outline(pos, P.viewport_inv), P.proj_inv), P.view_inv);
+}
+
 // The attribute record of record ridx (drawClipped's per-vertex inputs).
-PR_DEV void write_attr(const SetupParams& P, uint32_t ridx, const SubVtx* v, const float* recipw, int matid) {
+// mw: the vertices' world positions when the caller has them (the chain
+// below of each vertex's screen position), else null.
+PR_DEV void write_attr(const SetupParams& P, uint32_t ridx, const SubVtx* v, const float* recipw, int matid,
+                       const V4* mw) {
     AttrRec A;
     V4 m[3];
 #pragma unroll
@@ -275,7 +281,7 @@ PR_DEV void write_attr(const SetupParams& P, uint32_t ridx, const SubVtx* v, con
         A.uv[k * 2 + 1] = v[k].v;
         A.col[k] = v[k].col;
         // render/raster.go:467-469
-        m[k] = apply4_outline(apply4_outline(apply4_outline(v[k].pos, P.viewport_inv), P.proj_inv), P.view_inv);
+        m[k] = mw ? mw[k] : world_of(P, v[k].pos);
         A.m[k * 3 + 0] = m[k].x;
         A.m[k * 3 + 1] = m[k].y;
         A.m[k * 3 + 2] = m[k].z;
@@ -295,7 +301,7 @@ PR_DEV void write_attr(const SetupParams& P, uint32_t ridx, const SubVtx* v, con
 // attribute record is left to attr_kernel, which writes it only for records
 // that win a pixel.
 PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, const SubVtx* v, const float* recipw,
-                          int matid) {
+                          int matid, const V4* mw = nullptr) {
     RasterRec R;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -315,7 +321,7 @@ PR_DEV uint32_t write_sub(const SetupParams& P, uint32_t ridx, uint32_t seq, con
 #pragma unroll
     for (int k = 0; k < 4; k++) rd[k] = rs[k];
     if (P.attr_state) P.attr_state[ridx] = P.defer_attr ? 1u : 0u;
-    if (P.arec && !P.defer_attr) write_attr(P, ridx, v, recipw, matid);
+    if (P.arec && !P.defer_attr) write_attr(P, ridx, v, recipw, matid, mw);
     return area;
 }
 
@@ -608,30 +614,76 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
     emit_tasks_warp(P, ridxs, areas, nw);
 }
 
-// clip_one with the fan spread over lanes: a group of kClipLanes lanes takes
-// entry j, every lane of it clips the triangle (the same arithmetic, so the
-// same polygon), and lane `sub` interpolates and writes sub-triangle sub
-// alone. The group's lanes reserve their records in lane order, so its
-// sub-triangles keep consecutive records from first_rec[t]. Each record is
-// the one clip_one writes; only the chain of one lane gets shorter (a
-// frame's few clipped triangles otherwise run as a few long serial threads).
+// clip_one with the work spread over a group of kClipLanes lanes per listed
+// triangle. Lane k < 3 transforms vertex k (screen position, -1/W, normal);
+// every lane then clips the triangle (the same arithmetic, so the same
+// polygon); lane q re-interpolates polygon vertex q (and q + 8) with its
+// world position; lane `sub` assembles and writes fan sub-triangle sub. Each
+// value is the one clip_one computes, from the same inputs in the same
+// order; a warp just issues each per-vertex step once instead of once per
+// vertex (a frame's few clipped triangles are a serial chain, often on
+// cold instruction caches). The group's lanes reserve their records in lane
+// order, so its sub-triangles keep consecutive records from first_rec[t].
 constexpr int kClipLanes = 8;  // >= the most sub-triangles of a clipped triangle (9 vertices: 7)
-PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint32_t j, uint32_t n, uint32_t sub) {
+struct ClipGroupSm {
+    V4 pos[3], nor[3];
+    float recipw[3];
+    SubVtx cv[9];  // the polygon's re-interpolated vertices
+    V4 mw[9];      // and their world positions
+};
+PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint32_t j, uint32_t n, uint32_t sub,
+                           ClipGroupSm& G) {
     SubVtx v[3];
     float recipw[3];
     int matid = -1;
-    bool contained = false;
     uint32_t t = 0;
     int nc = 0;
     V4 clips[10];
     if (j < n) {
         t = clip_list[j];
-        transform_main(P, nullptr, t, v, recipw, &matid, &contained);
+        // the listed triangle passed transform_main_geom's culls in setup
+        const uint32_t k = min(sub, 2u);
+        float trans[16];
+        const uint32_t o = object_trans(P, nullptr, t, trans);
+        const V4 cp = mulv(trans, ld4(P.pos[t * 3 + k]));
+        const float rw = P.perspective ? __fdiv_rn(-1.0f, cp.w) : 1.0f;
+        const V4 sp = pos4(viewport_apply(P, cp));
+        const V4 nn = apply4_outline(ld4(P.nor[t * 3 + k]), P.obj_normal + o * 16);
+        if (sub < 3u) {
+            G.pos[k] = sp;
+            G.nor[k] = nn;
+            G.recipw[k] = rw;
+        }
+        int m = P.mat[t];
+        if (m >= 0) m += P.obj_matbase[o];
+        matid = m;
+    }
+    __syncwarp();
+    if (j < n) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            v[k].pos = G.pos[k];
+            v[k].nor = G.nor[k];
+            recipw[k] = G.recipw[k];
+            const float2 uv = P.uv[t * 3 + k];
+            v[k].u = uv.x;
+            v[k].v = uv.y;
+            v[k].col = pack_col(P.col[t * 3 + k]);
+        }
         V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
         nc = sutherland_hodgman(in3, ext_w(P), ext_h(P), clips);
         if (nc < 0) {
             atomicOr(&P.cnt->overflow, 4u);
             nc = 0;
+        }
+    }
+    const bool attrs = P.arec && !P.defer_attr;
+    if (nc > 2) {
+        const float psabc = sabc_of(v[0].pos.x, v[0].pos.y, v[1].pos.x, v[1].pos.y, v[2].pos.x, v[2].pos.y);
+        for (int i = (int)sub; i < nc; i += kClipLanes) {
+            const SubVtx cv = clip_vertex(clips[i], v, psabc);
+            G.cv[i] = cv;
+            if (attrs) G.mw[i] = world_of(P, cv.pos);
         }
     }
     __syncwarp();
@@ -647,12 +699,9 @@ PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint
             atomicMax(&P.cnt->need_rec, ridx + 1u);
         } else {
             if (sub == 0) P.first_rec[t] = ridx;
-            const float psabc = sabc_of(v[0].pos.x, v[0].pos.y, v[1].pos.x, v[1].pos.y, v[2].pos.x, v[2].pos.y);
-            SubVtx s[3];
-            s[0] = clip_vertex(clips[0], v, psabc);
-            s[1] = clip_vertex(clips[sub + 1], v, psabc);
-            s[2] = clip_vertex(clips[sub + 2], v, psabc);
-            area = write_sub(P, ridx, t * 8u + sub, s, recipw, matid);
+            const SubVtx s[3] = {G.cv[0], G.cv[sub + 1], G.cv[sub + 2]};
+            const V4 mw[3] = {G.mw[0], G.mw[sub + 1], G.mw[sub + 2]};
+            area = write_sub(P, ridx, t * 8u + sub, s, recipw, matid, attrs ? mw : nullptr);
             nw = 1;
         }
     }
@@ -661,9 +710,13 @@ PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint
 __global__ void __launch_bounds__(128) clip_kernel(const __grid_constant__ SetupParams P, const uint32_t* clip_list) {
     const uint32_t n = (P.cnt_rec ? P.cnt_rec : P.cnt)->n_clipped;
     constexpr uint32_t kPerBlock = 128 / kClipLanes;
+    __shared__ ClipGroupSm s_g[kPerBlock];
     // grid-stride over the list (uniform per block, so every warp calls clip_one_group whole)
-    for (uint32_t b = blockIdx.x * kPerBlock; b < n; b += gridDim.x * kPerBlock)
-        clip_one_group(P, clip_list, b + threadIdx.x / kClipLanes, n, threadIdx.x % kClipLanes);
+    for (uint32_t b = blockIdx.x * kPerBlock; b < n; b += gridDim.x * kPerBlock) {
+        clip_one_group(P, clip_list, b + threadIdx.x / kClipLanes, n, threadIdx.x % kClipLanes,
+                       s_g[threadIdx.x / kClipLanes]);
+        __syncwarp();  // the group's scratch is free for its next entry
+    }
 }
 
 // passShadows / drawDepth for one input triangle (render/shadow.go:137-192)
