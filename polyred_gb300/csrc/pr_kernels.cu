@@ -231,10 +231,10 @@ PR_DEV int sutherland_hodgman(const V4* in3, float w, float h, V4* out) {
         V4* o = buf[cur ^ 1];
         int m = 0;
         V4 s = inp[n - 1];
+        bool fs = dot4(sub4(s, P), N) > 0.0f;  // plane.pointInFront
         for (int i = 0; i < n; i++) {
             V4 e = inp[i];
-            bool fe = dot4(sub4(e, P), N) > 0.0f;  // plane.pointInFront
-            bool fs = dot4(sub4(s, P), N) > 0.0f;
+            const bool fe = dot4(sub4(e, P), N) > 0.0f;
             // A convex polygon gains at most one vertex per plane (<= 9 in
             // all); more means NaN coordinates broke convexity.
             if (m + (fe && !fs ? 2 : 1) > 9) return -1;
@@ -245,12 +245,71 @@ PR_DEV int sutherland_hodgman(const V4* in3, float w, float h, V4* out) {
                 o[m++] = intersect_segment(P, N, s, e);
             }
             s = e;
+            fs = fe;  // the same test of the same vertex
         }
         n = m;
         cur ^= 1;
     }
     for (int i = 0; i < n; i++) out[i] = buf[cur][i];
     return n;
+}
+
+// sutherland_hodgman over a group of kClipLanes (16) lanes, lane i holding
+// polygon vertex i (n <= 9 between planes). For each plane every lane
+// tests the edge from the previous vertex to its own, exactly as the loop
+// above does at step i, and places its 0, 1 or 2 output vertices at the
+// exclusive prefix sum of the counts, so each output polygon is the loop's,
+// vertex for vertex; the loop's overflow check at step i sees the same
+// prefix count. All 32 lanes of the warp call; a lane outside [0, n) holds
+// nothing. Returns the vertex count (or -1) to every lane of the group, and
+// lane i < count gets vertex i in *v. ring: the group's 2 x 10 vertices of
+// shared scratch.
+constexpr int kClipLanes = 16;  // >= 9 polygon vertices
+PR_DEV int sutherland_hodgman_group(V4* v, int n, float w, float h, uint32_t sub, V4 (*ring)[10]) {
+    const unsigned full = 0xffffffffu;
+    const uint32_t gbase = (threadIdx.x & 31u) & ~(uint32_t)(kClipLanes - 1);
+    const float pp[6][4] = {{w, 0, 0, 1}, {0, 0, 0, 1}, {0, h, 0, 1}, {0, 0, 0, 1}, {0, 0, 1, 1}, {0, 0, -1, 1}};
+    const float pn[6][4] = {{-1, 0, 0, 1}, {1, 0, 0, 1}, {0, -1, 0, 1}, {0, 1, 0, 1}, {0, 0, -1, 1}, {0, 0, 1, 1}};
+    int res = n;
+    for (int pl = 0; pl < 6; pl++) {
+        const V4 P = {pp[pl][0], pp[pl][1], pp[pl][2], pp[pl][3]};
+        const V4 N = {pn[pl][0], pn[pl][1], pn[pl][2], pn[pl][3]};
+        const bool act = (int)sub < n;  // n == 0 (an empty polygon, or a finished group): no lane acts
+        const V4 e = *v;
+        const bool fe = act && dot4(sub4(e, P), N) > 0.0f;
+        const int src = sub == 0u ? n - 1 : (int)sub - 1;  // the previous vertex (the last one for vertex 0)
+        V4 sv;
+        sv.x = __shfl_sync(full, e.x, src < 0 ? 0 : src, kClipLanes);
+        sv.y = __shfl_sync(full, e.y, src < 0 ? 0 : src, kClipLanes);
+        sv.z = __shfl_sync(full, e.z, src < 0 ? 0 : src, kClipLanes);
+        sv.w = __shfl_sync(full, e.w, src < 0 ? 0 : src, kClipLanes);
+        const bool fs = __shfl_sync(full, (int)fe, src < 0 ? 0 : src, kClipLanes) != 0;
+        const int cnt = !act ? 0 : fe ? (fs ? 1 : 2) : (fs ? 1 : 0);
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < kClipLanes; d <<= 1) {
+            const int t = __shfl_up_sync(full, incl, d, kClipLanes);
+            if ((int)sub >= d) incl += t;
+        }
+        const int m = incl - cnt;  // the loop's m at this step
+        const int total = __shfl_sync(full, incl, kClipLanes - 1, kClipLanes);
+        const bool over = act && m + (fe && !fs ? 2 : 1) > 9;
+        const bool any_over = ((__ballot_sync(full, over) >> gbase) & ((1u << kClipLanes) - 1u)) != 0u;
+        V4* o = ring[pl & 1];
+        if (act && !any_over) {
+            if (fe) {
+                if (!fs) o[m] = intersect_segment(P, N, sv, e);
+                o[m + (fs ? 0 : 1)] = e;
+            } else if (fs) {
+                o[m] = intersect_segment(P, N, sv, e);
+            }
+        }
+        __syncwarp();
+        if (n > 0) res = any_over ? -1 : total;
+        n = (n > 0 && !any_over) ? total : 0;
+        if ((int)sub < n) *v = o[sub];  // ring[pl & 1] is next written two planes on, after a sync
+    }
+    return res;
 }
 
 // Vec4.Apply kept out of line in the per-triangle setup kernels: a dozen
@@ -616,20 +675,20 @@ PR_DEV void clip_one(const SetupParams& P, const uint32_t* clip_list, uint32_t j
 
 // clip_one with the work spread over a group of kClipLanes lanes per listed
 // triangle. Lane k < 3 transforms vertex k (screen position, -1/W, normal);
-// every lane then clips the triangle (the same arithmetic, so the same
-// polygon); lane q re-interpolates polygon vertex q (and q + 8) with its
-// world position; lane `sub` assembles and writes fan sub-triangle sub. Each
-// value is the one clip_one computes, from the same inputs in the same
+// the group clips the triangle with one polygon vertex per lane
+// (sutherland_hodgman_group); lane q re-interpolates polygon vertex q with
+// its world position; lane `sub` assembles and writes fan sub-triangle sub.
+// Each value is the one clip_one computes, from the same inputs in the same
 // order; a warp just issues each per-vertex step once instead of once per
-// vertex (a frame's few clipped triangles are a serial chain, often on
-// cold instruction caches). The group's lanes reserve their records in lane
+// vertex (a frame's few clipped triangles are a serial chain, often on cold
+// instruction caches). The group's lanes reserve their records in lane
 // order, so its sub-triangles keep consecutive records from first_rec[t].
-constexpr int kClipLanes = 8;  // >= the most sub-triangles of a clipped triangle (9 vertices: 7)
 struct ClipGroupSm {
     V4 pos[3], nor[3];
     float recipw[3];
-    SubVtx cv[9];  // the polygon's re-interpolated vertices
-    V4 mw[9];      // and their world positions
+    V4 ring[2][10];  // the clipper's polygons
+    SubVtx cv[9];    // the polygon's re-interpolated vertices
+    V4 mw[9];        // and their world positions
 };
 PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint32_t j, uint32_t n, uint32_t sub,
                            ClipGroupSm& G) {
@@ -637,8 +696,6 @@ PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint
     float recipw[3];
     int matid = -1;
     uint32_t t = 0;
-    int nc = 0;
-    V4 clips[10];
     if (j < n) {
         t = clip_list[j];
         // the listed triangle passed transform_main_geom's culls in setup
@@ -659,6 +716,7 @@ PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint
         matid = m;
     }
     __syncwarp();
+    V4 pv = {0.0f, 0.0f, 0.0f, 0.0f};  // this lane's polygon vertex
     if (j < n) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -670,21 +728,19 @@ PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint
             v[k].v = uv.y;
             v[k].col = pack_col(P.col[t * 3 + k]);
         }
-        V4 in3[3] = {v[0].pos, v[1].pos, v[2].pos};
-        nc = sutherland_hodgman(in3, ext_w(P), ext_h(P), clips);
-        if (nc < 0) {
-            atomicOr(&P.cnt->overflow, 4u);
-            nc = 0;
-        }
+        pv = v[min(sub, 2u)].pos;
+    }
+    int nc = sutherland_hodgman_group(&pv, j < n ? 3 : 0, ext_w(P), ext_h(P), sub, G.ring);
+    if (nc < 0) {
+        if (sub == 0u) atomicOr(&P.cnt->overflow, 4u);
+        nc = 0;
     }
     const bool attrs = P.arec && !P.defer_attr;
-    if (nc > 2) {
+    if ((int)sub < nc && nc > 2) {
         const float psabc = sabc_of(v[0].pos.x, v[0].pos.y, v[1].pos.x, v[1].pos.y, v[2].pos.x, v[2].pos.y);
-        for (int i = (int)sub; i < nc; i += kClipLanes) {
-            const SubVtx cv = clip_vertex(clips[i], v, psabc);
-            G.cv[i] = cv;
-            if (attrs) G.mw[i] = world_of(P, cv.pos);
-        }
+        const SubVtx cv = clip_vertex(pv, v, psabc);
+        G.cv[sub] = cv;
+        if (attrs) G.mw[sub] = world_of(P, cv.pos);
     }
     __syncwarp();
     const bool mine = (int)sub < nc - 2;
@@ -699,9 +755,9 @@ PR_DEV void clip_one_group(const SetupParams& P, const uint32_t* clip_list, uint
             atomicMax(&P.cnt->need_rec, ridx + 1u);
         } else {
             if (sub == 0) P.first_rec[t] = ridx;
-            const SubVtx s[3] = {G.cv[0], G.cv[sub + 1], G.cv[sub + 2]};
+            const SubVtx s3[3] = {G.cv[0], G.cv[sub + 1], G.cv[sub + 2]};
             const V4 mw[3] = {G.mw[0], G.mw[sub + 1], G.mw[sub + 2]};
-            area = write_sub(P, ridx, t * 8u + sub, s, recipw, matid, attrs ? mw : nullptr);
+            area = write_sub(P, ridx, t * 8u + sub, s3, recipw, matid, attrs ? mw : nullptr);
             nw = 1;
         }
     }
