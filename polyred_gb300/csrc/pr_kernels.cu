@@ -1782,22 +1782,24 @@ __device__ __noinline__ float ao_settle_group(const int (*s_off)[kAoTable], cons
 }
 
 // The march of ao_fast_groups for frames without NaN depths, bookkept per
-// group of four taps: a group is a candidate when the largest upper bound of
-// its taps exceeds lb; it then raises lb by the largest lower bound of its
-// taps and becomes the pending group (bounded above by that largest upper
-// bound phi). A pending group is settled (its taps above lb evaluated
-// exactly) only when a later candidate's lower bound does not clear phi, and
-// at the end. Every tap above the final lb is thus evaluated exactly, and
-// best is the exact maximum.
+// unit of two groups of four taps (eight taps; a last odd group alone): a
+// unit is a candidate when the largest upper bound of its taps exceeds lb;
+// it then raises lb by the largest lower bound of its taps and becomes the
+// pending unit (bounded above by that largest upper bound phi). A pending
+// unit is settled (its taps above lb evaluated exactly, group by group) only
+// when a later candidate's lower bound does not clear phi, and at the end.
+// Every tap above the final lb is thus evaluated exactly, and best is the
+// exact maximum, whatever the unit's size; eight taps per unit halve the
+// candidate steps a warp issues (some lane of a warp is a candidate in most
+// units).
 template <bool TINY>
 PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const float (*s_rlo)[kAoTable],
                               const float (*s_rhi)[kAoTable], int k, const float* p0, const float* pA, int tstar,
                               float z, float pxf, float pyf, float dX, float dY, float& best) {
     float lb = best;
-    int pg = -1;
+    int pg = -1, pn = 0;  // pending unit: first group, group count
     float phi = 0.0f;
-#pragma unroll 2
-    for (int g = 0; g < n_groups; g++) {
+    auto tap_hi_lo = [&](int g, float& gh, float& gl_unused, float e[4]) {
         const int t0 = 4 * g + 2;
         const int4 o = *reinterpret_cast<const int4*>(&s_off[k][4 * g]);
         const float4 rh = *reinterpret_cast<const float4*>(&s_rhi[k][4 * g]);
@@ -1805,22 +1807,50 @@ PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const 
         const float* q1 = (TINY && t0 + 1 < tstar) ? pA : p0;
         const float* q2 = (TINY && t0 + 2 < tstar) ? pA : p0;
         const float* q3 = (TINY && t0 + 3 < tstar) ? pA : p0;
-        const float e0 = __fsub_rn(__ldg(q0 + o.x), z), e1 = __fsub_rn(__ldg(q1 + o.y), z);
-        const float e2 = __fsub_rn(__ldg(q2 + o.z), z), e3 = __fsub_rn(__ldg(q3 + o.w), z);
-        const float gh = fmaxf(fmaxf(__fmul_ru(e0, rh.x), __fmul_ru(e1, rh.y)), fmaxf(__fmul_ru(e2, rh.z), __fmul_ru(e3, rh.w)));
+        e[0] = __fsub_rn(__ldg(q0 + o.x), z);
+        e[1] = __fsub_rn(__ldg(q1 + o.y), z);
+        e[2] = __fsub_rn(__ldg(q2 + o.z), z);
+        e[3] = __fsub_rn(__ldg(q3 + o.w), z);
+        gh = fmaxf(fmaxf(__fmul_ru(e[0], rh.x), __fmul_ru(e[1], rh.y)), fmaxf(__fmul_ru(e[2], rh.z), __fmul_ru(e[3], rh.w)));
+        (void)gl_unused;
+    };
+    auto group_lo = [&](int g, const float e[4]) {
+        const float4 rl = *reinterpret_cast<const float4*>(&s_rlo[k][4 * g]);
+        return fmaxf(fmaxf(__fmul_rd(e[0], rl.x), __fmul_rd(e[1], rl.y)), fmaxf(__fmul_rd(e[2], rl.z), __fmul_rd(e[3], rl.w)));
+    };
+    auto settle = [&]() {
+        for (int q = 0; q < pn; q++)
+            best = fmaxf(best, ao_settle_group<TINY>(s_off, s_rhi, k, pg + q, p0, pA, tstar, z, pxf, pyf, dX, dY, lb));
+        lb = fmaxf(lb, best);
+    };
+    int g = 0;
+    for (; g + 1 < n_groups; g += 2) {
+        float ea[4], eb[4], ha, hb, unused = 0.0f;
+        tap_hi_lo(g, ha, unused, ea);
+        tap_hi_lo(g + 1, hb, unused, eb);
+        const float gh = fmaxf(ha, hb);
         if (gh > lb) {
-            const float4 rl = *reinterpret_cast<const float4*>(&s_rlo[k][4 * g]);
-            const float gl = fmaxf(fmaxf(__fmul_rd(e0, rl.x), __fmul_rd(e1, rl.y)), fmaxf(__fmul_rd(e2, rl.z), __fmul_rd(e3, rl.w)));
+            const float gl = fmaxf(group_lo(g, ea), group_lo(g + 1, eb));
             lb = fmaxf(lb, gl);
-            if (pg >= 0 && gl < phi) {
-                best = fmaxf(best, ao_settle_group<TINY>(s_off, s_rhi, k, pg, p0, pA, tstar, z, pxf, pyf, dX, dY, lb));
-                lb = fmaxf(lb, best);
-            }
+            if (pg >= 0 && gl < phi) settle();
             pg = g;
+            pn = 2;
             phi = gh;
         }
     }
-    if (pg >= 0) best = fmaxf(best, ao_settle_group<TINY>(s_off, s_rhi, k, pg, p0, pA, tstar, z, pxf, pyf, dX, dY, lb));
+    if (g < n_groups) {  // the last group alone
+        float e[4], gh, unused = 0.0f;
+        tap_hi_lo(g, gh, unused, e);
+        if (gh > lb) {
+            const float gl = group_lo(g, e);
+            lb = fmaxf(lb, gl);
+            if (pg >= 0 && gl < phi) settle();
+            pg = g;
+            pn = 1;
+            phi = gh;
+        }
+    }
+    if (pg >= 0) settle();
 }
 
 // AmbientOcclusionShade (material/ao.go:20-73) for the pixels the shade
