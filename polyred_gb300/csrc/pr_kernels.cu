@@ -1799,7 +1799,8 @@ PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const 
     float lb = best;
     int pg = -1, pn = 0;  // pending unit: first group, group count
     float phi = 0.0f;
-    auto tap_hi_lo = [&](int g, float& gh, float& gl_unused, float e[4]) {
+    // the elevations of group g's taps and the largest upper bound of their ratios
+    auto group_hi = [&](int g, float& gh, float e[4]) {
         const int t0 = 4 * g + 2;
         const int4 o = *reinterpret_cast<const int4*>(&s_off[k][4 * g]);
         const float4 rh = *reinterpret_cast<const float4*>(&s_rhi[k][4 * g]);
@@ -1812,7 +1813,6 @@ PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const 
         e[2] = __fsub_rn(__ldg(q2 + o.z), z);
         e[3] = __fsub_rn(__ldg(q3 + o.w), z);
         gh = fmaxf(fmaxf(__fmul_ru(e[0], rh.x), __fmul_ru(e[1], rh.y)), fmaxf(__fmul_ru(e[2], rh.z), __fmul_ru(e[3], rh.w)));
-        (void)gl_unused;
     };
     auto group_lo = [&](int g, const float e[4]) {
         const float4 rl = *reinterpret_cast<const float4*>(&s_rlo[k][4 * g]);
@@ -1824,10 +1824,11 @@ PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const 
         lb = fmaxf(lb, best);
     };
     int g = 0;
+#pragma unroll 2
     for (; g + 1 < n_groups; g += 2) {
-        float ea[4], eb[4], ha, hb, unused = 0.0f;
-        tap_hi_lo(g, ha, unused, ea);
-        tap_hi_lo(g + 1, hb, unused, eb);
+        float ea[4], eb[4], ha, hb;
+        group_hi(g, ha, ea);
+        group_hi(g + 1, hb, eb);
         const float gh = fmaxf(ha, hb);
         if (gh > lb) {
             const float gl = fmaxf(group_lo(g, ea), group_lo(g + 1, eb));
@@ -1839,8 +1840,8 @@ PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const 
         }
     }
     if (g < n_groups) {  // the last group alone
-        float e[4], gh, unused = 0.0f;
-        tap_hi_lo(g, gh, unused, e);
+        float e[4], gh;
+        group_hi(g, gh, e);
         if (gh > lb) {
             const float gl = group_lo(g, e);
             lb = fmaxf(lb, gl);
@@ -2022,8 +2023,10 @@ PR_DEV void ao_finish(const AoParams& P, uint32_t i, float T) {
     P.rgba[i] = make_uchar4(o.x, o.y, o.z, c.w);
 }
 
+// 4 blocks per SM (up to 64 registers): the march's eight-tap units, two
+// at a time, keep sixteen depth loads in flight per thread without spills.
 template <bool kApply>
-__global__ void __launch_bounds__(kAoThreads, 5) ao_kernel(const __grid_constant__ AoParams P) {
+__global__ void __launch_bounds__(kAoThreads, 4) ao_kernel(const __grid_constant__ AoParams P) {
     __shared__ __align__(16) int s_off[8][kAoTable];
     __shared__ __align__(16) float s_rlo[8][kAoTable];
     __shared__ __align__(16) float s_rhi[8][kAoTable];
