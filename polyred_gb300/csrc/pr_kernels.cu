@@ -1791,8 +1791,9 @@ __device__ __noinline__ float ao_settle_group(const int (*s_off)[kAoTable], cons
 // Every tap above the final lb is thus evaluated exactly, and best is the
 // exact maximum, whatever the unit's size; eight taps per unit halve the
 // candidate steps a warp issues (some lane of a warp is a candidate in most
-// units).
-template <bool TINY>
+// units). UNROLL: the unit loop unrolled by two (the single-view kernel, at
+// 64 registers; the batched kernel keeps one unit at a time).
+template <bool TINY, bool UNROLL>
 PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const float (*s_rlo)[kAoTable],
                               const float (*s_rhi)[kAoTable], int k, const float* p0, const float* pA, int tstar,
                               float z, float pxf, float pyf, float dX, float dY, float& best) {
@@ -1824,7 +1825,7 @@ PR_DEV void ao_fast_groups_nf(int n_groups, const int (*s_off)[kAoTable], const 
         lb = fmaxf(lb, best);
     };
     int g = 0;
-#pragma unroll 2
+#pragma unroll(UNROLL ? 2 : 1)
     for (; g + 1 < n_groups; g += 2) {
         float ea[4], eb[4], ha, hb;
         group_hi(g, ha, ea);
@@ -1979,11 +1980,12 @@ PR_DEV void ao_one(const AoParams& P, uint32_t j, const int (*s_off)[kAoTable], 
                 }
                 const float* pA = p0 + (tiny == 1 ? 1 : -W);
                 if (nan_free)
-                    ao_fast_groups_nf<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
+                    ao_fast_groups_nf<true, !kApply>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY,
+                                                     best);
                 else
                     ok = ao_fast_groups<true>(n_groups, s_off, s_rlo, s_rhi, k, p0, pA, lo, z, pxf, pyf, dX, dY, best);
             } else if (nan_free) {
-                ao_fast_groups_nf<false>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
+                ao_fast_groups_nf<false, !kApply>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
             } else {
                 ok = ao_fast_groups<false>(n_groups, s_off, s_rlo, s_rhi, k, p0, p0, 0, z, pxf, pyf, dX, dY, best);
             }
