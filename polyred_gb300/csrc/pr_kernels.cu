@@ -1072,8 +1072,9 @@ __global__ void __launch_bounds__(kRasterWarps * 32, 6) raster_kernel(const __gr
         // where larger grabs would leave warps without work
         // The early depth test pays on passes with many fragments per pixel;
         // on short lists its extra read only lengthens each warp's chain.
-        // A list of fewer than grab tasks per warp (a small frame: a few
-        // thousand tasks, mostly from one or two large triangles) is spread
+        // A list of fewer than kSpreadShare (and fewer than grab) tasks per
+        // warp (a small frame: a few thousand tasks, mostly from one or two
+        // large triangles; a 2048^2 shadow pass) is spread
         // over every warp instead, down to one task each, by warp index: the
         // pass then lasts one or two small batches rather than grab tasks in
         // a few warps, and no warp waits on the counter. Its batches being
