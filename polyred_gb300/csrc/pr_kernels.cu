@@ -617,7 +617,9 @@ PR_DEV void setup_main_one(const SetupParams& P, const ObjCache* C, uint32_t t, 
     }
     emit_tasks_warp(P, &ridx, &area, 1);
 }
-__global__ void __launch_bounds__(128) setup_main_kernel(const __grid_constant__ SetupParams P, uint32_t* clip_list) {
+// 8 blocks per SM (64 registers, a few spilled on rare paths): more warps to
+// hide the per-triangle loads and stores measured faster than 80 registers at 6.
+__global__ void __launch_bounds__(128, 8) setup_main_kernel(const __grid_constant__ SetupParams P, uint32_t* clip_list) {
     __shared__ ObjCache C;
     if (!P.obj_trans) obj_cache_fill(P, blockIdx.x * blockDim.x, C);  // uniform
     setup_main_one(P, &C, blockIdx.x * blockDim.x + threadIdx.x, clip_list);
