@@ -814,7 +814,8 @@ PR_DEV void setup_shadow_one(const SetupParams& P, const ObjCache* C, uint32_t t
     uint32_t ridx = t;
     emit_tasks_warp(P, &ridx, &area, ok ? 1 : 0);
 }
-__global__ void __launch_bounds__(128) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
+// 9 blocks per SM (56 registers): more warps than at 62 registers and 8.
+__global__ void __launch_bounds__(128, 9) setup_shadow_kernel(const __grid_constant__ SetupParams P) {
     __shared__ ObjCache C;
     if (!P.obj_trans) obj_cache_fill(P, blockIdx.x * blockDim.x, C);  // uniform
     setup_shadow_one(P, &C, blockIdx.x * blockDim.x + threadIdx.x);
@@ -1633,7 +1634,9 @@ PR_DEV void ao_append_tile(const ShadeParams& P, bool pending, uint32_t i) {
     }
 }
 template <bool kTex>
-__global__ void __launch_bounds__(256) shade_kernel(const __grid_constant__ ShadeParams P) {
+// 4 blocks per SM (64 registers, a few spilled): 32 warps to hide the
+// record, attribute and shadow-map loads measured faster than 80 registers at 3.
+__global__ void __launch_bounds__(256, 4) shade_kernel(const __grid_constant__ ShadeParams P) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
     const bool pending = shade_one<kTex>(P, x, r);
     if (P.ao_list && !P.ao_listed) ao_append_tile(P, pending, (uint32_t)r * (uint32_t)P.W + (uint32_t)x);
