@@ -73,3 +73,18 @@ def test_hostmath_matches_library_on_random_inputs(native_lib, oracle_lib):
         v1, p1 = pmath.shadow_camera(lp, tgt, cv, cp)
         v2, p2 = hostmath.shadow_camera(lp, tgt, cv, cp)
         assert same(v1, v2) and same(p1, p2)
+
+
+def test_bench_reads_the_committed_ao_profile():
+    """The bench's roofline line takes the AO kernel's DRAM traffic and
+    instruction count from its committed ncu summary: both parse, and the
+    summary's issue-rate arithmetic matches its own figures."""
+    import re
+    import bench
+    traffic, inst = bench.ncu_traffic(), bench.ncu_instructions()
+    assert traffic is not None and 1e6 < traffic < 1e9, traffic
+    assert inst is not None and 1e7 < inst < 1e10, inst
+    text = open(os.path.join(ROOT, "profiles", "ao_kernel_sphere_field_1080p.txt")).read()
+    dur = float(re.search(r"^duration_us: ([0-9.]+)", text, re.M).group(1))
+    stated = float(re.search(r"fraction of its own time: .* = ([0-9.]+)\.", text).group(1))
+    assert abs(inst / (152 * 4 * 2.07e9 * dur * 1e-6) - stated) < 0.01, (inst, dur, stated)
