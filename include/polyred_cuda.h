@@ -341,8 +341,8 @@ int pr_shadow_camera(const float light_pos[3], const float scene_center[3],
  * width*height <= PR_NOALLOC_MAX_TEXELS, raster tasks (1024-pixel chunks of
  * the triangles' pixel boxes) <= PR_NOALLOC_MAX_TASKS.
  *
- * The first call on a device looks up the array's device address, so make
- * that call before any stream capture. Every call uses the same array: calls
+ * The first call on a device looks up the array's device address. Every
+ * call uses the same array: calls
  * whose work overlaps on the GPU (other streams, other host threads) race and
  * corrupt each other. The call returns when its work on `stream` is done.
  */
